@@ -1,0 +1,273 @@
+"""aboria_gb300: the GB300 (sm_103a) particle hot path behind Aboria's API.
+
+Python mirror of the reference's operator interface over the C ABI declared
+in ``include/abx.h`` (ctypes, no torch types in the boundary).  Names follow
+the reference: ``Particles`` with ``init_neighbour_search``,
+``euclidean_search`` counts/lists, ``create_sparse_operator``,
+``create_dense_operator`` and ``K * b``.
+
+Vector arguments may be numpy arrays (host memory) or CUDA tensors / any
+object exposing ``data_ptr()`` (device memory); the library stages host
+buffers itself.  There is no CPU fallback: if the CUDA library cannot be
+loaded every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+from ._lib import ABXError, lib, load_library  # noqa: F401
+
+__all__ = [
+    "ABXError", "Context", "Particles", "Kernel", "Operator", "create_sparse_operator",
+    "create_dense_operator", "radius_count", "radius_query_csr", "PREC_FP64", "PREC_MIXED",
+    "K_CONST", "K_GAUSSIAN", "K_WENDLAND_C2", "K_COMPACT_GAUSSIAN", "K_LAPLACE",
+    "K_MULTIQUADRIC", "K_SCALAR_SUM", "default_context",
+]
+
+PREC_FP64, PREC_MIXED = 0, 1
+(K_CONST, K_GAUSSIAN, K_WENDLAND_C2, K_COMPACT_GAUSSIAN, K_LAPLACE, K_MULTIQUADRIC,
+ K_SCALAR_SUM) = range(7)
+
+
+def _ptr(a):
+    """Raw pointer of a numpy array (host) or a tensor-like (device)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("arrays must be C-contiguous")
+        return C.c_void_p(a.ctypes.data)
+    if hasattr(a, "data_ptr"):
+        if hasattr(a, "is_contiguous") and not a.is_contiguous():
+            raise ValueError("tensors must be contiguous")
+        return C.c_void_p(a.data_ptr())
+    raise TypeError(f"unsupported array type {type(a)!r}")
+
+
+def _check(status, what="abx call"):
+    if status != 0:
+        msg = lib().abx_last_error().decode(errors="replace")
+        raise ABXError(status, f"{what} failed ({status}): {msg}")
+
+
+class Context:
+    """One device and one stream (``abx_context``)."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        self._h = C.c_void_p()
+        _check(lib().abx_context_create(device, C.c_void_p(stream or 0), C.byref(self._h)),
+               "abx_context_create")
+
+    def synchronize(self):
+        _check(lib().abx_context_synchronize(self._h), "abx_context_synchronize")
+
+    def close(self):
+        if self._h:
+            lib().abx_context_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(int(os.environ.get("ABX_DEVICE", "0")))
+    return _default_ctx
+
+
+class Particles:
+    """``Particles<std::tuple<scalar>, D>`` (src/Particles.h:108-112)."""
+
+    def __init__(self, dim: int = 3, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.dim = dim
+        self._h = C.c_void_p()
+        _check(lib().abx_particles_create(self.ctx._h, dim, C.byref(self._h)),
+               "abx_particles_create")
+
+    def __del__(self):
+        try:
+            if self._h:
+                lib().abx_particles_destroy(self._h)
+        except Exception:
+            pass
+
+    def __len__(self):
+        return int(lib().abx_particles_size(self._h))
+
+    def set(self, pos, ids=None):
+        """Replace the contents with ``len(pos)`` particles (like push_back)."""
+        n = int(pos.shape[0])
+        if isinstance(pos, np.ndarray):
+            pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(n, self.dim)
+        if ids is not None and isinstance(ids, np.ndarray):
+            ids = np.ascontiguousarray(ids, dtype=np.int64)
+        _check(lib().abx_particles_set(self._h, n, _ptr(pos), _ptr(ids)), "abx_particles_set")
+        return self
+
+    def set_scalar(self, s):
+        if isinstance(s, np.ndarray):
+            s = np.ascontiguousarray(s, dtype=np.float64)
+        _check(lib().abx_particles_set_scalar(self._h, _ptr(s)), "abx_particles_set_scalar")
+
+    def set_positions(self, pos):
+        if isinstance(pos, np.ndarray):
+            pos = np.ascontiguousarray(pos, dtype=np.float64)
+        _check(lib().abx_particles_set_positions(self._h, _ptr(pos)),
+               "abx_particles_set_positions")
+
+    def init_neighbour_search(self, lo, hi, periodic, n_particles_in_leaf: float = 10.0):
+        lo = np.ascontiguousarray(lo, dtype=np.float64)
+        hi = np.ascontiguousarray(hi, dtype=np.float64)
+        per = np.ascontiguousarray([1 if p else 0 for p in periodic], dtype=np.int32)
+        _check(lib().abx_particles_init_neighbour_search(self._h, _ptr(lo), _ptr(hi), _ptr(per),
+                                                         float(n_particles_in_leaf)),
+               "abx_particles_init_neighbour_search")
+        return self
+
+    def update_positions(self):
+        _check(lib().abx_particles_update_positions(self._h), "abx_particles_update_positions")
+
+    @property
+    def positions(self) -> np.ndarray:
+        out = np.empty((len(self), self.dim), dtype=np.float64)
+        _check(lib().abx_particles_get_positions(self._h, _ptr(out)), "get_positions")
+        return out
+
+    @property
+    def ids(self) -> np.ndarray:
+        out = np.empty(len(self), dtype=np.int64)
+        _check(lib().abx_particles_get_ids(self._h, _ptr(out)), "get_ids")
+        return out
+
+    @property
+    def scalar(self) -> np.ndarray:
+        out = np.empty(len(self), dtype=np.float64)
+        _check(lib().abx_particles_get_scalar(self._h, _ptr(out)), "get_scalar")
+        return out
+
+    def grid(self):
+        size = np.zeros(self.dim, dtype=np.uint32)
+        side = np.zeros(self.dim, dtype=np.float64)
+        nc = C.c_uint32()
+        _check(lib().abx_particles_get_grid(self._h, _ptr(size), _ptr(side), C.byref(nc)),
+               "get_grid")
+        return size, side, int(nc.value)
+
+    def buckets(self):
+        _, _, nc = self.grid()
+        bb = np.empty(nc, dtype=np.uint32)
+        be = np.empty(nc, dtype=np.uint32)
+        keys = np.empty(len(self), dtype=np.uint32)
+        _check(lib().abx_particles_get_buckets(self._h, _ptr(bb), _ptr(be), _ptr(keys)),
+               "get_buckets")
+        return bb, be, keys
+
+
+def radius_count(p: Particles, q, r: float, out=None):
+    """Neighbour counts of ``euclidean_search(p.get_query(), q_i, r)``."""
+    nq = int(q.shape[0])
+    if isinstance(q, np.ndarray):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+    if out is None:
+        out = np.empty(nq, dtype=np.int32)
+    _check(lib().abx_radius_count(p._h, nq, _ptr(q), float(r), _ptr(out)), "abx_radius_count")
+    return out
+
+
+def radius_query_csr(p: Particles, q, r: float):
+    """Neighbour lists (storage indices) as CSR ``(rowptr, cols)``."""
+    nq = int(q.shape[0])
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    rowptr = np.empty(nq + 1, dtype=np.int64)
+    _check(lib().abx_radius_query_csr(p._h, nq, _ptr(q), float(r), _ptr(rowptr), None, 0),
+           "abx_radius_query_csr")
+    nnz = int(rowptr[-1])
+    cols = np.empty(max(nnz, 1), dtype=np.int32)
+    _check(lib().abx_radius_query_csr(p._h, nq, _ptr(q), float(r), _ptr(rowptr), _ptr(cols), nnz),
+           "abx_radius_query_csr")
+    return rowptr, cols[:nnz]
+
+
+class Kernel(C.Structure):
+    _fields_ = [("kind", C.c_int), ("p", C.c_double * 4)]
+
+    @classmethod
+    def make(cls, kind: int, *params: float) -> "Kernel":
+        k = cls()
+        k.kind = kind
+        for i, v in enumerate(params[:4]):
+            k.p[i] = float(v)
+        return k
+
+
+class Operator:
+    """``MatrixReplacement``: ``K * b`` returns ``c = K b``."""
+
+    def __init__(self, h, rows: Particles, cols: Particles):
+        self._h = h
+        self.rows, self.cols = rows, cols  # held by reference, as the reference does
+
+    def __del__(self):
+        try:
+            if self._h:
+                lib().abx_operator_destroy(self._h)
+        except Exception:
+            pass
+
+    def set_precision(self, mode: int):
+        _check(lib().abx_operator_set_precision(self._h, mode), "set_precision")
+        return self
+
+    @property
+    def shape(self):
+        return (int(lib().abx_operator_rows(self._h)), int(lib().abx_operator_cols(self._h)))
+
+    def matvec(self, b, out=None, sync=True):
+        """``c = K b``.  Host (numpy) results are complete on return; device
+        results are synchronised with the context stream unless sync=False."""
+        nr, nc = self.shape
+        if isinstance(b, np.ndarray):
+            b = np.ascontiguousarray(b, dtype=np.float64)
+            if b.shape[0] != nc:
+                raise ValueError(f"rhs has {b.shape[0]} rows, operator has {nc} columns")
+            if out is None:
+                out = np.empty(nr, dtype=np.float64)
+        elif out is None:
+            import torch  # device tensors only
+            out = torch.empty(nr, dtype=torch.float64, device=b.device)
+        _check(lib().abx_operator_matvec(self._h, _ptr(b), _ptr(out)), "abx_operator_matvec")
+        if sync and not isinstance(out, np.ndarray):
+            self.rows.ctx.synchronize()
+        return out
+
+    def __mul__(self, b):
+        return self.matvec(b)
+
+
+def create_sparse_operator(rows: Particles, cols: Particles, radius: float, kernel: Kernel,
+                           precision: int = PREC_FP64) -> Operator:
+    h = C.c_void_p()
+    _check(lib().abx_create_sparse_operator(rows._h, cols._h, float(radius), C.byref(kernel),
+                                            C.byref(h)), "abx_create_sparse_operator")
+    return Operator(h, rows, cols).set_precision(precision)
+
+
+def create_dense_operator(rows: Particles, cols: Particles, kernel: Kernel,
+                          precision: int = PREC_FP64) -> Operator:
+    h = C.c_void_p()
+    _check(lib().abx_create_dense_operator(rows._h, cols._h, C.byref(kernel), C.byref(h)),
+           "abx_create_dense_operator")
+    return Operator(h, rows, cols).set_precision(precision)

@@ -1,0 +1,80 @@
+// Handle types behind the C ABI: particle sets with their cell list, and
+// operators with their pair layout.
+#pragma once
+
+#include "common.cuh"
+
+namespace abx {
+
+// Grow-only staging for one vector argument that may be host memory.
+struct HostStage {
+  DevBuf<unsigned char> buf;
+  bool host_ = false;
+  int in(abx_context *ctx, const void *user, size_t bytes, const void **dev);
+  int out(abx_context *ctx, void *user, size_t bytes, void **dev);
+  int finish(abx_context *ctx, void *user, size_t bytes);
+};
+
+// The CellListOrdered grid (src/CellListOrdered.h:132-186), padded to 3
+// dimensions: unused dimensions have size 1, side 1, and coordinate 0.
+struct GridDesc {
+  int dim;
+  double lo[3], hi[3];
+  int periodic[3];
+  uint32_t size[3];
+  double side[3];
+  double inv_side[3];
+  uint32_t ncells;
+};
+
+}  // namespace abx
+
+struct abx_particles {
+  abx_context *ctx = nullptr;
+  int dim = 3;
+  int64_t n = 0;
+  // Storage in the current order; positions are SoA: pos[d*n + i].
+  abx::DevBuf<double> pos, pos_alt;
+  abx::DevBuf<int64_t> ids, ids_alt;
+  abx::DevBuf<double> scalar, scalar_alt;
+  bool has_scalar = false;
+  int64_t next_id = 0;
+  // Neighbour search state.
+  bool domain_set = false;
+  bool searchable = false;
+  abx::GridDesc grid{};
+  double n_leaf = 10.0;
+  size_t size_calculated_with_n = (size_t)-1;  // CellListOrdered.h:106
+  int64_t n_alive_prev = 0;                     // m_alive_indices.size()
+  abx::DevBuf<uint32_t> keys;                   // sorted bucket key per particle
+  abx::DevBuf<uint32_t> bucket_begin, bucket_end;
+  uint64_t version = 0;  // bumped by every rebuild; operators check it
+  abx::HostStage stage_a, stage_b;
+};
+
+namespace abx {
+struct PairLayout;   // pairs.cu
+struct DenseLayout;  // dense.cu
+}  // namespace abx
+
+struct abx_operator {
+  int kind = 0;  // 0 sparse, 1 dense
+  abx_particles *rows = nullptr, *cols = nullptr;
+  uint64_t rows_version = 0, cols_version = 0;
+  double radius = 0.0;
+  abx_kernel k{};
+  int precision = ABX_PREC_FP64;
+  abx::PairLayout *pairs = nullptr;
+  abx::HostStage stage_b, stage_c;
+  int64_t last_candidates = 0, last_pairs = 0;
+};
+
+namespace abx {
+int particles_grid_desc(const abx_particles *p, GridDesc *g);
+// pairs.cu
+int pair_layout_build(abx_operator *op);
+void pair_layout_free(PairLayout *L);
+int sparse_matvec_device(abx_operator *op, const double *b, double *c);
+// dense.cu
+int dense_matvec_device(abx_operator *op, const double *b, double *c);
+}  // namespace abx

@@ -1,0 +1,289 @@
+// Kernel operators: create_sparse_operator / create_dense_operator and K*b.
+//
+// Reference: MatrixReplacement (src/Operators.h:75-281) with the Eigen product
+// specialisation generic_product_impl::scaleAndAddTo
+// (src/detail/Operators.h:207-229), which zero-initialises the destination and
+// calls KernelX::evaluate.  The dense kernel restates KernelDense::evaluate
+// (src/Kernels.h:212-239): for each row i, in column order j = 0..n-1,
+// c_i += f(a_i, b_j) * b_j.  Each thread owns one row and walks the columns in
+// exactly that order, so the FP64 mode reproduces the reference's summation
+// order; columns are staged through shared memory 256 at a time.
+#include <cmath>
+
+#include "common.cuh"
+#include "handles.cuh"
+
+namespace abx {
+namespace {
+
+constexpr int DT = 256;  // rows per CTA = staged columns per tile
+
+struct DenseParams {
+  int dim, kind;
+  double p0;
+  float p0f, c_exp2;
+  int64_t nr, nc;
+  const double *rpos, *cpos;  // SoA storage order
+  const double *b;
+  const double *s_row, *s_col;
+  double *c;
+  double origin[3];
+};
+
+template <int KIND> __device__ __forceinline__ double dk64(double d2, double p0, double si,
+                                                           double sj) {
+  if (KIND == ABX_K_CONST) return p0;
+  if (KIND == ABX_K_GAUSSIAN || KIND == ABX_K_COMPACT_GAUSSIAN) return exp(-d2 * p0);
+  if (KIND == ABX_K_WENDLAND_C2) {
+    const double q = sqrt(d2) * p0;
+    if (q >= 1.0) return 0.0;
+    const double t = 1.0 - q;
+    const double t2 = t * t;
+    return t2 * t2 * (4.0 * q + 1.0);
+  }
+  if (KIND == ABX_K_LAPLACE) return 1.0 / (sqrt(d2) + p0);
+  if (KIND == ABX_K_MULTIQUADRIC) return sqrt(d2 + p0);
+  if (KIND == ABX_K_SCALAR_SUM) return si + sj;
+  return 0.0;
+}
+
+template <int KIND> __device__ __forceinline__ float dk32(float d2, float p0f, float c_exp2) {
+  if (KIND == ABX_K_CONST) return p0f;
+  if (KIND == ABX_K_GAUSSIAN || KIND == ABX_K_COMPACT_GAUSSIAN) return exp2f(d2 * c_exp2);
+  if (KIND == ABX_K_WENDLAND_C2) {
+    const float q = d2 * rsqrtf(fmaxf(d2, 1e-36f)) * p0f;
+    const float t = fmaxf(1.0f - q, 0.0f);
+    const float t2 = t * t;
+    return t2 * t2 * fmaf(4.0f, q, 1.0f);
+  }
+  if (KIND == ABX_K_LAPLACE) return __fdividef(1.0f, d2 * rsqrtf(fmaxf(d2, 1e-36f)) + p0f);
+  if (KIND == ABX_K_MULTIQUADRIC) {
+    const float a = d2 + p0f;
+    return a * rsqrtf(fmaxf(a, 1e-36f));
+  }
+  return 0.f;
+}
+
+template <int KIND> __global__ void __launch_bounds__(DT) k_dense_fp64(DenseParams P) {
+  __shared__ double sx[DT], sy[DT], sz[DT], sb[DT], ss[DT];
+  const int64_t i = (int64_t)blockIdx.x * DT + threadIdx.x;
+  const bool act = i < P.nr;
+  double xi[3] = {0, 0, 0};
+  if (act)
+    for (int d = 0; d < P.dim; ++d) xi[d] = P.rpos[(int64_t)d * P.nr + i];
+  const double si = (KIND == ABX_K_SCALAR_SUM && act) ? P.s_row[i] : 0.0;
+  double acc = 0.0;
+  for (int64_t t = 0; t < P.nc; t += DT) {
+    const int64_t j = t + threadIdx.x;
+    if (j < P.nc) {
+      sx[threadIdx.x] = P.cpos[j];
+      sy[threadIdx.x] = P.dim > 1 ? P.cpos[P.nc + j] : 0.0;
+      sz[threadIdx.x] = P.dim > 2 ? P.cpos[2 * P.nc + j] : 0.0;
+      sb[threadIdx.x] = P.b[j];
+      ss[threadIdx.x] = (KIND == ABX_K_SCALAR_SUM) ? P.s_col[j] : 0.0;
+    }
+    __syncthreads();
+    const int nt = (int)((P.nc - t) < DT ? (P.nc - t) : DT);
+    for (int jj = 0; jj < nt; ++jj) {
+      const double pj[3] = {sx[jj], sy[jj], sz[jj]};
+      double d2 = 0.0;
+      for (int d = 0; d < P.dim; ++d) {
+        const double dx = __dsub_rn(pj[d], xi[d]);
+        d2 = __dadd_rn(d2, __dmul_rn(dx, dx));
+      }
+      acc = __dadd_rn(acc, __dmul_rn(dk64<KIND>(d2, P.p0, si, ss[jj]), sb[jj]));
+    }
+    __syncthreads();
+  }
+  if (act) P.c[i] = acc;
+}
+
+template <int KIND> __global__ void __launch_bounds__(DT) k_dense_mixed(DenseParams P) {
+  __shared__ float4 sp[DT];
+  const int64_t i = (int64_t)blockIdx.x * DT + threadIdx.x;
+  const bool act = i < P.nr;
+  float xi[3] = {0.f, 0.f, 0.f};
+  if (act)
+    for (int d = 0; d < P.dim; ++d) xi[d] = (float)(P.rpos[(int64_t)d * P.nr + i] - P.origin[d]);
+  double acc = 0.0;
+  for (int64_t t = 0; t < P.nc; t += DT) {
+    const int64_t j = t + threadIdx.x;
+    if (j < P.nc) {
+      float4 v;
+      v.x = (float)(P.cpos[j] - P.origin[0]);
+      v.y = P.dim > 1 ? (float)(P.cpos[P.nc + j] - P.origin[1]) : 0.f;
+      v.z = P.dim > 2 ? (float)(P.cpos[2 * P.nc + j] - P.origin[2]) : 0.f;
+      v.w = (float)P.b[j];
+      sp[threadIdx.x] = v;
+    }
+    __syncthreads();
+    const int nt = (int)((P.nc - t) < DT ? (P.nc - t) : DT);
+    float a32 = 0.f;
+    for (int jj = 0; jj < nt; ++jj) {
+      const float4 v = sp[jj];
+      const float d0 = v.x - xi[0], d1 = v.y - xi[1], d2v = v.z - xi[2];
+      const float dd = fmaf(d2v, d2v, fmaf(d1, d1, d0 * d0));
+      a32 = fmaf(dk32<KIND>(dd, P.p0f, P.c_exp2), v.w, a32);
+    }
+    acc += (double)a32;
+    __syncthreads();
+  }
+  if (act) P.c[i] = acc;
+}
+
+template <int KIND> int launch_dense(abx_context *ctx, const DenseParams &P, bool mixed) {
+  const unsigned blocks = ceil_div(P.nr, DT);
+  if (mixed && KIND != ABX_K_SCALAR_SUM)
+    k_dense_mixed<KIND><<<blocks, DT, 0, ctx->stream>>>(P);
+  else
+    k_dense_fp64<KIND><<<blocks, DT, 0, ctx->stream>>>(P);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  return ABX_OK;
+}
+
+}  // namespace
+
+int dense_matvec_device(abx_operator *op, const double *b, double *c) {
+  abx_context *ctx = op->rows->ctx;
+  DenseParams P{};
+  P.dim = op->rows->dim;
+  P.kind = op->k.kind;
+  P.p0 = op->k.p[0];
+  P.p0f = (float)op->k.p[0];
+  P.c_exp2 = (float)(-op->k.p[0] * 1.4426950408889634);
+  P.nr = op->rows->n;
+  P.nc = op->cols->n;
+  P.rpos = op->rows->pos.ptr;
+  P.cpos = op->cols->pos.ptr;
+  P.b = b;
+  P.c = c;
+  if (P.kind == ABX_K_SCALAR_SUM) {
+    ABX_REQUIRE(op->rows->has_scalar && op->cols->has_scalar, ABX_ERR_STATE,
+                "ABX_K_SCALAR_SUM needs a scalar column on both particle sets");
+    P.s_row = op->rows->scalar.ptr;
+    P.s_col = op->cols->scalar.ptr;
+  }
+  // FP32 coordinates are taken relative to the column domain centre when a
+  // domain is set, else to the origin.
+  for (int d = 0; d < 3; ++d) P.origin[d] = 0.0;
+  if (op->cols->domain_set)
+    for (int d = 0; d < P.dim; ++d)
+      P.origin[d] = 0.5 * (op->cols->grid.lo[d] + op->cols->grid.hi[d]);
+  if (P.nr == 0) return ABX_OK;
+  const bool mixed = op->precision == ABX_PREC_MIXED;
+  switch (P.kind) {
+  case ABX_K_CONST: return launch_dense<ABX_K_CONST>(ctx, P, mixed);
+  case ABX_K_GAUSSIAN: return launch_dense<ABX_K_GAUSSIAN>(ctx, P, mixed);
+  case ABX_K_WENDLAND_C2: return launch_dense<ABX_K_WENDLAND_C2>(ctx, P, mixed);
+  case ABX_K_COMPACT_GAUSSIAN: return launch_dense<ABX_K_COMPACT_GAUSSIAN>(ctx, P, mixed);
+  case ABX_K_LAPLACE: return launch_dense<ABX_K_LAPLACE>(ctx, P, mixed);
+  case ABX_K_MULTIQUADRIC: return launch_dense<ABX_K_MULTIQUADRIC>(ctx, P, mixed);
+  case ABX_K_SCALAR_SUM: return launch_dense<ABX_K_SCALAR_SUM>(ctx, P, false);
+  }
+  set_error("unknown kernel kind %d", P.kind);
+  return ABX_ERR_INVALID;
+}
+
+}  // namespace abx
+
+using namespace abx;
+
+extern "C" {
+
+static int check_kernel(const abx_kernel *k) {
+  ABX_REQUIRE(k, ABX_ERR_INVALID, "null kernel descriptor");
+  ABX_REQUIRE(k->kind >= ABX_K_CONST && k->kind <= ABX_K_SCALAR_SUM, ABX_ERR_INVALID,
+              "unknown kernel kind %d", k->kind);
+  return ABX_OK;
+}
+
+int abx_create_sparse_operator(abx_particles *rows, abx_particles *cols, double radius,
+                               const abx_kernel *k, abx_operator **out) {
+  ABX_REQUIRE(rows && cols && out, ABX_ERR_INVALID, "null argument");
+  ABX_TRY(check_kernel(k));
+  ABX_REQUIRE(rows->ctx == cols->ctx, ABX_ERR_INVALID, "particle sets on different contexts");
+  ABX_REQUIRE(rows->dim == cols->dim, ABX_ERR_INVALID, "dimension mismatch");
+  ABX_REQUIRE(cols->searchable, ABX_ERR_STATE,
+              "init_neighbour_search not called on the column particle set");
+  ABX_REQUIRE(radius >= 0 && std::isfinite(radius), ABX_ERR_INVALID, "invalid radius");
+  ABX_TRY(ctx_activate(rows->ctx));
+  abx_operator *op = new abx_operator();
+  op->kind = 0;
+  op->rows = rows;
+  op->cols = cols;
+  op->radius = radius;
+  op->k = *k;
+  int st = pair_layout_build(op);
+  if (st != ABX_OK) {
+    if (op->pairs) pair_layout_free(op->pairs);
+    delete op;
+    return st;
+  }
+  *out = op;
+  return ABX_OK;
+}
+
+int abx_create_dense_operator(abx_particles *rows, abx_particles *cols, const abx_kernel *k,
+                              abx_operator **out) {
+  ABX_REQUIRE(rows && cols && out, ABX_ERR_INVALID, "null argument");
+  ABX_TRY(check_kernel(k));
+  ABX_REQUIRE(rows->ctx == cols->ctx, ABX_ERR_INVALID, "particle sets on different contexts");
+  ABX_REQUIRE(rows->dim == cols->dim, ABX_ERR_INVALID, "dimension mismatch");
+  abx_operator *op = new abx_operator();
+  op->kind = 1;
+  op->rows = rows;
+  op->cols = cols;
+  op->k = *k;
+  *out = op;
+  return ABX_OK;
+}
+
+int abx_operator_destroy(abx_operator *op) {
+  if (!op) return ABX_OK;
+  cudaSetDevice(op->rows->ctx->device);
+  cudaStreamSynchronize(op->rows->ctx->stream);
+  if (op->pairs) pair_layout_free(op->pairs);
+  delete op;
+  return ABX_OK;
+}
+
+int abx_operator_set_precision(abx_operator *op, int mode) {
+  ABX_REQUIRE(op, ABX_ERR_INVALID, "null operator");
+  ABX_REQUIRE(mode == ABX_PREC_FP64 || mode == ABX_PREC_MIXED, ABX_ERR_INVALID,
+              "unknown precision mode %d", mode);
+  op->precision = mode;
+  return ABX_OK;
+}
+
+int64_t abx_operator_rows(const abx_operator *op) { return op ? op->rows->n : -1; }
+int64_t abx_operator_cols(const abx_operator *op) { return op ? op->cols->n : -1; }
+
+int abx_operator_matvec(abx_operator *op, const double *b, double *c) {
+  ABX_REQUIRE(op, ABX_ERR_INVALID, "null operator");
+  const int64_t nr = op->rows->n, nc = op->cols->n;
+  ABX_REQUIRE((b || nc == 0) && (c || nr == 0), ABX_ERR_INVALID, "null vector");
+  abx_context *ctx = op->rows->ctx;
+  ABX_TRY(ctx_activate(ctx));
+  if (op->kind == 0)
+    ABX_REQUIRE(op->cols->searchable, ABX_ERR_STATE,
+                "init_neighbour_search not called on the column particle set");
+  const void *bd;
+  void *cd;
+  ABX_TRY(op->stage_b.in(ctx, b, (size_t)nc * sizeof(double), &bd));
+  ABX_TRY(op->stage_c.out(ctx, c, (size_t)nr * sizeof(double), &cd));
+  if (op->kind == 0)
+    ABX_TRY(sparse_matvec_device(op, (const double *)bd, (double *)cd));
+  else
+    ABX_TRY(dense_matvec_device(op, (const double *)bd, (double *)cd));
+  ABX_TRY(op->stage_c.finish(ctx, c, (size_t)nr * sizeof(double)));
+  return ABX_OK;
+}
+
+int abx_operator_last_stats(abx_operator *op, int64_t *candidates, int64_t *pairs) {
+  ABX_REQUIRE(op, ABX_ERR_INVALID, "null operator");
+  if (candidates) *candidates = op->last_candidates;
+  if (pairs) *pairs = op->last_pairs;
+  return ABX_OK;
+}
+
+}  // extern "C"

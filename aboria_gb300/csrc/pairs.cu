@@ -1,0 +1,907 @@
+// Radius search and the matrix-free sparse operator on the GPU.
+//
+// Reference path restated: KernelSparse::evaluate (src/Kernels.h:720-751)
+// calls euclidean_search (src/Search.h:839-845) per row, which walks periodic
+// images x buckets of the CellListOrdered grid and accepts a candidate iff
+// !(((0+dx0^2)+dx1^2)+dx2^2 > r^2) in FP64 with dx = x_j - (x_i + image*L)
+// (src/Search.h:438-465, src/detail/Distance.h:132-137); it then accumulates
+// c_i += f(dx, a_i, b_j) * b_j.
+//
+// GB300 design (not a translation of the bucket-walk iterator):
+//  * An internal fine grid of side ~r/3 (padded to 3 dims, last real
+//    dimension fastest) re-sorts the column particles so that each (e0,e1)
+//    row of fine cells is one contiguous index range; a query tile then
+//    visits ~49 contiguous ranges instead of iterating buckets.
+//  * Work unit = one warp = up to 32 spatially adjacent queries.  The warp
+//    stages 32 candidates at a time in shared memory (one coalesced 16 B load
+//    per lane) and every lane tests its query against all of them
+//    (broadcast LDS), so each candidate costs one LDS + the pair arithmetic.
+//  * Mixed mode: candidate and query coordinates are FP32 offsets from the
+//    tile's reference cell (magnitude <= a few cells, so ~1e-9 absolute
+//    error).  A pair is accepted outright if d2 <= r2_lo, rejected if
+//    d2 > r2_hi, and only inside that rounding band is the reference's exact
+//    FP64 test evaluated, so neighbour decisions are identical to the FP64
+//    test.  Kernel values are FP32; each lane sums a staged block of <= 32
+//    terms in FP32 and adds the block into an FP64 accumulator.
+//  * FP64 mode: candidates are staged as absolute FP64 positions and every
+//    pair evaluates the reference's formula exactly (no FMA contraction).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "handles.cuh"
+
+namespace abx {
+
+struct alignas(32) D4 {
+  double x, y, z, w;
+};
+
+struct FineGrid {
+  int dim, eoff;
+  int m[3];
+  double h[3];
+  float hf[3];
+  double lo[3];
+  double L[3];
+  int periodic[3];
+  int K[3];
+  uint32_t ncells;
+};
+
+// A point set ordered by fine cell.
+struct PointLayout {
+  int64_t n = 0;
+  DevBuf<uint32_t> perm;  // kernel order -> source index
+  DevBuf<int4> cell;      // unclamped fine cell (internal dims)
+  DevBuf<float4> loc;     // FP32 offset from the clamped cell corner; .w = clamped c2 bits
+  DevBuf<D4> posk;        // FP64 position in kernel order (internal dims, pad = 0)
+  DevBuf<uint32_t> keys;  // sorted clamped cell keys
+};
+
+struct PairLayout {
+  FineGrid fg;
+  double r = 0;
+  uint64_t cols_version = 0, rows_version = 0;
+  bool self = true;
+  PointLayout cols;
+  PointLayout rows_own;
+  PointLayout *rows = nullptr;
+  DevBuf<uint32_t> cell_start;  // fg.ncells + 1
+  DevBuf<int2> units;           // (first query in kernel order, count <= 32)
+  int nunits = 0;
+  DevBuf<float> bk32;
+  DevBuf<double> bk64;
+  DevBuf<double> sk;  // column scalar in kernel order
+  DevBuf<double> sq;  // row scalar in kernel order
+  DevBuf<double> ck;  // result in row kernel order
+  DevBuf<int> counter;
+};
+
+void pair_layout_free(PairLayout *L) { delete L; }
+
+namespace {
+
+constexpr int TPB = 256;
+constexpr int WARPS_PER_CTA = 4;
+constexpr int GROUP_E2 = 2;  // a unit spans at most this many fine cells along e2
+
+enum { POL_COUNT = 0, POL_LIST = 1, POL_MATVEC = 2 };
+
+// ------------------------------------------------------------ layout build ---
+FineGrid make_fine_grid(const GridDesc &g, double r, int64_t npts, int F) {
+  FineGrid fg{};
+  fg.dim = g.dim;
+  fg.eoff = 3 - g.dim;
+  const double target = r > 0 ? r / F : 0.0;
+  for (int e = 0; e < 3; ++e) {
+    const int d = e - fg.eoff;
+    if (d < 0) {
+      fg.m[e] = 1;
+      fg.h[e] = 1.0;
+      fg.lo[e] = 0.0;
+      fg.L[e] = 1.0;
+      fg.periodic[e] = 0;
+      continue;
+    }
+    fg.lo[e] = g.lo[d];
+    fg.L[e] = g.hi[d] - g.lo[d];
+    fg.periodic[e] = g.periodic[d];
+    double m = target > 0 ? std::floor(fg.L[e] / target * (1.0 - 1e-9)) : 1.0;
+    if (!(m >= 1.0)) m = 1.0;
+    if (m > 1023.0) m = 1023.0;
+    fg.m[e] = (int)m;
+  }
+  // keep the fine grid within a few cells per point
+  const double cap = std::max<double>(64.0, 4.0 * (double)npts);
+  for (int it = 0; it < 64; ++it) {
+    double tot = (double)fg.m[0] * fg.m[1] * fg.m[2];
+    if (tot <= cap) break;
+    int eb = 0;
+    for (int e = 1; e < 3; ++e)
+      if (fg.m[e] > fg.m[eb]) eb = e;
+    fg.m[eb] = std::max(1, (int)(fg.m[eb] * 0.8));
+  }
+  fg.ncells = (uint32_t)fg.m[0] * fg.m[1] * fg.m[2];
+  for (int e = 0; e < 3; ++e) {
+    const int d = e - fg.eoff;
+    fg.h[e] = d < 0 ? 1.0 : fg.L[e] / fg.m[e];
+    fg.hf[e] = (float)fg.h[e];
+    fg.K[e] = d < 0 ? 0 : (int)std::ceil(r / fg.h[e] * (1.0 + 1e-9));
+    if (fg.K[e] > 2 * fg.m[e] + 1) fg.K[e] = 2 * fg.m[e] + 1;
+  }
+  return fg;
+}
+
+__device__ __forceinline__ int fine_coord(double x, double lo, double h, int m) {
+  // floor((x - lo)/h) computed as in the layout; unclamped
+  const double t = floor((x - lo) / h);
+  if (!(t == t)) return 1000000000;  // NaN: far outside, never a neighbour
+  if (t < -1e9) return -1000000000;
+  if (t > 1e9) return 1000000000;
+  return (int)t;
+}
+
+// Source points (SoA, dim columns, n) -> clamped key, unclamped cell.
+__global__ void k_fine_keys(const double *__restrict__ src, int64_t n, int64_t stride, FineGrid fg,
+                            uint32_t *__restrict__ keys, uint32_t *__restrict__ vals) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int c[3];
+  for (int e = 0; e < 3; ++e) {
+    const int d = e - fg.eoff;
+    if (d < 0) {
+      c[e] = 0;
+      continue;
+    }
+    int u = fine_coord(src[(int64_t)d * stride + i], fg.lo[e], fg.h[e], fg.m[e]);
+    c[e] = min(max(u, 0), fg.m[e] - 1);
+  }
+  keys[i] = ((uint32_t)c[0] * fg.m[1] + c[1]) * fg.m[2] + c[2];
+  vals[i] = (uint32_t)i;
+}
+
+// Anchor cell of a point: the clamped cell for column particles (their range
+// membership), the unclamped cell for query points (which may lie outside
+// the domain and must keep their true periodic image).  loc holds the FP32
+// offset from the anchor cell's corner and, in .w, the anchor's e2 index.
+__global__ void k_fill_layout(const double *__restrict__ src, int64_t stride, FineGrid fg,
+                              const uint32_t *__restrict__ perm, int64_t n, int clamp_anchor,
+                              int4 *__restrict__ cell, float4 *__restrict__ loc,
+                              D4 *__restrict__ posk) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint32_t i = perm[k];
+  double x[3];
+  int u[3], c[3];
+  float f[3];
+  for (int e = 0; e < 3; ++e) {
+    const int d = e - fg.eoff;
+    if (d < 0) {
+      x[e] = 0.0;
+      u[e] = 0;
+      c[e] = 0;
+      f[e] = 0.f;
+      continue;
+    }
+    x[e] = src[(int64_t)d * stride + i];
+    u[e] = fine_coord(x[e], fg.lo[e], fg.h[e], fg.m[e]);
+    c[e] = clamp_anchor ? min(max(u[e], 0), fg.m[e] - 1) : u[e];
+    const double corner = fg.lo[e] + (double)c[e] * fg.h[e];
+    f[e] = (float)(x[e] - corner);
+  }
+  cell[k] = make_int4(c[0], c[1], c[2], 0);
+  loc[k] = make_float4(f[0], f[1], f[2], __int_as_float(c[2]));
+  posk[k] = D4{x[0], x[1], x[2], 0.0};
+}
+
+__global__ void k_mark_runs_fine(const uint32_t *__restrict__ keys, int64_t n,
+                                 uint32_t *__restrict__ first, uint32_t *__restrict__ last) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint32_t key = keys[k];
+  if (k == 0 || keys[k - 1] != key) first[key] = (uint32_t)k;
+  if (k == n - 1 || keys[k + 1] != key) last[key] = (uint32_t)(k + 1);
+}
+
+__global__ void k_sub(const uint32_t *__restrict__ a, uint32_t n, uint32_t *__restrict__ b) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) b[c] -= a[c];
+}
+
+int build_points(abx_context *ctx, const double *src_soa, int64_t n, int64_t stride,
+                 const FineGrid &fg, bool clamp_anchor, PointLayout &P) {
+  cudaStream_t s = ctx->stream;
+  P.n = n;
+  ABX_TRY(P.perm.reserve(n ? n : 1));
+  ABX_TRY(P.keys.reserve(n ? n : 1));
+  ABX_TRY(P.cell.reserve(n ? n : 1));
+  ABX_TRY(P.loc.reserve(n ? n : 1));
+  ABX_TRY(P.posk.reserve(n ? n : 1));
+  if (n == 0) return ABX_OK;
+  DevBuf<uint32_t> tmp;
+  const size_t rt = radix_temp_u32(n);
+  ABX_TRY(tmp.reserve(2 * (size_t)n + rt + 64));
+  k_fine_keys<<<ceil_div(n, TPB), TPB, 0, s>>>(src_soa, n, stride, fg, P.keys.ptr, P.perm.ptr);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  int bits = 0;
+  while (bits < 32 && ((uint64_t)(fg.ncells - 1) >> bits) != 0) ++bits;
+  ABX_TRY(radix_sort_pairs(P.keys.ptr, P.perm.ptr, n, bits, tmp.ptr, tmp.ptr + n, tmp.ptr + 2 * n,
+                           s));
+  k_fill_layout<<<ceil_div(n, TPB), TPB, 0, s>>>(src_soa, stride, fg, P.perm.ptr, n,
+                                                 clamp_anchor ? 1 : 0, P.cell.ptr, P.loc.ptr,
+                                                 P.posk.ptr);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  ABX_CHECK_CUDA(cudaStreamSynchronize(s));
+  return ABX_OK;
+}
+
+int build_cell_start(abx_context *ctx, PairLayout &L) {
+  cudaStream_t s = ctx->stream;
+  const uint32_t nc = L.fg.ncells;
+  ABX_TRY(L.cell_start.reserve((size_t)nc + 1));
+  DevBuf<uint32_t> first;
+  ABX_TRY(first.reserve((size_t)nc + 1 + scan_temp_elems((size_t)nc + 1)));
+  uint32_t *cs = L.cell_start.ptr;
+  ABX_CHECK_CUDA(cudaMemsetAsync(cs, 0, ((size_t)nc + 1) * 4, s));
+  ABX_CHECK_CUDA(cudaMemsetAsync(first.ptr, 0, ((size_t)nc + 1) * 4, s));
+  const int64_t n = L.cols.n;
+  if (n > 0) {
+    k_mark_runs_fine<<<ceil_div(n, TPB), TPB, 0, s>>>(L.cols.keys.ptr, n, first.ptr, cs);
+    ABX_CHECK_CUDA(cudaGetLastError());
+    k_sub<<<ceil_div(nc, TPB), TPB, 0, s>>>(first.ptr, nc, cs);
+    ABX_CHECK_CUDA(cudaGetLastError());
+  }
+  // counts -> exclusive scan over nc+1 entries (last entry 0 -> total)
+  ABX_TRY(exclusive_scan_u32(cs, (size_t)nc + 1, first.ptr + nc + 1, s));
+  ABX_CHECK_CUDA(cudaStreamSynchronize(s));
+  return ABX_OK;
+}
+
+// Units: greedy runs of <= 32 consecutive queries (kernel order) in one
+// (e0,e1) row spanning at most GROUP_E2 fine cells along e2.
+int build_units(abx_context *ctx, PairLayout &L) {
+  PointLayout &Q = *L.rows;
+  const int64_t n = Q.n;
+  std::vector<uint32_t> keys(n);
+  if (n) {
+    ABX_CHECK_CUDA(cudaMemcpy(keys.data(), Q.keys.ptr, n * 4, cudaMemcpyDeviceToHost));
+  }
+  std::vector<int2> units;
+  units.reserve(n / 16 + 16);
+  const uint32_t m2 = (uint32_t)L.fg.m[2];
+  int64_t i = 0;
+  while (i < n) {
+    const uint32_t row = keys[i] / m2;
+    const uint32_t c2 = keys[i] % m2;
+    int64_t j = i + 1;
+    while (j < n && j - i < 32) {
+      const uint32_t rj = keys[j] / m2, cj = keys[j] % m2;
+      if (rj != row || cj >= c2 + GROUP_E2) break;
+      ++j;
+    }
+    units.push_back(make_int2((int)i, (int)(j - i)));
+    i = j;
+  }
+  L.nunits = (int)units.size();
+  ABX_TRY(L.units.reserve(units.size() ? units.size() : 1));
+  if (!units.empty())
+    ABX_CHECK_CUDA(cudaMemcpy(L.units.ptr, units.data(), units.size() * sizeof(int2),
+                              cudaMemcpyHostToDevice));
+  ABX_TRY(L.counter.reserve(4));
+  return ABX_OK;
+}
+
+// ------------------------------------------------------------- kernels ---
+struct KParams {
+  FineGrid fg;
+  double r, r2;
+  double prune2;  // squared pruning distance (r plus a safety margin)
+  // kernel functor parameters
+  int kind;
+  double p0;
+  float p0f, c_exp2;  // c_exp2 = -p0*log2(e)
+  // columns (kernel order)
+  const float4 *cloc;
+  const D4 *cpos;
+  const uint32_t *cell_start;
+  const float *b32;
+  const double *b64;
+  const double *s_col;
+  // queries (kernel order)
+  const int4 *qcell;
+  const float4 *qloc;
+  const D4 *qpos;
+  const double *s_row;
+  const int2 *units;
+  int nunits;
+  int *counter;
+  // outputs (query kernel order)
+  int32_t *counts;
+  const int64_t *rowptr;  // for LIST: query kernel order -> output offset
+  int32_t *cols_out;      // storage index of the column particle
+  const uint32_t *cperm;  // column kernel order -> storage index
+  double *c;
+};
+
+template <int KIND> __device__ __forceinline__ float kern32(float d2, const KParams &P) {
+  if (KIND == ABX_K_CONST) return P.p0f;
+  if (KIND == ABX_K_GAUSSIAN || KIND == ABX_K_COMPACT_GAUSSIAN) return exp2f(d2 * P.c_exp2);
+  if (KIND == ABX_K_WENDLAND_C2) {
+    const float q = d2 * rsqrtf(fmaxf(d2, 1e-36f)) * P.p0f;
+    const float t = fmaxf(1.0f - q, 0.0f);
+    const float t2 = t * t;
+    return t2 * t2 * fmaf(4.0f, q, 1.0f);
+  }
+  if (KIND == ABX_K_LAPLACE) return __fdividef(1.0f, d2 * rsqrtf(fmaxf(d2, 1e-36f)) + P.p0f);
+  if (KIND == ABX_K_MULTIQUADRIC) {
+    const float a = d2 + P.p0f;
+    return a * rsqrtf(fmaxf(a, 1e-36f));
+  }
+  return 0.f;
+}
+
+template <int KIND>
+__device__ __forceinline__ double kern64(double d2, const KParams &P, double si, double sj) {
+  if (KIND == ABX_K_CONST) return P.p0;
+  if (KIND == ABX_K_GAUSSIAN || KIND == ABX_K_COMPACT_GAUSSIAN) return exp(-d2 * P.p0);
+  if (KIND == ABX_K_WENDLAND_C2) {
+    const double q = sqrt(d2) * P.p0;
+    if (q >= 1.0) return 0.0;
+    const double t = 1.0 - q;
+    const double t2 = t * t;
+    return t2 * t2 * (4.0 * q + 1.0);
+  }
+  if (KIND == ABX_K_LAPLACE) return 1.0 / (sqrt(d2) + P.p0);
+  if (KIND == ABX_K_MULTIQUADRIC) return sqrt(d2 + P.p0);
+  if (KIND == ABX_K_SCALAR_SUM) return si + sj;
+  return 0.0;
+}
+
+// The reference's FP64 acceptance test for one (query, candidate, image):
+// accum = ((0 + dx0^2) + dx1^2) + dx2^2 over the REAL dimensions in order, no
+// FMA; inside iff !(accum > r^2).  Returns accum (or +inf if outside).
+__device__ __forceinline__ double exact_d2(const D4 &xq, const D4 &xj, const int *img,
+                                           const FineGrid &fg) {
+  const double q[3] = {xq.x, xq.y, xq.z};
+  const double p[3] = {xj.x, xj.y, xj.z};
+  double acc = 0.0;
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    if (e < fg.eoff) continue;
+    const double cur = __dadd_rn(q[e], __dmul_rn((double)img[e], fg.L[e]));
+    const double dx = __dsub_rn(p[e], cur);
+    acc = __dadd_rn(acc, __dmul_rn(dx, dx));
+  }
+  return acc;
+}
+
+struct WarpSmem32 {
+  float4 p[32];
+  int idx[32];
+};
+struct WarpSmem64 {
+  double x[32], y[32], z[32], b[32], s[32];
+  int idx[32];
+};
+
+// Walk all candidate segments of the warp's unit; for each segment call
+// seg(start, end, img[3], du0, du1, c2shift) where the staged e2 offset of a
+// candidate with clamped cell c2 is (c2 + c2shift) cells from the reference.
+template <class Seg>
+__device__ __forceinline__ void for_each_segment(const KParams &P, const int lo[3],
+                                                 const int hi[3], Seg &&seg) {
+  const FineGrid &fg = P.fg;
+  const int a0 = max(lo[0] - fg.K[0], fg.periodic[0] ? -fg.m[0] : 0);
+  const int b0 = min(hi[0] + fg.K[0], fg.periodic[0] ? 2 * fg.m[0] - 1 : fg.m[0] - 1);
+  for (int u0 = a0; u0 <= b0; ++u0) {
+    const int g0c = max(max(lo[0] - u0, u0 - hi[0]) - 1, 0);
+    const double g0 = g0c * fg.h[0];
+    const double g0s = g0 * g0;
+    if (g0s > P.prune2) continue;
+    int w0 = u0, i0 = 0;
+    if (u0 < 0) { w0 = u0 + fg.m[0]; i0 = 1; }
+    else if (u0 >= fg.m[0]) { w0 = u0 - fg.m[0]; i0 = -1; }
+    const int a1 = max(lo[1] - fg.K[1], fg.periodic[1] ? -fg.m[1] : 0);
+    const int b1 = min(hi[1] + fg.K[1], fg.periodic[1] ? 2 * fg.m[1] - 1 : fg.m[1] - 1);
+    for (int u1 = a1; u1 <= b1; ++u1) {
+      const int g1c = max(max(lo[1] - u1, u1 - hi[1]) - 1, 0);
+      const double g1 = g1c * fg.h[1];
+      const double rem = P.prune2 - g0s - g1 * g1;
+      if (rem < 0.0) continue;
+      int w1 = u1, i1 = 0;
+      if (u1 < 0) { w1 = u1 + fg.m[1]; i1 = 1; }
+      else if (u1 >= fg.m[1]) { w1 = u1 - fg.m[1]; i1 = -1; }
+      // e2 extent: cells whose gap <= sqrt(rem)
+      int ext = (int)floor(sqrt(rem) / fg.h[2]) + 1;
+      if (ext > fg.K[2]) ext = fg.K[2];
+      int a2 = lo[2] - ext, b2 = hi[2] + ext;
+      const uint32_t rowbase = ((uint32_t)w0 * fg.m[1] + w1) * (uint32_t)fg.m[2];
+      const int m2 = fg.m[2];
+      // split the unwrapped e2 range into image segments
+      const int segs_lo[3] = {fg.periodic[2] ? -m2 : 0, 0, m2};
+      const int segs_hi[3] = {-1, m2 - 1, fg.periodic[2] ? 2 * m2 - 1 : m2 - 1};
+      const int segimg[3] = {1, 0, -1};
+#pragma unroll 1
+      for (int sgi = 0; sgi < 3; ++sgi) {
+        if (sgi != 1 && !fg.periodic[2]) continue;
+        const int sa = max(a2, segs_lo[sgi]), sb = min(b2, segs_hi[sgi]);
+        if (sa > sb) continue;
+        const int shift = segimg[sgi] * m2;  // w2 = u2 + shift
+        const uint32_t start = P.cell_start[rowbase + (uint32_t)(sa + shift)];
+        const uint32_t end = P.cell_start[rowbase + (uint32_t)(sb + shift) + 1];
+        if (start >= end) continue;
+        const int img[3] = {i0, i1, segimg[sgi]};
+        seg(start, end, img, u0 - lo[0], u1 - lo[1], -shift - lo[2]);
+      }
+    }
+  }
+}
+
+// Mixed-precision pair kernel: FP32 prefilter + exact FP64 band, FP32 terms.
+template <int POL, int KIND>
+__global__ void __launch_bounds__(WARPS_PER_CTA * 32)
+    k_pairs_mixed(KParams P) {
+  __shared__ WarpSmem32 sm_all[WARPS_PER_CTA];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  WarpSmem32 &sm = sm_all[wid];
+  const FineGrid &fg = P.fg;
+  for (;;) {
+    int unit = 0;
+    if (lane == 0) unit = atomicAdd(P.counter, 1);
+    unit = __shfl_sync(0xffffffffu, unit, 0);
+    if (unit >= P.nunits) break;
+    const int2 U = P.units[unit];
+    const bool active = lane < U.y;
+    const int qi = U.x + (active ? lane : 0);
+    const int4 qc = P.qcell[qi];
+    const float4 ql = P.qloc[qi];
+    int lo[3] = {qc.x, qc.y, qc.z}, hi[3] = {qc.x, qc.y, qc.z};
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      int a = active ? lo[e] : 0x7fffffff, b = active ? hi[e] : -0x7fffffff;
+      a = __reduce_min_sync(0xffffffffu, a);
+      b = __reduce_max_sync(0xffffffffu, b);
+      lo[e] = a;
+      hi[e] = b;
+    }
+    // query offset from the reference cell lo
+    const float pq0 = fmaf((float)(qc.x - lo[0]), fg.hf[0], ql.x);
+    const float pq1 = fmaf((float)(qc.y - lo[1]), fg.hf[1], ql.y);
+    const float pq2 = fmaf((float)(qc.z - lo[2]), fg.hf[2], ql.z);
+    // rounding band for this tile: every staged coordinate is at most `span`
+    // cells from the reference corner, so each FP32 offset carries less than
+    // (3*span+2)*h*2^-24 absolute error and a difference of two of them less
+    // than edx = (span+2)*h*2^-20; |d2_f32 - d2| <= band follows.
+    int span = 0;
+#pragma unroll
+    for (int e = 0; e < 3; ++e) span = max(span, hi[e] - lo[e] + 2 * fg.K[e] + 2);
+    double hmax = fmax(fmax(fg.h[0] * (fg.eoff <= 0), fg.h[1] * (fg.eoff <= 1)), fg.h[2]);
+    const double edx = (double)(span + 2) * hmax * 9.5367431640625e-07;  // 2^-20
+    const double band = 2.0 * 1.7320508075688772 * (P.r + edx) * edx + edx * edx * 3.0 +
+                        4.0 * 5.960464477539063e-08 * (P.r2 + 1e-300) + 1e-300;
+    const float r2lo = __double2float_rd(fmax(P.r2 - band, 0.0));
+    const float r2hi = __double2float_ru(P.r2 + band);
+    D4 xq;
+    xq.x = xq.y = xq.z = xq.w = 0.0;
+    double acc64 = 0.0;
+    int count = 0;
+    int64_t out_off = 0;
+    if (POL == POL_LIST && active) out_off = P.rowptr[qi];
+
+    for_each_segment(P, lo, hi, [&](uint32_t start, uint32_t end, const int *img, int du0,
+                                    int du1, int c2shift) {
+      const float o0 = (float)du0 * fg.hf[0];
+      const float o1 = (float)du1 * fg.hf[1];
+      for (uint32_t t = start; t < end; t += 32) {
+        const uint32_t k = t + lane;
+        if (k < end) {
+          const float4 cl = P.cloc[k];
+          const int c2 = __float_as_int(cl.w);
+          float4 st;
+          st.x = cl.x + o0;
+          st.y = cl.y + o1;
+          st.z = fmaf((float)(c2 + c2shift), fg.hf[2], cl.z);
+          st.w = (POL == POL_MATVEC) ? P.b32[k] : 0.f;
+          sm.p[lane] = st;
+          sm.idx[lane] = (int)k;
+        }
+        __syncwarp();
+        const int nt = min(32u, end - t);
+        float acc32 = 0.f;
+        for (int j = 0; j < nt; ++j) {
+          const float4 c = sm.p[j];
+          const float d0 = c.x - pq0, d1 = c.y - pq1, d2v = c.z - pq2;
+          const float dd = fmaf(d2v, d2v, fmaf(d1, d1, d0 * d0));
+          bool in = dd <= r2lo;
+          if (!in && dd <= r2hi) {
+            // rounding band: decide with the reference's FP64 test
+            if (xq.w == 0.0) {
+              xq = P.qpos[qi];
+              xq.w = 1.0;
+            }
+            const D4 xj = P.cpos[sm.idx[j]];
+            in = !(exact_d2(xq, xj, img, fg) > P.r2);
+          }
+          if (in && active) {
+            if (POL == POL_MATVEC) acc32 = fmaf(kern32<KIND>(dd, P), c.w, acc32);
+            if (POL == POL_COUNT) ++count;
+            if (POL == POL_LIST) P.cols_out[out_off++] = (int32_t)P.cperm[sm.idx[j]];
+          }
+        }
+        if (POL == POL_MATVEC) acc64 += (double)acc32;
+        __syncwarp();
+      }
+    });
+    if (active) {
+      if (POL == POL_MATVEC) P.c[qi] = acc64;
+      if (POL == POL_COUNT) P.counts[qi] = count;
+    }
+  }
+}
+
+// FP64 pair kernel: the reference's arithmetic for every pair.
+template <int POL, int KIND>
+__global__ void __launch_bounds__(WARPS_PER_CTA * 32)
+    k_pairs_fp64(KParams P) {
+  __shared__ WarpSmem64 sm_all[WARPS_PER_CTA];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  WarpSmem64 &sm = sm_all[wid];
+  const FineGrid &fg = P.fg;
+  for (;;) {
+    int unit = 0;
+    if (lane == 0) unit = atomicAdd(P.counter, 1);
+    unit = __shfl_sync(0xffffffffu, unit, 0);
+    if (unit >= P.nunits) break;
+    const int2 U = P.units[unit];
+    const bool active = lane < U.y;
+    const int qi = U.x + (active ? lane : 0);
+    const int4 qc = P.qcell[qi];
+    int lo[3] = {qc.x, qc.y, qc.z}, hi[3] = {qc.x, qc.y, qc.z};
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      int a = active ? lo[e] : 0x7fffffff, b = active ? hi[e] : -0x7fffffff;
+      lo[e] = __reduce_min_sync(0xffffffffu, a);
+      hi[e] = __reduce_max_sync(0xffffffffu, b);
+    }
+    const D4 xq = P.qpos[qi];
+    const double si = (KIND == ABX_K_SCALAR_SUM) ? P.s_row[qi] : 0.0;
+    double acc = 0.0;
+    int count = 0;
+    int64_t out_off = 0;
+    if (POL == POL_LIST && active) out_off = P.rowptr[qi];
+    for_each_segment(P, lo, hi, [&](uint32_t start, uint32_t end, const int *img, int, int, int) {
+      // image point x + I*L (src/Search.h:188-190), real dimensions only
+      double cur[3];
+      const double q[3] = {xq.x, xq.y, xq.z};
+#pragma unroll
+      for (int e = 0; e < 3; ++e)
+        cur[e] = __dadd_rn(q[e], __dmul_rn((double)img[e], fg.L[e]));
+      for (uint32_t t = start; t < end; t += 32) {
+        const uint32_t k = t + lane;
+        if (k < end) {
+          const D4 p = P.cpos[k];
+          sm.x[lane] = p.x;
+          sm.y[lane] = p.y;
+          sm.z[lane] = p.z;
+          sm.b[lane] = (POL == POL_MATVEC) ? P.b64[k] : 0.0;
+          sm.s[lane] = (KIND == ABX_K_SCALAR_SUM) ? P.s_col[k] : 0.0;
+          sm.idx[lane] = (int)k;
+        }
+        __syncwarp();
+        const int nt = min(32u, end - t);
+        for (int j = 0; j < nt; ++j) {
+          const double pj[3] = {sm.x[j], sm.y[j], sm.z[j]};
+          double a = 0.0;
+#pragma unroll
+          for (int e = 0; e < 3; ++e) {
+            if (e < fg.eoff) continue;
+            const double dx = __dsub_rn(pj[e], cur[e]);
+            a = __dadd_rn(a, __dmul_rn(dx, dx));
+          }
+          if (!(a > P.r2) && active) {
+            if (POL == POL_MATVEC)
+              acc = __dadd_rn(acc, __dmul_rn(kern64<KIND>(a, P, si, sm.s[j]), sm.b[j]));
+            if (POL == POL_COUNT) ++count;
+            if (POL == POL_LIST) P.cols_out[out_off++] = (int32_t)P.cperm[sm.idx[j]];
+          }
+        }
+        __syncwarp();
+      }
+    });
+    if (active) {
+      if (POL == POL_MATVEC) P.c[qi] = acc;
+      if (POL == POL_COUNT) P.counts[qi] = count;
+    }
+  }
+}
+
+__global__ void k_gather_b(const double *__restrict__ b, const uint32_t *__restrict__ perm,
+                           int64_t n, float *__restrict__ b32, double *__restrict__ b64) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const double v = b[perm[k]];
+  if (b32) b32[k] = (float)v;
+  if (b64) b64[k] = v;
+}
+
+__global__ void k_scatter_c(const double *__restrict__ ck, const uint32_t *__restrict__ perm,
+                            int64_t n, double *__restrict__ c) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  c[perm[k]] = ck[k];
+}
+
+template <class T>
+__global__ void k_scatter(const T *__restrict__ src, const uint32_t *__restrict__ perm, int64_t n,
+                          T *__restrict__ dst) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  dst[perm[k]] = src[k];
+}
+
+KParams base_params(const PairLayout &L) {
+  KParams P{};
+  P.fg = L.fg;
+  P.r = L.r;
+  P.r2 = L.r * L.r;
+  double hmax = 0;
+  for (int e = 0; e < 3; ++e)
+    if (e >= L.fg.eoff) hmax = std::max(hmax, L.fg.h[e]);
+  const double margin = L.r * 1e-9 + hmax * 1e-9;
+  P.prune2 = (L.r + margin) * (L.r + margin);
+  P.cloc = L.cols.loc.ptr;
+  P.cpos = L.cols.posk.ptr;
+  P.cell_start = L.cell_start.ptr;
+  P.cperm = L.cols.perm.ptr;
+  P.qcell = L.rows->cell.ptr;
+  P.qloc = L.rows->loc.ptr;
+  P.qpos = L.rows->posk.ptr;
+  P.units = L.units.ptr;
+  P.nunits = L.nunits;
+  P.counter = L.counter.ptr;
+  return P;
+}
+
+int grid_blocks(abx_context *ctx, int nunits) {
+  int blocks = ctx->num_sms * 8;
+  const int need = (nunits + WARPS_PER_CTA - 1) / WARPS_PER_CTA;
+  return std::max(1, std::min(blocks, need));
+}
+
+template <int POL, int KIND> int launch_pairs(abx_context *ctx, const KParams &P, bool mixed) {
+  const int blocks = grid_blocks(ctx, P.nunits);
+  ABX_CHECK_CUDA(cudaMemsetAsync(P.counter, 0, sizeof(int), ctx->stream));
+  if (mixed)
+    k_pairs_mixed<POL, KIND><<<blocks, WARPS_PER_CTA * 32, 0, ctx->stream>>>(P);
+  else
+    k_pairs_fp64<POL, KIND><<<blocks, WARPS_PER_CTA * 32, 0, ctx->stream>>>(P);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  return ABX_OK;
+}
+
+template <int POL> int launch_pairs_kind(abx_context *ctx, const KParams &P, bool mixed) {
+  switch (P.kind) {
+  case ABX_K_CONST: return launch_pairs<POL, ABX_K_CONST>(ctx, P, mixed);
+  case ABX_K_GAUSSIAN: return launch_pairs<POL, ABX_K_GAUSSIAN>(ctx, P, mixed);
+  case ABX_K_WENDLAND_C2: return launch_pairs<POL, ABX_K_WENDLAND_C2>(ctx, P, mixed);
+  case ABX_K_COMPACT_GAUSSIAN: return launch_pairs<POL, ABX_K_COMPACT_GAUSSIAN>(ctx, P, mixed);
+  case ABX_K_LAPLACE: return launch_pairs<POL, ABX_K_LAPLACE>(ctx, P, mixed);
+  case ABX_K_MULTIQUADRIC: return launch_pairs<POL, ABX_K_MULTIQUADRIC>(ctx, P, mixed);
+  case ABX_K_SCALAR_SUM: return launch_pairs<POL, ABX_K_SCALAR_SUM>(ctx, P, false);
+  }
+  set_error("unknown kernel kind %d", P.kind);
+  return ABX_ERR_INVALID;
+}
+
+// Build a layout for cols (a searchable particle set) and a query set given as
+// SoA FP64 (qsrc, nq, stride) -- or the column set itself when qsrc == null.
+int layout_build(abx_context *ctx, abx_particles *cols, double r, const double *qsrc, int64_t nq,
+                 int64_t qstride, PairLayout &L) {
+  GridDesc g;
+  ABX_TRY(particles_grid_desc(cols, &g));
+  L.r = r;
+  L.fg = make_fine_grid(g, r, std::max<int64_t>(cols->n, 1), 3);
+  L.cols_version = cols->version;
+  ABX_TRY(build_points(ctx, cols->pos.ptr, cols->n, cols->n, L.fg, true, L.cols));
+  ABX_TRY(build_cell_start(ctx, L));
+  if (!qsrc) {
+    L.self = true;
+    L.rows = &L.cols;
+  } else {
+    L.self = false;
+    ABX_TRY(build_points(ctx, qsrc, nq, qstride, L.fg, false, L.rows_own));
+    L.rows = &L.rows_own;
+  }
+  ABX_TRY(build_units(ctx, L));
+  return ABX_OK;
+}
+
+}  // namespace
+
+int pair_layout_build(abx_operator *op) {
+  abx_context *ctx = op->rows->ctx;
+  if (op->pairs) delete op->pairs;
+  op->pairs = new PairLayout();
+  PairLayout &L = *op->pairs;
+  const bool self = op->rows == op->cols;
+  ABX_TRY(layout_build(ctx, op->cols, op->radius, self ? nullptr : op->rows->pos.ptr,
+                       op->rows->n, op->rows->n, L));
+  L.rows_version = op->rows->version;
+  const int64_t nr = L.rows->n, nc = L.cols.n;
+  ABX_TRY(L.bk32.reserve(nc ? nc : 1));
+  ABX_TRY(L.bk64.reserve(nc ? nc : 1));
+  ABX_TRY(L.ck.reserve(nr ? nr : 1));
+  if (op->k.kind == ABX_K_SCALAR_SUM) {
+    ABX_REQUIRE(op->rows->has_scalar && op->cols->has_scalar, ABX_ERR_STATE,
+                "ABX_K_SCALAR_SUM needs a scalar column on both particle sets");
+    ABX_TRY(L.sk.reserve(nc ? nc : 1));
+    ABX_TRY(L.sq.reserve(nr ? nr : 1));
+    if (nc)
+      k_gather_b<<<ceil_div(nc, TPB), TPB, 0, ctx->stream>>>(op->cols->scalar.ptr, L.cols.perm.ptr,
+                                                             nc, nullptr, L.sk.ptr);
+    if (nr)
+      k_gather_b<<<ceil_div(nr, TPB), TPB, 0, ctx->stream>>>(op->rows->scalar.ptr, L.rows->perm.ptr,
+                                                             nr, nullptr, L.sq.ptr);
+    ABX_CHECK_CUDA(cudaGetLastError());
+  }
+  ABX_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  return ABX_OK;
+}
+
+int sparse_matvec_device(abx_operator *op, const double *b, double *c) {
+  abx_context *ctx = op->rows->ctx;
+  if (!op->pairs || op->pairs->cols_version != op->cols->version ||
+      op->pairs->rows_version != op->rows->version)
+    ABX_TRY(pair_layout_build(op));
+  PairLayout &L = *op->pairs;
+  const int64_t nr = L.rows->n, nc = L.cols.n;
+  if (nr == 0) return ABX_OK;
+  const bool mixed = op->precision == ABX_PREC_MIXED && op->k.kind != ABX_K_SCALAR_SUM;
+  if (nc > 0)
+    k_gather_b<<<ceil_div(nc, TPB), TPB, 0, ctx->stream>>>(
+        b, L.cols.perm.ptr, nc, mixed ? L.bk32.ptr : nullptr, mixed ? nullptr : L.bk64.ptr);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  KParams P = base_params(L);
+  P.kind = op->k.kind;
+  P.p0 = op->k.p[0];
+  P.p0f = (float)op->k.p[0];
+  P.c_exp2 = (float)(-op->k.p[0] * 1.4426950408889634);
+  P.b32 = L.bk32.ptr;
+  P.b64 = L.bk64.ptr;
+  P.s_col = L.sk.ptr;
+  P.s_row = L.sq.ptr;
+  P.c = L.ck.ptr;
+  if (nc == 0) {
+    ABX_CHECK_CUDA(cudaMemsetAsync(c, 0, nr * sizeof(double), ctx->stream));
+    return ABX_OK;
+  }
+  ABX_TRY(launch_pairs_kind<POL_MATVEC>(ctx, P, mixed));
+  k_scatter_c<<<ceil_div(nr, TPB), TPB, 0, ctx->stream>>>(L.ck.ptr, L.rows->perm.ptr, nr, c);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  return ABX_OK;
+}
+
+namespace {
+__global__ void k_aos_to_soa_q(const double *__restrict__ aos, int64_t n, int dim,
+                               double *__restrict__ soa) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int d = 0; d < dim; ++d) soa[(int64_t)d * n + i] = aos[i * dim + d];
+}
+
+__global__ void k_count_to_i64(const int32_t *__restrict__ counts, const uint32_t *__restrict__ perm,
+                               int64_t n, int64_t *__restrict__ rowcnt) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  rowcnt[perm[k]] = counts[k];
+}
+
+__global__ void k_rowptr_to_kernel(const int64_t *__restrict__ rowptr,
+                                   const uint32_t *__restrict__ perm, int64_t n,
+                                   int64_t *__restrict__ rowptr_k) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  rowptr_k[k] = rowptr[perm[k]];
+}
+}  // namespace
+
+// Radius queries for arbitrary points (C ABI helpers).
+int radius_query(abx_particles *p, int64_t nq, const double *q_host_or_dev, double r,
+                 int32_t *counts_user, int64_t *rowptr_user, int32_t *cols_user, int64_t cap) {
+  abx_context *ctx = p->ctx;
+  cudaStream_t s = ctx->stream;
+  ABX_REQUIRE(p->searchable, ABX_ERR_STATE, "init_neighbour_search not called on this particle set");
+  ABX_REQUIRE(r >= 0 && std::isfinite(r), ABX_ERR_INVALID, "invalid radius");
+  const int D = p->dim;
+  const void *qd;
+  ABX_TRY(p->stage_b.in(ctx, q_host_or_dev, (size_t)nq * D * sizeof(double), &qd));
+  DevBuf<double> qsoa;
+  ABX_TRY(qsoa.reserve((size_t)D * (nq ? nq : 1)));
+  if (nq)
+    k_aos_to_soa_q<<<ceil_div(nq, TPB), TPB, 0, s>>>((const double *)qd, nq, D, qsoa.ptr);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  PairLayout L;
+  ABX_TRY(layout_build(ctx, p, r, qsoa.ptr, nq, nq, L));
+  if (nq == 0) {
+    if (rowptr_user) {
+      int64_t z = 0;
+      ABX_CHECK_CUDA(cudaMemcpy(rowptr_user, &z, sizeof(int64_t), cudaMemcpyDefault));
+    }
+    return ABX_OK;
+  }
+  DevBuf<int32_t> cnt_k;
+  ABX_TRY(cnt_k.reserve(nq));
+  KParams P = base_params(L);
+  P.kind = ABX_K_CONST;
+  P.counts = cnt_k.ptr;
+  ABX_CHECK_CUDA(cudaMemsetAsync(cnt_k.ptr, 0, nq * 4, s));
+  if (p->n > 0) ABX_TRY(launch_pairs<POL_COUNT, ABX_K_CONST>(ctx, P, true));
+  if (counts_user) {
+    DevBuf<int32_t> cnt;
+    ABX_TRY(cnt.reserve(nq));
+    k_scatter<int32_t><<<ceil_div(nq, TPB), TPB, 0, s>>>(cnt_k.ptr, L.rows->perm.ptr, nq, cnt.ptr);
+    ABX_CHECK_CUDA(cudaGetLastError());
+    ABX_CHECK_CUDA(cudaMemcpyAsync(counts_user, cnt.ptr, nq * 4, cudaMemcpyDefault, s));
+    ABX_CHECK_CUDA(cudaStreamSynchronize(s));
+  }
+  if (rowptr_user) {
+    // rowptr in input order: counts -> int64 -> exclusive scan (host: nq+1)
+    DevBuf<int64_t> rc;
+    ABX_TRY(rc.reserve(nq));
+    k_count_to_i64<<<ceil_div(nq, TPB), TPB, 0, s>>>(cnt_k.ptr, L.rows->perm.ptr, nq, rc.ptr);
+    ABX_CHECK_CUDA(cudaGetLastError());
+    std::vector<int64_t> h(nq + 1);
+    ABX_CHECK_CUDA(cudaMemcpyAsync(h.data(), rc.ptr, nq * 8, cudaMemcpyDeviceToHost, s));
+    ABX_CHECK_CUDA(cudaStreamSynchronize(s));
+    int64_t run = 0;
+    for (int64_t i = 0; i < nq; ++i) {
+      const int64_t c = h[i];
+      h[i] = run;
+      run += c;
+    }
+    h[nq] = run;
+    ABX_CHECK_CUDA(cudaMemcpy(rowptr_user, h.data(), (nq + 1) * 8, cudaMemcpyDefault));
+    if (cols_user) {
+      ABX_REQUIRE(cap >= run, ABX_ERR_CAPACITY, "cols capacity %lld < nnz %lld", (long long)cap,
+                  (long long)run);
+      DevBuf<int64_t> rp, rpk;
+      DevBuf<int32_t> colsd;
+      ABX_TRY(rp.reserve(nq));
+      ABX_TRY(rpk.reserve(nq));
+      ABX_TRY(colsd.reserve(run ? run : 1));
+      ABX_CHECK_CUDA(cudaMemcpyAsync(rp.ptr, h.data(), nq * 8, cudaMemcpyHostToDevice, s));
+      k_rowptr_to_kernel<<<ceil_div(nq, TPB), TPB, 0, s>>>(rp.ptr, L.rows->perm.ptr, nq, rpk.ptr);
+      ABX_CHECK_CUDA(cudaGetLastError());
+      P.rowptr = rpk.ptr;
+      P.cols_out = colsd.ptr;
+      if (p->n > 0 && run > 0) ABX_TRY(launch_pairs<POL_LIST, ABX_K_CONST>(ctx, P, true));
+      ABX_CHECK_CUDA(cudaMemcpyAsync(cols_user, colsd.ptr, run * 4, cudaMemcpyDefault, s));
+      ABX_CHECK_CUDA(cudaStreamSynchronize(s));
+    }
+  }
+  ABX_CHECK_CUDA(cudaStreamSynchronize(s));
+  return ABX_OK;
+}
+
+}  // namespace abx
+
+using namespace abx;
+
+extern "C" {
+
+int abx_radius_count(abx_particles *p, int64_t nq, const double *q, double r, int32_t *counts) {
+  ABX_REQUIRE(p && (q || nq == 0) && (counts || nq == 0), ABX_ERR_INVALID, "null argument");
+  ABX_TRY(ctx_activate(p->ctx));
+  return radius_query(p, nq, q, r, counts, nullptr, nullptr, 0);
+}
+
+int abx_radius_query_csr(abx_particles *p, int64_t nq, const double *q, double r, int64_t *rowptr,
+                         int32_t *cols, int64_t cap) {
+  ABX_REQUIRE(p && (q || nq == 0) && rowptr, ABX_ERR_INVALID, "null argument");
+  ABX_TRY(ctx_activate(p->ctx));
+  return radius_query(p, nq, q, r, nullptr, rowptr, cols, cap);
+}
+
+}  // extern "C"

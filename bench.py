@@ -1,0 +1,373 @@
+"""Benchmark: kernel-operator matvec/s at N = 4,194,304 (the sparse-operator
+workload: 16-Gaussian mixture + 20% uniform background, periodic unit box,
+r = 0.02, Wendland C2 kernel, b ~ N(0,1); FP32 kernel evaluation with FP32
+blocks summed in FP64 into an FP64 result).
+
+One step = one K*b over the whole particle set.
+  value : device-resident b and c, CUDA events on the launching stream, L2
+          flushed (256 MB write) between timed steps.
+  e2e   : the same matvec through the C ABI with pinned HOST b and c, the
+          host->device copy of b and the device->host copy of c inside the
+          timed region (abx_operator_matvec stages them itself).
+--impl reference times the reference algorithm restated in C++ (the oracle,
+OpenMP on all host threads) on a bounded sample of rows of the same workload.
+
+Multi-GPU: the path runs as independent replicas (one per rank); value is the
+sum of matvecs over ranks divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "tests"))
+
+N_PARTICLES = 4_194_304
+RADIUS = 0.02
+FLOP_PER_PAIR = 20  # FP32 FLOP per accepted pair: dx(3) d2(5) q(3) Wendland(7) accumulate(2)
+WORKLOAD = ("sparse operator, 3D, N=4,194,304: 16 isotropic Gaussians (sigma 0.03, centres "
+            "U[0.1,0.9]^3) + 20% uniform, periodic unit box, CellListOrdered n_leaf=10, "
+            "r=0.02, Wendland C2 (1-q)^4(4q+1), b~N(0,1)")
+
+
+def make_workload(seed=2024):
+    import workloads
+    pos = workloads.gaussian_mixture(N_PARTICLES, 3, k=16, sigma=0.03, frac_uniform=0.2,
+                                     seed=seed, periodic=True)
+    b_by_id = np.random.default_rng(seed + 1).standard_normal(N_PARTICLES)
+    return pos, b_by_id
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def profile_traffic():
+    """Per-launch DRAM bytes of the pair kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "pairs_matvec_traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            return None
+    return None
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    import aboria_gb300 as ab
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx = ab.Context(local, stream=stream.cuda_stream)
+    pos, b_by_id = make_workload()
+    p = ab.Particles(3, ctx).set(pos)
+    t0 = time.perf_counter()
+    p.init_neighbour_search([0, 0, 0], [1, 1, 1], [True, True, True], 10.0)
+    build_s = time.perf_counter() - t0
+    ids = p.ids
+    b_host = np.ascontiguousarray(b_by_id[ids])
+    kern = ab.Kernel.make(ab.K_WENDLAND_C2, 1.0 / RADIUS)
+    t0 = time.perf_counter()
+    K = ab.create_sparse_operator(p, p, RADIUS, kern, ab.PREC_MIXED)
+    layout_s = time.perf_counter() - t0
+
+    b_dev = torch.from_numpy(b_host).cuda()
+    c_dev = torch.empty_like(b_dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")
+
+    # correctness side-checks (outside the timed region)
+    counts = ab.radius_count(p, p.positions, RADIUS)
+    pairs = int(counts.astype(np.int64).sum())
+    K64 = ab.create_sparse_operator(p, p, RADIUS, kern, ab.PREC_FP64)
+    c64 = K64.matvec(b_dev).cpu().numpy()
+    del K64
+    c32 = K.matvec(b_dev).cpu().numpy()
+    mixed_err = float(np.linalg.norm(c32 - c64) / np.linalg.norm(c64))
+    mixed_maxerr = float(np.max(np.abs(c32 - c64)) / np.max(np.abs(c64)))
+
+    for _ in range(args.warmup):
+        K.matvec(b_dev, out=c_dev)
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    for i in range(args.steps):
+        flush.fill_(i)
+        ev[i][0].record(stream)
+        K.matvec(b_dev, out=c_dev, sync=False)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    clocks = sampler.stop()
+
+    # e2e: host pinned buffers through the C ABI (copies inside the call)
+    b_pin = torch.from_numpy(b_host).pin_memory()
+    c_pin = torch.empty(N_PARTICLES, dtype=torch.float64).pin_memory()
+    b_np = b_pin.numpy()
+    c_np = c_pin.numpy()
+    for _ in range(2):
+        K.matvec(b_np, out=c_np)
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        K.matvec(b_np, out=c_np)  # returns after the D2H copy has landed
+    e2e_s = time.perf_counter() - t0
+    assert np.array_equal(c_np, c32), "host-buffer matvec differs from device-buffer matvec"
+
+    ms = float(np.mean(step_ms))
+    t_total = sum(step_ms) / 1e3
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([t_total, e2e_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_total, e2e_s = float(t[0]), float(t[1])
+    value = world * args.steps / t_total
+    e2e_value = world * args.steps / e2e_s
+
+    peaks, peak_kind = measured_peaks()
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    sm_max = peaks.get("sm_max_mhz", 2070.0)
+    fp32_peak_tflops = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    comp_bytes = N_PARTICLES * (24 + 8 + 8) + 405224 * 8
+    achieved_gbs = comp_bytes / (ms / 1e3) / 1e9
+    achieved_tflops = pairs * FLOP_PER_PAIR / (ms / 1e3) / 1e12
+    tr = profile_traffic()
+    out = {
+        "metric": "kernel-op matvec/s (N=4M)",
+        "value": value,
+        "unit": "matvec/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {
+            "workload": WORKLOAD,
+            "n": N_PARTICLES,
+            "radius": RADIUS,
+            "precision": "FP32 kernel values, FP32 blocks of <=32 terms summed in FP64",
+            "pairs_per_matvec": pairs,
+            "mean_neighbours": pairs / N_PARTICLES,
+            "l2": "flushed between timed steps (256 MB write outside the events)",
+            "parallelism": f"replicas x{world}",
+            "cell_build_s": build_s,
+            "operator_layout_s": layout_s,
+        },
+        "e2e": {"value": e2e_value, "unit": "matvec/s",
+                "h2d_bytes_per_step": N_PARTICLES * 8, "d2h_bytes_per_step": N_PARTICLES * 8},
+        "roofline": {
+            "bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved_gbs / hbm_peak, "peak_source": peak_kind,
+            "traffic": (tr or {}).get("dram_bytes_per_launch"),
+            "note": "compulsory bytes N*(24+8+8)+ncells*8 per matvec; the pair kernel is "
+                    "FP32-issue bound, see compute_roofline",
+        },
+        "compute_roofline": {
+            "bound": "fp32", "achieved": achieved_tflops, "peak": fp32_peak_tflops,
+            "unit": "TFLOP/s", "frac": achieved_tflops / fp32_peak_tflops,
+            "flop_per_pair": FLOP_PER_PAIR,
+            "peak_source": f"152 SM x 128 FP32 lanes x 2 x {sm_max:.0f} MHz (nominal)",
+        },
+        "accuracy": {"mixed_vs_fp64_rel_l2": mixed_err, "mixed_vs_fp64_rel_max": mixed_maxerr},
+        "gpu_launches": 3 * args.steps,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(pos, b_by_id, budget_s=args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def cpu_baseline(pos, b_by_id, budget_s=15.0):
+    """The oracle (C++ restatement of the reference's OpenMP path) on a bounded
+    sample of rows; returns matvec/s extrapolated to all N rows."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    t0 = time.perf_counter()
+    cl = oracle.celllist_build(pos, [0, 0, 0], [1, 1, 1], [True] * 3, 10.0)
+    build_s = time.perf_counter() - t0
+    b = np.ascontiguousarray(b_by_id[cl.perm])
+    rng = np.random.default_rng(5)
+    rows_done = 0
+    t_spent = 0.0
+    chunk = 2000
+    while t_spent < budget_s and rows_done < N_PARTICLES:
+        idx = rng.integers(0, cl.n, size=chunk)
+        t0 = time.perf_counter()
+        oracle.sparse_matvec(cl, cl.pos[idx], RADIUS, 2, [1.0 / RADIUS], b)
+        t_spent += time.perf_counter() - t0
+        rows_done += chunk
+        chunk = min(chunk * 2, 200000)
+    rate_rows = rows_done / t_spent
+    return {"value": rate_rows / cl.n, "unit": "matvec/s", "cores": oracle.num_threads(),
+            "kind": "port",
+            "sample": f"{rows_done} random rows of {cl.n} ({t_spent:.1f} s of FP64 row "
+                      f"evaluation in the reference's neighbour order), extrapolated to one "
+                      f"full matvec; cell-list build {build_s:.1f} s not included"}
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    pos, b_by_id = make_workload()
+    cl = oracle.celllist_build(pos, [0, 0, 0], [1, 1, 1], [True] * 3, 10.0)
+    b = np.ascontiguousarray(b_by_id[cl.perm])
+    rng = np.random.default_rng(6)
+    sample = 20000
+    idx = rng.integers(0, cl.n, size=sample)
+    for _ in range(args.warmup):
+        oracle.sparse_matvec(cl, cl.pos[idx[:2000]], RADIUS, 2, [1.0 / RADIUS], b)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.sparse_matvec(cl, cl.pos[idx], RADIUS, 2, [1.0 / RADIUS], b)
+        times.append(time.perf_counter() - t0)
+    t = float(np.mean(times))
+    value = (sample / t) / cl.n
+    desc = (f"{sample} random rows of {cl.n} per step (FP64, reference neighbour order), "
+            f"extrapolated to one full matvec")
+    out = {
+        "impl": "reference",
+        "metric": "kernel-op matvec/s (N=4M)",
+        "value": value,
+        "unit": "matvec/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t * 1e3 * cl.n / sample,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "n": N_PARTICLES, "radius": RADIUS},
+        "cpu_baseline": {"value": value, "unit": "matvec/s", "cores": oracle.num_threads(),
+                         "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": "matvec/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,147 @@
+/*
+ * abx.h -- C ABI of the aboria_gb300 library: the GB300 (sm_103a) particle
+ * hot path behind Aboria's header API.
+ *
+ * Plain C: opaque handles, pointers and sizes, int status codes.  Every entry
+ * point returns ABX_OK (0) or an ABX_ERR_* code and leaves a message for
+ * abx_last_error().  The reference reports errors with CHECK/ASSERT, which
+ * print and raise SIGTRAP (src/Log.h:43-81); the C++ header layer
+ * (include/aboria_gb/Aboria.h) maps a non-zero status back to that behaviour.
+ *
+ * Vector arguments (positions, b, c, counts, ...) may be host memory
+ * (pageable or pinned) or device memory; the library detects which
+ * (cudaPointerGetAttributes) and stages host buffers through the device
+ * around the call.  All work runs on the context's stream; calls that return
+ * data to host memory synchronise that stream before returning.
+ *
+ * Index conventions follow the reference: after
+ * abx_particles_init_neighbour_search the particle storage is in cell order
+ * (src/Particles.h:694-726), and row/column k of every operator is the k-th
+ * particle in that order.  abx_particles_get_ids maps it back to insertion ids.
+ */
+#ifndef ABX_H_
+#define ABX_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define ABX_API __attribute__((visibility("default")))
+#else
+#define ABX_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ABX_OK 0
+#define ABX_ERR_INVALID 1   /* bad argument */
+#define ABX_ERR_CUDA 2      /* CUDA runtime error */
+#define ABX_ERR_ALLOC 3     /* device allocation failed */
+#define ABX_ERR_STATE 4     /* e.g. neighbour search not initialised */
+#define ABX_ERR_TIMEOUT 5   /* a bounded device-side wait gave up */
+#define ABX_ERR_CAPACITY 6  /* caller-provided output too small */
+#define ABX_ERR_NUMERIC 7   /* breakdown / non-finite value detected */
+
+/* Precision modes of the pair kernels. */
+#define ABX_PREC_FP64 0  /* FP64 evaluation and accumulation (1e-12 parity mode) */
+#define ABX_PREC_MIXED 1 /* FP32 evaluation, FP32 blocks of <=32 terms summed in FP64 */
+
+/* Built-in kernel functors (the closures passed to create_*_operator). */
+#define ABX_K_CONST 0            /* p0                                   */
+#define ABX_K_GAUSSIAN 1         /* exp(-|dx|^2 * p0)                    */
+#define ABX_K_WENDLAND_C2 2      /* q=|dx|*p0: (1-q)^4 (4q+1), 0 if q>=1 */
+#define ABX_K_COMPACT_GAUSSIAN 3 /* exp(-p0 |dx|^2), p0 = eps^2          */
+#define ABX_K_LAPLACE 4          /* 1/(|dx| + p0)                        */
+#define ABX_K_MULTIQUADRIC 5     /* sqrt(|dx|^2 + p0)                    */
+#define ABX_K_SCALAR_SUM 6       /* s_row[i] + s_col[j] (particle scalars) */
+
+typedef struct abx_kernel {
+  int kind;
+  double p[4];
+} abx_kernel;
+
+typedef struct abx_context abx_context;
+typedef struct abx_particles abx_particles;
+typedef struct abx_operator abx_operator;
+
+/* ------------------------------------------------------------ library ---- */
+ABX_API const char *abx_last_error(void);
+ABX_API int abx_version(void);
+
+/* Execution context: one device and one stream.  stream may be NULL (the
+ * library creates its own) or a cudaStream_t owned by the caller. */
+ABX_API int abx_context_create(int device, void *stream, abx_context **out);
+ABX_API int abx_context_destroy(abx_context *ctx);
+ABX_API int abx_context_synchronize(abx_context *ctx);
+
+/* -------------------------------------------------------------- particles --
+ * Particles<std::tuple<...>, D> storage (src/Particles.h:108-112): positions
+ * (D doubles each, D in 1..3), ids, and one optional scalar column that the
+ * ABX_K_SCALAR_SUM functor reads (get<var>(particle) in the reference).      */
+ABX_API int abx_particles_create(abx_context *ctx, int dim, abx_particles **out);
+ABX_API int abx_particles_destroy(abx_particles *p);
+/* Replace the contents with n particles (AoS n*dim positions).  ids may be
+ * NULL (ids 0..n-1), like consecutive push_back calls. */
+ABX_API int abx_particles_set(abx_particles *p, int64_t n, const double *pos, const int64_t *ids);
+/* Per-particle scalar in the current storage order (reordered with the rest). */
+ABX_API int abx_particles_set_scalar(abx_particles *p, const double *s);
+ABX_API int64_t abx_particles_size(const abx_particles *p);
+ABX_API int abx_particles_get_positions(abx_particles *p, double *pos_out);
+ABX_API int abx_particles_get_ids(abx_particles *p, int64_t *ids_out);
+ABX_API int abx_particles_get_scalar(abx_particles *p, double *s_out);
+
+/* Particles::init_neighbour_search (src/Particles.h:445-456): set the domain,
+ * enforce it (periodic wrap or delete, src/NeighbourSearchBase.h:185-238),
+ * build the CellListOrdered grid (src/CellListOrdered.h:132-259) and reorder
+ * storage into stable (cell key, insertion) order. */
+ABX_API int abx_particles_init_neighbour_search(abx_particles *p, const double *lo, const double *hi,
+                                        const int *periodic, double n_particles_in_leaf);
+/* Particles::update_positions (src/Particles.h:526-540) after positions were
+ * replaced with abx_particles_set_positions (same n, current storage order). */
+ABX_API int abx_particles_set_positions(abx_particles *p, const double *pos);
+ABX_API int abx_particles_update_positions(abx_particles *p);
+/* Grid of the cell list: size[dim], side[dim], total bucket count. */
+ABX_API int abx_particles_get_grid(abx_particles *p, uint32_t *size, double *side, uint32_t *ncells);
+/* bucket_begin/bucket_end (src/CellListOrdered.h:231-239), ncells each, and
+ * the sorted bucket key of every particle (n). */
+ABX_API int abx_particles_get_buckets(abx_particles *p, uint32_t *bucket_begin, uint32_t *bucket_end,
+                              uint32_t *keys);
+
+/* -------------------------------------------------------- radius search --
+ * euclidean_search(query, x, r) (src/Search.h:839-845) for nq query points:
+ * every stored particle j (and periodic image) with
+ * ((0+dx0^2)+dx1^2)+dx2^2 <= r^2 in FP64, dx = x_j - (x + image*L). */
+ABX_API int abx_radius_count(abx_particles *p, int64_t nq, const double *q, double r, int32_t *counts);
+/* Neighbour lists as CSR: rowptr[nq+1] and cols[] (indices into storage
+ * order, ascending within a row; a particle reached through two periodic
+ * images appears twice).  Call with cols == NULL to get rowptr only (nnz in
+ * rowptr[nq]); cap is the capacity of cols. */
+ABX_API int abx_radius_query_csr(abx_particles *p, int64_t nq, const double *q, double r,
+                         int64_t *rowptr, int32_t *cols, int64_t cap);
+
+/* -------------------------------------------------------------- operators --
+ * create_sparse_operator (src/Operators.h:478-515, KernelSparseConst
+ * src/Kernels.h:754-776), create_dense_operator (src/Operators.h:312-318,
+ * KernelDense src/Kernels.h:138-268).  The operator holds the particle sets by
+ * reference (as the reference's kernels do, src/Kernels.h:133-135): they must
+ * outlive it and not be re-searched while it is in use. */
+ABX_API int abx_create_sparse_operator(abx_particles *rows, abx_particles *cols, double radius,
+                               const abx_kernel *k, abx_operator **out);
+ABX_API int abx_create_dense_operator(abx_particles *rows, abx_particles *cols, const abx_kernel *k,
+                              abx_operator **out);
+ABX_API int abx_operator_destroy(abx_operator *op);
+ABX_API int abx_operator_set_precision(abx_operator *op, int mode);
+ABX_API int64_t abx_operator_rows(const abx_operator *op);
+ABX_API int64_t abx_operator_cols(const abx_operator *op);
+/* c = K*b (Eigen assignment semantics, generic_product_impl::scaleAndAddTo
+ * src/detail/Operators.h:207-229 with alpha == 1 on a zeroed destination). */
+ABX_API int abx_operator_matvec(abx_operator *op, const double *b, double *c);
+/* Pair work of the last matvec: candidate pairs tested and pairs accepted. */
+ABX_API int abx_operator_last_stats(abx_operator *op, int64_t *candidates, int64_t *pairs);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ABX_H_ */

@@ -1,0 +1,552 @@
+// Oracle for the particle hot path: TEST INFRASTRUCTURE ONLY.
+//
+// A plain C++17 + OpenMP restatement of the reference algorithms (Aboria,
+// header-only C++14).  It is loaded by the test-suite and by the CPU-baseline
+// leg of bench.py, and nothing in the product (the aboria_gb300 package, the
+// CUDA library or the C++ headers) links or calls it.  The reference itself
+// cannot be compiled here (it requires Boost and Eigen headers), so this file
+// restates its arithmetic operation for operation; every function names the
+// reference file:line it follows.  It is pinned against the reference's own
+// known-answer tests in tests/test_oracle_kats.py (golden values transcribed in
+// tests/golden/reference_kats.json).
+//
+// Build: oracle/build_oracle.sh (g++ -O2 -fopenmp -ffp-contract=off).  FP
+// contraction must stay off: the reference's FP64 radius test is evaluated
+// without FMA on x86-64, and aarch64 g++ would otherwise fuse a*b+c.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <numeric>
+#include <utility>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+struct Grid {
+  int D;
+  double lo[3], hi[3];
+  int periodic[3];
+  uint32_t size[3];
+  double side[3], inv_side[3];
+  uint32_t ncells;
+};
+
+// CellListOrdered::set_domain_impl, src/CellListOrdered.h:132-186.
+void make_grid(Grid &g, int D, const double *lo, const double *hi,
+               const int *periodic, double n_leaf, int64_t n_alive) {
+  g.D = D;
+  for (int d = 0; d < D; ++d) {
+    g.lo[d] = lo[d];
+    g.hi[d] = hi[d];
+    g.periodic[d] = periodic[d];
+  }
+  const size_t n = (size_t)n_alive;
+  if (n_leaf > (double)n) {
+    for (int d = 0; d < D; ++d) g.size[d] = 1;
+  } else {
+    double total_volume = 1.0;
+    for (int d = 0; d < D; ++d) total_volume *= (hi[d] - lo[d]);
+    const double box_volume = n_leaf / double(n) * total_volume;
+    const double box_side = std::pow(box_volume, 1.0 / D);
+    for (int d = 0; d < D; ++d) {
+      g.size[d] = (unsigned int)std::floor((hi[d] - lo[d]) / box_side);
+      if (g.size[d] == 0) g.size[d] = 1;
+    }
+  }
+  g.ncells = 1;
+  for (int d = 0; d < D; ++d) {
+    g.side[d] = (hi[d] - lo[d]) / g.size[d];
+    g.inv_side[d] = 1.0 / g.side[d];  // point_to_bucket_index ctor, SpatialUtil.h:113-116
+    g.ncells *= g.size[d];
+  }
+}
+
+// bucket_index::collapse_index_vector, src/detail/SpatialUtil.h:49-59
+// (int vector overload: unsigned multiplier, wraps modulo 2^32).
+uint32_t collapse(const Grid &g, const int *v) {
+  uint32_t index = 0, mult = 1;
+  for (int i = g.D - 1; i >= 0; --i) {
+    if (i != g.D - 1) mult *= g.size[i + 1];
+    index += mult * (uint32_t)v[i];
+  }
+  return index;
+}
+
+// point_to_bucket_index::find_bucket_index_vector, SpatialUtil.h:125-132.
+void bucket_vec(const Grid &g, const double *x, int *v) {
+  for (int d = 0; d < g.D; ++d)
+    v[d] = (int)std::floor((x[d] - g.lo[d]) * g.inv_side[d]);
+}
+
+// distance_helper<2>::norm2, src/detail/Distance.h:132-137 (pow(x,2) == x*x).
+inline double norm2(const double *dx, int D) {
+  double accum = 0;
+  for (int i = 0; i < D; ++i) accum = accum + dx[i] * dx[i];
+  return accum;
+}
+
+// Built-in kernel functors (the closures the reference's tests and the
+// benchmark workloads pass to create_sparse_operator / create_dense_operator).
+enum {
+  K_CONST = 0,
+  K_GAUSSIAN = 1,         // exp(-|dx|^2 * p0)
+  K_WENDLAND_C2 = 2,      // q=|dx|*p0 ; (1-q)^4 (4q+1), 0 for q>=1
+  K_COMPACT_GAUSSIAN = 3, // exp(-p0 * |dx|^2)   (p0 = eps^2)
+  K_LAPLACE = 4,          // 1/(|dx| + p0)
+  K_MULTIQUADRIC = 5,     // sqrt(|dx|^2 + p0)
+  K_SCALAR_SUM = 6,       // row_s[i] + col_s[j]
+};
+
+struct KDesc {
+  int kind;
+  double p[4];
+  const double *row_s;
+  const double *col_s;
+};
+
+inline double kernel_eval(const KDesc &k, const double *dx, int D, int64_t i,
+                          int64_t j) {
+  double d2 = 0;
+  for (int d = 0; d < D; ++d) d2 = d2 + dx[d] * dx[d];
+  switch (k.kind) {
+  case K_CONST:
+    return k.p[0];
+  case K_GAUSSIAN:
+  case K_COMPACT_GAUSSIAN:
+    return std::exp(-d2 * k.p[0]);
+  case K_WENDLAND_C2: {
+    const double q = std::sqrt(d2) * k.p[0];
+    if (q >= 1.0) return 0.0;
+    const double t = 1.0 - q;
+    const double t2 = t * t;
+    return t2 * t2 * (4.0 * q + 1.0);
+  }
+  case K_LAPLACE:
+    return 1.0 / (std::sqrt(d2) + k.p[0]);
+  case K_MULTIQUADRIC:
+    return std::sqrt(d2 + k.p[0]);
+  case K_SCALAR_SUM:
+    return k.row_s[i] + k.col_s[j];
+  }
+  return 0.0;
+}
+
+struct CellList {
+  Grid g;
+  int64_t n;
+  const double *pos;  // sorted, n*D
+  const uint32_t *begin, *end;
+};
+
+// The reference's per-query walk: search_iterator (src/Search.h:150-487) over
+// periodic images (lattice order, last dim fastest: src/LatticeIterator.h:269-281)
+// x bucket quadrants (lattice_iterator_within_distance,
+// src/NeighbourSearchBase.h:1720-2009) x bucket storage order
+// (CellListOrderedQuery::get_bucket_particles, src/CellListOrdered.h:472-491),
+// with check_candidate's FP64 test (src/Search.h:438-465).
+template <class Visit>
+void search_walk(const CellList &cl, const double *x, double r, Visit &&visit) {
+  const Grid &g = cl.g;
+  const int D = g.D;
+  const double r2 = r * r;  // get_value_to_accumulate: pow(r, 2)
+  double L[3], half_side[3];
+  for (int d = 0; d < D; ++d) {
+    L[d] = g.hi[d] - g.lo[d];
+    half_side[d] = 0.5 * g.side[d];
+  }
+  int img_lo[3], img_hi[3], img[3];
+  for (int d = 0; d < D; ++d) {
+    img_lo[d] = g.periodic[d] ? -1 : 0;
+    img_hi[d] = g.periodic[d] ? 2 : 1;
+    img[d] = img_lo[d];
+  }
+  for (;;) {
+    double p[3];
+    for (int d = 0; d < D; ++d) p[d] = x[d] + img[d] * L[d];
+    // outside_domain, NeighbourSearchBase.h:1949-1958
+    bool outside;
+    {
+      double dx[3];
+      for (int d = 0; d < D; ++d) {
+        const double c = 0.5 * (g.lo[d] + g.hi[d]) - p[d];
+        const double hd = 0.5 * (g.hi[d] - g.lo[d]);
+        dx[d] = std::max(std::abs(c) - hd, 0.0);
+      }
+      outside = norm2(dx, D) > r2;
+    }
+    if (!outside) {
+      auto min_dist = [&](const int *b) {
+        double dx[3];
+        for (int d = 0; d < D; ++d) {
+          const double centre = (b[d] + 0.5) * g.side[d] + g.lo[d];
+          dx[d] = std::max(std::abs(centre - p[d]) - half_side[d], 0.0);
+        }
+        return norm2(dx, D);
+      };
+      for (int quadrant = 0; quadrant < (1 << D); ++quadrant) {
+        int mn[3], idx[3];
+        bool none = false;
+        for (int d = 0; d < D; ++d) {
+          const bool up = (quadrant >> d) & 1;
+          mn[d] = (int)std::floor((p[d] + (up ? 0.5 : -0.5) * g.side[d] - g.lo[d]) *
+                                  g.inv_side[d]);
+        }
+        none = min_dist(mn) > r2;
+        if (!none) {
+          for (int d = 0; d < D; ++d) {
+            const bool up = (quadrant >> d) & 1;
+            const int endb = (int)g.size[d] - 1;
+            if (up) {
+              if (mn[d] < 0) mn[d] = 0;
+              else if (mn[d] > endb) { none = true; mn[d] = endb; }
+            } else {
+              if (mn[d] < 0) { none = true; mn[d] = 0; }
+              else if (mn[d] > endb) mn[d] = endb;
+            }
+          }
+        }
+        if (none) continue;
+        for (int d = 0; d < D; ++d) idx[d] = mn[d];
+        for (;;) {
+          // visit bucket idx
+          const uint32_t b = collapse(g, idx);
+          for (uint32_t k = cl.begin[b]; k < cl.end[b]; ++k) {
+            const double *pj = cl.pos + (int64_t)k * D;
+            double dx[3];
+            for (int d = 0; d < D; ++d) dx[d] = pj[d] - p[d];
+            if (!(norm2(dx, D) > r2)) visit((int64_t)k, dx);
+          }
+          // increment, NeighbourSearchBase.h:1960-2008
+          bool valid = false;
+          for (int i = D - 1; i >= 0; --i) {
+            const bool up = (quadrant >> i) & 1;
+            bool pot;
+            if (up) { ++idx[i]; pot = idx[i] <= (int)g.size[i] - 1; }
+            else { --idx[i]; pot = idx[i] >= 0; }
+            if (pot) pot = min_dist(idx) <= r2;
+            if (pot) { valid = true; break; }
+            idx[i] = mn[i];
+          }
+          if (!valid) break;
+        }
+      }
+    }
+    // next periodic image
+    int d = D - 1;
+    for (; d >= 0; --d) {
+      if (++img[d] < img_hi[d]) break;
+      img[d] = img_lo[d];
+    }
+    if (d < 0) break;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+void orc_set_num_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
+// Grid dimensions for n_alive particles (set_domain_impl).
+uint32_t orc_grid(int D, const double *lo, const double *hi, const int *periodic,
+                  double n_leaf, int64_t n_alive, uint32_t *size_out,
+                  double *side_out) {
+  Grid g;
+  make_grid(g, D, lo, hi, periodic, n_leaf, n_alive);
+  for (int d = 0; d < D; ++d) {
+    size_out[d] = g.size[d];
+    side_out[d] = g.side[d];
+  }
+  return g.ncells;
+}
+
+// Unit KATs: collapse_index_vector / reassemble_index_vector
+// (src/detail/SpatialUtil.h:49-96).
+uint32_t orc_collapse(int D, const uint32_t *size, const int *v) {
+  Grid g;
+  g.D = D;
+  for (int d = 0; d < D; ++d) g.size[d] = size[d];
+  // 4-D is needed by the reference KAT; use a local copy of the loop.
+  uint32_t index = 0, mult = 1;
+  for (int i = D - 1; i >= 0; --i) {
+    if (i != D - 1) mult *= size[i + 1];
+    index += mult * (uint32_t)v[i];
+  }
+  return index;
+}
+
+void orc_reassemble(int D, const uint32_t *size, uint32_t index, int *v) {
+  unsigned int i = index;
+  for (int d = D - 1; d >= 0; --d) {
+    const double div = (double)i / size[d];
+    v[d] = (int)std::round((div - std::floor(div)) * size[d]);
+    i = (unsigned int)std::floor(div);
+  }
+}
+
+// point_to_bucket_index::operator(), SpatialUtil.h:119-138.
+int orc_point_to_bucket(int D, const uint32_t *size, const double *lo,
+                        const double *side, const double *x, int *v) {
+  Grid g;
+  g.D = D;
+  for (int d = 0; d < D; ++d) {
+    g.size[d] = size[d];
+    g.lo[d] = lo[d];
+    g.side[d] = side[d];
+    g.inv_side[d] = 1.0 / side[d];
+  }
+  bucket_vec(g, x, v);
+  return (int)collapse(g, v);
+}
+
+// Full cell-list build for a fresh particle set: Particles::init_neighbour_search
+// (src/Particles.h:445-456) -> neighbour_search_base::update_positions
+// (src/NeighbourSearchBase.h:350-495: enforce_domain_lambda :185-238, alive
+// scan/scatter :391-434) -> CellListOrdered::update_positions_impl
+// (src/CellListOrdered.h:190-259: hash, sort_by_key, lower/upper_bound) ->
+// Particles::reorder (src/Particles.h:694-726).
+//
+// pos_in: n*D FP64 (AoS).  On return pos_io holds the domain-enforced input
+// positions (periodic wrap applied).  Outputs are sized by the caller: pos_out
+// and perm_out and keys_out for n entries, begin/end for ncells (orc_grid
+// with the alive count; callers pass ncells_cap as capacity).  Returns the
+// number of alive particles, or -1 if ncells_cap is too small.
+// stable=1: (key, original index) order, the Thrust backend's stable
+// sort_by_key (src/detail/Algorithms.h:193-196); stable=0: std::sort with a
+// key-only comparison, as the reference's STL backend
+// (src/detail/Algorithms.h:173-190).
+int64_t orc_celllist_build(int D, int64_t n, double *pos_io, const double *lo,
+                           const double *hi, const int *periodic, double n_leaf,
+                           int stable, double *pos_out, int64_t *perm_out,
+                           uint32_t *keys_out, uint32_t *bucket_begin,
+                           uint32_t *bucket_end, uint32_t ncells_cap,
+                           uint32_t *size_out, double *side_out) {
+  std::vector<uint8_t> alive(n, 1);
+  for (int64_t i = 0; i < n; ++i) {
+    double *r = pos_io + i * D;
+    for (int d = 0; d < D; ++d) {
+      if (!std::isfinite(r[d])) {
+        alive[i] = 0;
+      } else if (periodic[d]) {
+        while (r[d] < lo[d]) r[d] += (hi[d] - lo[d]);
+        while (r[d] >= hi[d]) r[d] -= (hi[d] - lo[d]);
+      } else if ((r[d] < lo[d]) || (r[d] >= hi[d])) {
+        alive[i] = 0;
+      }
+    }
+  }
+  std::vector<int64_t> alive_idx;
+  alive_idx.reserve(n);
+  for (int64_t i = 0; i < n; ++i)
+    if (alive[i]) alive_idx.push_back(i);
+  const int64_t na = (int64_t)alive_idx.size();
+  Grid g;
+  make_grid(g, D, lo, hi, periodic, n_leaf, na);
+  if (g.ncells > ncells_cap) return -1;
+  for (int d = 0; d < D; ++d) {
+    size_out[d] = g.size[d];
+    side_out[d] = g.side[d];
+  }
+  std::vector<std::pair<uint32_t, int64_t>> kv(na);
+  for (int64_t k = 0; k < na; ++k) {
+    int v[3];
+    bucket_vec(g, pos_io + alive_idx[k] * D, v);
+    kv[k] = {collapse(g, v), alive_idx[k]};
+  }
+  auto cmp = [](const std::pair<uint32_t, int64_t> &a,
+                const std::pair<uint32_t, int64_t> &b) { return a.first < b.first; };
+  if (stable)
+    std::stable_sort(kv.begin(), kv.end(), cmp);
+  else
+    std::sort(kv.begin(), kv.end(), cmp);
+  for (int64_t k = 0; k < na; ++k) {
+    keys_out[k] = kv[k].first;
+    perm_out[k] = kv[k].second;
+    for (int d = 0; d < D; ++d) pos_out[k * D + d] = pos_io[kv[k].second * D + d];
+  }
+  for (uint32_t c = 0; c < g.ncells; ++c) {
+    bucket_begin[c] = (uint32_t)(std::lower_bound(keys_out, keys_out + na, c) - keys_out);
+    bucket_end[c] = (uint32_t)(std::upper_bound(keys_out, keys_out + na, c) - keys_out);
+  }
+  return na;
+}
+
+// Neighbour counts of nq query points against a built cell list
+// (euclidean_search, src/Search.h:839-845), OpenMP over queries.
+void orc_radius_count(int D, const uint32_t *size, const double *lo,
+                      const double *hi, const int *periodic, const double *side,
+                      int64_t n, const double *pos_sorted, const uint32_t *bbegin,
+                      const uint32_t *bend, int64_t nq, const double *q, double r,
+                      int32_t *counts) {
+  CellList cl;
+  Grid &g = cl.g;
+  g.D = D;
+  g.ncells = 1;
+  for (int d = 0; d < D; ++d) {
+    g.size[d] = size[d];
+    g.lo[d] = lo[d];
+    g.hi[d] = hi[d];
+    g.periodic[d] = periodic[d];
+    g.side[d] = side[d];
+    g.inv_side[d] = 1.0 / side[d];
+    g.ncells *= size[d];
+  }
+  cl.n = n;
+  cl.pos = pos_sorted;
+  cl.begin = bbegin;
+  cl.end = bend;
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t i = 0; i < nq; ++i) {
+    int32_t c = 0;
+    search_walk(cl, q + i * D, r, [&](int64_t, const double *) { ++c; });
+    counts[i] = c;
+  }
+}
+
+// Neighbour lists in the reference's visiting order, CSR (rowptr from counts).
+void orc_radius_lists(int D, const uint32_t *size, const double *lo,
+                      const double *hi, const int *periodic, const double *side,
+                      int64_t n, const double *pos_sorted, const uint32_t *bbegin,
+                      const uint32_t *bend, int64_t nq, const double *q, double r,
+                      const int64_t *rowptr, int64_t *cols, double *dx_out) {
+  CellList cl;
+  Grid &g = cl.g;
+  g.D = D;
+  for (int d = 0; d < D; ++d) {
+    g.size[d] = size[d];
+    g.lo[d] = lo[d];
+    g.hi[d] = hi[d];
+    g.periodic[d] = periodic[d];
+    g.side[d] = side[d];
+    g.inv_side[d] = 1.0 / side[d];
+  }
+  cl.n = n;
+  cl.pos = pos_sorted;
+  cl.begin = bbegin;
+  cl.end = bend;
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t i = 0; i < nq; ++i) {
+    int64_t o = rowptr[i];
+    search_walk(cl, q + i * D, r, [&](int64_t k, const double *dx) {
+      cols[o] = k;
+      if (dx_out)
+        for (int d = 0; d < D; ++d) dx_out[o * D + d] = dx[d];
+      ++o;
+    });
+  }
+}
+
+// KernelSparse::evaluate (src/Kernels.h:720-751): c = 0; for each row i (omp
+// parallel for, :734-736), for each neighbour j in search order,
+// c[i] += f(dx, a_i, b_j) * b[j].  The row particles are the query points.
+void orc_sparse_matvec(int D, const uint32_t *size, const double *lo,
+                       const double *hi, const int *periodic, const double *side,
+                       int64_t ncol, const double *col_pos, const uint32_t *bbegin,
+                       const uint32_t *bend, int64_t nrow, const double *row_pos,
+                       double r, int kind, const double *params,
+                       const double *row_s, const double *col_s, const double *b,
+                       double *c) {
+  CellList cl;
+  Grid &g = cl.g;
+  g.D = D;
+  for (int d = 0; d < D; ++d) {
+    g.size[d] = size[d];
+    g.lo[d] = lo[d];
+    g.hi[d] = hi[d];
+    g.periodic[d] = periodic[d];
+    g.side[d] = side[d];
+    g.inv_side[d] = 1.0 / side[d];
+  }
+  cl.n = ncol;
+  cl.pos = col_pos;
+  cl.begin = bbegin;
+  cl.end = bend;
+  KDesc k{kind, {params[0], params[1], params[2], params[3]}, row_s, col_s};
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t i = 0; i < nrow; ++i) {
+    double acc = 0.0;
+    search_walk(cl, row_pos + i * D, r, [&](int64_t j, const double *dx) {
+      acc += kernel_eval(k, dx, D, i, j) * b[j];
+    });
+    c[i] = acc;
+  }
+}
+
+// KernelDense::evaluate (src/Kernels.h:212-239): c[i] = sum_j f(a_i, b_j) b[j]
+// in column order; the built-in functors see dx = x_j - x_i.
+void orc_dense_matvec(int D, int64_t nrow, const double *row_pos, int64_t ncol,
+                      const double *col_pos, int kind, const double *params,
+                      const double *row_s, const double *col_s, const double *b,
+                      double *c) {
+  KDesc k{kind, {params[0], params[1], params[2], params[3]}, row_s, col_s};
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < nrow; ++i) {
+    double acc = 0.0;
+    for (int64_t j = 0; j < ncol; ++j) {
+      double dx[3];
+      for (int d = 0; d < D; ++d) dx[d] = col_pos[j * D + d] - row_pos[i * D + d];
+      acc += kernel_eval(k, dx, D, i, j) * b[j];
+    }
+    c[i] = acc;
+  }
+}
+
+// Brute-force neighbour counts with periodic images, as the reference's
+// tests/neighbours.h:715-765 (brute_force_check, inclusive <= r^2).
+void orc_brute_counts(int D, int64_t n, const double *pos, const double *lo,
+                      const double *hi, int periodic, double r, int32_t *counts) {
+  const double r2 = r * r;
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t i = 0; i < n; ++i) {
+    int32_t c = 0;
+    for (int64_t j = 0; j < n; ++j) {
+      if (periodic) {
+        int img[3] = {-1, -1, -1};
+        for (;;) {
+          double dx[3];
+          for (int d = 0; d < D; ++d)
+            dx[d] = pos[j * D + d] - pos[i * D + d] - img[d] * (hi[d] - lo[d]);
+          double s = 0;
+          for (int d = 0; d < D; ++d) s += dx[d] * dx[d];
+          if (s <= r2) ++c;
+          int d = D - 1;
+          for (; d >= 0; --d) {
+            if (++img[d] < 2) break;
+            img[d] = -1;
+          }
+          if (d < 0) break;
+        }
+      } else {
+        double s = 0;
+        for (int d = 0; d < D; ++d) {
+          const double dx = pos[j * D + d] - pos[i * D + d];
+          s += dx * dx;
+        }
+        if (s <= r2) ++c;
+      }
+    }
+    counts[i] = c;
+  }
+}
+
+}  // extern "C"
