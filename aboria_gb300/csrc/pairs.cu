@@ -77,6 +77,7 @@ struct PairLayout {
   DevBuf<double> sq;  // row scalar in kernel order
   DevBuf<double> ck;  // result in row kernel order
   DevBuf<int> counter;
+  DevBuf<int> ext;  // e2 extent table
 };
 
 void pair_layout_free(PairLayout *L) { delete L; }
@@ -143,22 +144,28 @@ __device__ __forceinline__ int fine_coord(double x, double lo, double h, int m) 
   return (int)t;
 }
 
-// Source points (SoA, dim columns, n) -> clamped key, unclamped cell.
+// Sort key of a point: clamped fine cell (row-major, e2 fastest) times 8 plus
+// its octant within the cell, so that consecutive points of a dense cell are
+// also close together (tighter query tiles).
 __global__ void k_fine_keys(const double *__restrict__ src, int64_t n, int64_t stride, FineGrid fg,
                             uint32_t *__restrict__ keys, uint32_t *__restrict__ vals) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int c[3];
+  uint32_t sub = 0;
   for (int e = 0; e < 3; ++e) {
     const int d = e - fg.eoff;
     if (d < 0) {
       c[e] = 0;
       continue;
     }
-    int u = fine_coord(src[(int64_t)d * stride + i], fg.lo[e], fg.h[e], fg.m[e]);
+    const double x = src[(int64_t)d * stride + i];
+    int u = fine_coord(x, fg.lo[e], fg.h[e], fg.m[e]);
     c[e] = min(max(u, 0), fg.m[e] - 1);
+    const double f = x - (fg.lo[e] + (double)c[e] * fg.h[e]);
+    sub |= (f >= 0.5 * fg.h[e] ? 1u : 0u) << (2 - e);
   }
-  keys[i] = ((uint32_t)c[0] * fg.m[1] + c[1]) * fg.m[2] + c[2];
+  keys[i] = ((((uint32_t)c[0] * fg.m[1] + c[1]) * fg.m[2] + c[2]) << 3) | sub;
   vals[i] = (uint32_t)i;
 }
 
@@ -200,9 +207,9 @@ __global__ void k_mark_runs_fine(const uint32_t *__restrict__ keys, int64_t n,
                                  uint32_t *__restrict__ first, uint32_t *__restrict__ last) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
-  const uint32_t key = keys[k];
-  if (k == 0 || keys[k - 1] != key) first[key] = (uint32_t)k;
-  if (k == n - 1 || keys[k + 1] != key) last[key] = (uint32_t)(k + 1);
+  const uint32_t key = keys[k] >> 3;
+  if (k == 0 || (keys[k - 1] >> 3) != key) first[key] = (uint32_t)k;
+  if (k == n - 1 || (keys[k + 1] >> 3) != key) last[key] = (uint32_t)(k + 1);
 }
 
 __global__ void k_sub(const uint32_t *__restrict__ a, uint32_t n, uint32_t *__restrict__ b) {
@@ -226,7 +233,7 @@ int build_points(abx_context *ctx, const double *src_soa, int64_t n, int64_t str
   k_fine_keys<<<ceil_div(n, TPB), TPB, 0, s>>>(src_soa, n, stride, fg, P.keys.ptr, P.perm.ptr);
   ABX_CHECK_CUDA(cudaGetLastError());
   int bits = 0;
-  while (bits < 32 && ((uint64_t)(fg.ncells - 1) >> bits) != 0) ++bits;
+  while (bits < 32 && (((uint64_t)fg.ncells * 8 - 1) >> bits) != 0) ++bits;
   ABX_TRY(radix_sort_pairs(P.keys.ptr, P.perm.ptr, n, bits, tmp.ptr, tmp.ptr + n, tmp.ptr + 2 * n,
                            s));
   k_fill_layout<<<ceil_div(n, TPB), TPB, 0, s>>>(src_soa, stride, fg, P.perm.ptr, n,
@@ -259,26 +266,28 @@ int build_cell_start(abx_context *ctx, PairLayout &L) {
   return ABX_OK;
 }
 
-// Units: greedy runs of <= 32 consecutive queries (kernel order) in one
-// (e0,e1) row spanning at most GROUP_E2 fine cells along e2.
+// Units: greedy runs of <= 32 consecutive queries (kernel order) whose anchor
+// cells share (e0, e1) and span fewer than GROUP_E2 cells along e2.
 int build_units(abx_context *ctx, PairLayout &L) {
   PointLayout &Q = *L.rows;
   const int64_t n = Q.n;
-  std::vector<uint32_t> keys(n);
-  if (n) {
-    ABX_CHECK_CUDA(cudaMemcpy(keys.data(), Q.keys.ptr, n * 4, cudaMemcpyDeviceToHost));
-  }
+  ABX_REQUIRE(n < (int64_t)0x7fffffff, ABX_ERR_INVALID, "too many query points");
+  std::vector<int4> cell(n);
+  if (n) ABX_CHECK_CUDA(cudaMemcpy(cell.data(), Q.cell.ptr, n * sizeof(int4), cudaMemcpyDeviceToHost));
   std::vector<int2> units;
   units.reserve(n / 16 + 16);
-  const uint32_t m2 = (uint32_t)L.fg.m[2];
   int64_t i = 0;
   while (i < n) {
-    const uint32_t row = keys[i] / m2;
-    const uint32_t c2 = keys[i] % m2;
+    const int4 c0 = cell[i];
+    int zmin = c0.z, zmax = c0.z;
     int64_t j = i + 1;
     while (j < n && j - i < 32) {
-      const uint32_t rj = keys[j] / m2, cj = keys[j] % m2;
-      if (rj != row || cj >= c2 + GROUP_E2) break;
+      const int4 cj = cell[j];
+      if (cj.x != c0.x || cj.y != c0.y) break;
+      const int nz0 = std::min(zmin, cj.z), nz1 = std::max(zmax, cj.z);
+      if (nz1 - nz0 >= GROUP_E2) break;
+      zmin = nz0;
+      zmax = nz1;
       ++j;
     }
     units.push_back(make_int2((int)i, (int)(j - i)));
@@ -294,10 +303,14 @@ int build_units(abx_context *ctx, PairLayout &L) {
 }
 
 // ------------------------------------------------------------- kernels ---
+constexpr int EXT_TAB = 64;   // extent table covers gaps of < 64 cells in e0, e1
+constexpr int SEG_CAP = 96;   // segments per batch (32 rows x up to 3 image splits)
+
 struct KParams {
   FineGrid fg;
   double r, r2;
   double prune2;  // squared pruning distance (r plus a safety margin)
+  const int *ext;  // [EXT_TAB*EXT_TAB]: max e2 gap (cells) for e0/e1 gaps, -1 pruned
   // kernel functor parameters
   int kind;
   double p0;
@@ -361,7 +374,7 @@ __device__ __forceinline__ double kern64(double d2, const KParams &P, double si,
 
 // The reference's FP64 acceptance test for one (query, candidate, image):
 // accum = ((0 + dx0^2) + dx1^2) + dx2^2 over the REAL dimensions in order, no
-// FMA; inside iff !(accum > r^2).  Returns accum (or +inf if outside).
+// FMA, with dx = x_j - (x_i + image*L); inside iff !(accum > r^2).
 __device__ __forceinline__ double exact_d2(const D4 &xq, const D4 &xj, const int *img,
                                            const FineGrid &fg) {
   const double q[3] = {xq.x, xq.y, xq.z};
@@ -377,76 +390,173 @@ __device__ __forceinline__ double exact_d2(const D4 &xq, const D4 &xj, const int
   return acc;
 }
 
-struct WarpSmem32 {
-  float4 p[32];
-  int idx[32];
-};
-struct WarpSmem64 {
-  double x[32], y[32], z[32], b[32], s[32];
-  int idx[32];
+__device__ __forceinline__ void unpack_seg(int z, int img[3], int &du0, int &du1) {
+  img[0] = (z & 3) - 1;
+  img[1] = ((z >> 2) & 3) - 1;
+  img[2] = ((z >> 4) & 3) - 1;
+  du0 = ((z >> 6) & 0xfff) - 2048;
+  du1 = ((z >> 18) & 0xfff) - 2048;
+}
+
+// Per-warp shared state: the segment list of one batch of rows, its length
+// prefix, and one staged tile of candidates.
+struct WarpSeg {
+  int4 seg[SEG_CAP];      // start, end, packed(img, du0, du1), c2shift
+  int off[SEG_CAP + 1];   // exclusive prefix of segment lengths
 };
 
-// Walk all candidate segments of the warp's unit; for each segment call
-// seg(start, end, img[3], du0, du1, c2shift) where the staged e2 offset of a
-// candidate with clamped cell c2 is (c2 + c2shift) cells from the reference.
-template <class Seg>
-__device__ __forceinline__ void for_each_segment(const KParams &P, const int lo[3],
-                                                 const int hi[3], Seg &&seg) {
+// Build the candidate segments of rows [row0, row0+32) of the unit's stencil
+// into ws.seg (warp-cooperative: one row per lane, up to three image splits
+// along e2).  Returns the number of segments; ws.off holds the length prefix.
+__device__ __forceinline__ int build_segments(const KParams &P, const int lo[3], const int hi[3],
+                                              int a0, int a1, int R1, int nrows, int row0,
+                                              WarpSeg &ws, int lane) {
   const FineGrid &fg = P.fg;
-  const int a0 = max(lo[0] - fg.K[0], fg.periodic[0] ? -fg.m[0] : 0);
-  const int b0 = min(hi[0] + fg.K[0], fg.periodic[0] ? 2 * fg.m[0] - 1 : fg.m[0] - 1);
-  for (int u0 = a0; u0 <= b0; ++u0) {
+  int4 mine[3];
+  bool has[3] = {false, false, false};
+  const int t = row0 + lane;
+  if (t < nrows) {
+    const int u0 = a0 + t / R1, u1 = a1 + t % R1;
     const int g0c = max(max(lo[0] - u0, u0 - hi[0]) - 1, 0);
-    const double g0 = g0c * fg.h[0];
-    const double g0s = g0 * g0;
-    if (g0s > P.prune2) continue;
-    int w0 = u0, i0 = 0;
-    if (u0 < 0) { w0 = u0 + fg.m[0]; i0 = 1; }
-    else if (u0 >= fg.m[0]) { w0 = u0 - fg.m[0]; i0 = -1; }
-    const int a1 = max(lo[1] - fg.K[1], fg.periodic[1] ? -fg.m[1] : 0);
-    const int b1 = min(hi[1] + fg.K[1], fg.periodic[1] ? 2 * fg.m[1] - 1 : fg.m[1] - 1);
-    for (int u1 = a1; u1 <= b1; ++u1) {
-      const int g1c = max(max(lo[1] - u1, u1 - hi[1]) - 1, 0);
-      const double g1 = g1c * fg.h[1];
-      const double rem = P.prune2 - g0s - g1 * g1;
-      if (rem < 0.0) continue;
-      int w1 = u1, i1 = 0;
-      if (u1 < 0) { w1 = u1 + fg.m[1]; i1 = 1; }
-      else if (u1 >= fg.m[1]) { w1 = u1 - fg.m[1]; i1 = -1; }
-      // e2 extent: cells whose gap <= sqrt(rem)
-      int ext = (int)floor(sqrt(rem) / fg.h[2]) + 1;
-      if (ext > fg.K[2]) ext = fg.K[2];
-      int a2 = lo[2] - ext, b2 = hi[2] + ext;
+    const int g1c = max(max(lo[1] - u1, u1 - hi[1]) - 1, 0);
+    int ext;
+    if (g0c < EXT_TAB && g1c < EXT_TAB) {
+      ext = P.ext[g0c * EXT_TAB + g1c];
+    } else {
+      const double g0 = g0c * fg.h[0], g1 = g1c * fg.h[1];
+      const double rem = P.prune2 - g0 * g0 - g1 * g1;
+      ext = rem < 0.0 ? -1 : min((int)floor(sqrt(rem) / fg.h[2]), fg.K[2]);
+    }
+    if (ext >= 0) {
+      int w0 = u0, i0 = 0, w1 = u1, i1 = 0;
+      if (u0 < 0) { w0 = u0 + fg.m[0]; i0 = 1; } else if (u0 >= fg.m[0]) { w0 = u0 - fg.m[0]; i0 = -1; }
+      if (u1 < 0) { w1 = u1 + fg.m[1]; i1 = 1; } else if (u1 >= fg.m[1]) { w1 = u1 - fg.m[1]; i1 = -1; }
+      const int a2 = max(lo[2] - 1 - ext, lo[2] - fg.K[2]);
+      const int b2 = min(hi[2] + 1 + ext, hi[2] + fg.K[2]);
       const uint32_t rowbase = ((uint32_t)w0 * fg.m[1] + w1) * (uint32_t)fg.m[2];
       const int m2 = fg.m[2];
-      // split the unwrapped e2 range into image segments
-      const int segs_lo[3] = {fg.periodic[2] ? -m2 : 0, 0, m2};
-      const int segs_hi[3] = {-1, m2 - 1, fg.periodic[2] ? 2 * m2 - 1 : m2 - 1};
-      const int segimg[3] = {1, 0, -1};
-#pragma unroll 1
+#pragma unroll
       for (int sgi = 0; sgi < 3; ++sgi) {
         if (sgi != 1 && !fg.periodic[2]) continue;
-        const int sa = max(a2, segs_lo[sgi]), sb = min(b2, segs_hi[sgi]);
+        const int slo = sgi == 0 ? -m2 : (sgi == 1 ? 0 : m2);
+        const int shi = sgi == 0 ? -1 : (sgi == 1 ? m2 - 1 : 2 * m2 - 1);
+        const int sa = max(a2, slo), sb = min(b2, shi);
         if (sa > sb) continue;
-        const int shift = segimg[sgi] * m2;  // w2 = u2 + shift
+        const int i2 = 1 - sgi;            // image +1, 0, -1
+        const int shift = i2 * m2;         // wrapped w2 = u2 + shift
         const uint32_t start = P.cell_start[rowbase + (uint32_t)(sa + shift)];
         const uint32_t end = P.cell_start[rowbase + (uint32_t)(sb + shift) + 1];
         if (start >= end) continue;
-        const int img[3] = {i0, i1, segimg[sgi]};
-        seg(start, end, img, u0 - lo[0], u1 - lo[1], -shift - lo[2]);
+        const int z = (i0 + 1) | ((i1 + 1) << 2) | ((i2 + 1) << 4) |
+                      ((u0 - lo[0] + 2048) << 6) | ((u1 - lo[1] + 2048) << 18);
+        mine[sgi] = make_int4((int)start, (int)end, z, -shift - lo[2]);
+        has[sgi] = true;
       }
     }
   }
+  // compact into the shared list
+  const unsigned lt = (1u << lane) - 1u;
+  int base = 0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const unsigned m = __ballot_sync(0xffffffffu, has[k]);
+    if (has[k]) ws.seg[base + __popc(m & lt)] = mine[k];
+    base += __popc(m);
+  }
+  __syncwarp();
+  // exclusive prefix of the lengths: lane l owns entries 3l..3l+2
+  int len[3], s = 0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int i = 3 * lane + k;
+    len[k] = i < base ? ws.seg[i].y - ws.seg[i].x : 0;
+    s += len[k];
+  }
+  int incl = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  int run = incl - s;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int i = 3 * lane + k;
+    if (i < base) ws.off[i] = run;
+    run += len[k];
+  }
+  if (lane == 31) ws.off[base] = run;  // total
+  __syncwarp();
+  return base;
 }
 
-// Mixed-precision pair kernel: FP32 prefilter + exact FP64 band, FP32 terms.
-template <int POL, int KIND>
-__global__ void __launch_bounds__(WARPS_PER_CTA * 32)
-    k_pairs_mixed(KParams P) {
-  __shared__ WarpSmem32 sm_all[WARPS_PER_CTA];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  WarpSmem32 &sm = sm_all[wid];
+// Segment holding flattened candidate t (off[s] <= t < off[s+1]).
+__device__ __forceinline__ int find_seg(const WarpSeg &ws, int nseg, int t) {
+  int lo = 0, hi = nseg - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (ws.off[mid] <= t) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+struct WarpTile32 {
+  float4 p[32];
+  int2 meta[32];  // column kernel index, segment index
+};
+
+__device__ __forceinline__ float warp_min(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Unit prologue shared by both kernels: the warp's anchor-cell box [lo, hi]
+// and the row range of its stencil.
+__device__ __forceinline__ void unit_box(const KParams &P, const int4 qc, bool active, int lo[3],
+                                         int hi[3], int &a0, int &a1, int &R1, int &nrows) {
   const FineGrid &fg = P.fg;
+  lo[0] = hi[0] = qc.x;
+  lo[1] = hi[1] = qc.y;
+  lo[2] = hi[2] = qc.z;
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    const int a = active ? lo[e] : 0x7fffffff, b = active ? hi[e] : -0x7fffffff;
+    lo[e] = __reduce_min_sync(0xffffffffu, a);
+    hi[e] = __reduce_max_sync(0xffffffffu, b);
+  }
+  a0 = max(lo[0] - fg.K[0], fg.periodic[0] ? -fg.m[0] : 0);
+  const int b0 = min(hi[0] + fg.K[0], fg.periodic[0] ? 2 * fg.m[0] - 1 : fg.m[0] - 1);
+  a1 = max(lo[1] - fg.K[1], fg.periodic[1] ? -fg.m[1] : 0);
+  const int b1 = min(hi[1] + fg.K[1], fg.periodic[1] ? 2 * fg.m[1] - 1 : fg.m[1] - 1);
+  R1 = b1 - a1 + 1;
+  const int R0 = b0 - a0 + 1;
+  nrows = (R0 > 0 && R1 > 0) ? R0 * R1 : 0;
+}
+
+// Mixed-precision pair kernel.  Per unit (one warp, <= 32 queries):
+//   rows of the stencil -> segment list -> flattened candidate stream, 32 at a
+//   time -> each lane stages one candidate (FP32 offset from the unit's
+//   reference corner) and keeps it only if it lies within r of the warp's
+//   query bounding box -> every lane tests its query against the kept
+//   candidates.  Pairs with d2 <= r2lo are accepted in the branch-free loop;
+//   pairs in the rounding band (r2lo, r2hi] are re-decided afterwards with the
+//   exact FP64 test, which is rare enough to run divergently.
+template <int POL, int KIND>
+__global__ void __launch_bounds__(WARPS_PER_CTA * 32, 8)
+    k_pairs_mixed(KParams P) {
+  __shared__ WarpSeg seg_all[WARPS_PER_CTA];
+  __shared__ WarpTile32 tile_all[WARPS_PER_CTA];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  WarpSeg &ws = seg_all[wid];
+  WarpTile32 &sm = tile_all[wid];
+  const FineGrid &fg = P.fg;
+  const unsigned lt = (1u << lane) - 1u;
   for (;;) {
     int unit = 0;
     if (lane == 0) unit = atomicAdd(P.counter, 1);
@@ -457,83 +567,113 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32)
     const int qi = U.x + (active ? lane : 0);
     const int4 qc = P.qcell[qi];
     const float4 ql = P.qloc[qi];
-    int lo[3] = {qc.x, qc.y, qc.z}, hi[3] = {qc.x, qc.y, qc.z};
-#pragma unroll
-    for (int e = 0; e < 3; ++e) {
-      int a = active ? lo[e] : 0x7fffffff, b = active ? hi[e] : -0x7fffffff;
-      a = __reduce_min_sync(0xffffffffu, a);
-      b = __reduce_max_sync(0xffffffffu, b);
-      lo[e] = a;
-      hi[e] = b;
-    }
-    // query offset from the reference cell lo
+    int lo[3], hi[3], a0, a1, R1, nrows;
+    unit_box(P, qc, active, lo, hi, a0, a1, R1, nrows);
     const float pq0 = fmaf((float)(qc.x - lo[0]), fg.hf[0], ql.x);
     const float pq1 = fmaf((float)(qc.y - lo[1]), fg.hf[1], ql.y);
     const float pq2 = fmaf((float)(qc.z - lo[2]), fg.hf[2], ql.z);
-    // rounding band for this tile: every staged coordinate is at most `span`
-    // cells from the reference corner, so each FP32 offset carries less than
-    // (3*span+2)*h*2^-24 absolute error and a difference of two of them less
-    // than edx = (span+2)*h*2^-20; |d2_f32 - d2| <= band follows.
+    // warp bounding box of the query offsets (inactive lanes repeat lane 0)
+    const float bl0 = warp_min(pq0), bh0 = warp_max(pq0);
+    const float bl1 = warp_min(pq1), bh1 = warp_max(pq1);
+    const float bl2 = warp_min(pq2), bh2 = warp_max(pq2);
+    // rounding band: every staged coordinate lies within `span` cells of the
+    // reference corner, so an FP32 offset carries < (3*span+2)*h*2^-24 error
+    // and a difference of two < edx = (span+2)*h*2^-20; |d2_f32 - d2| <= band.
     int span = 0;
 #pragma unroll
     for (int e = 0; e < 3; ++e) span = max(span, hi[e] - lo[e] + 2 * fg.K[e] + 2);
-    double hmax = fmax(fmax(fg.h[0] * (fg.eoff <= 0), fg.h[1] * (fg.eoff <= 1)), fg.h[2]);
-    const double edx = (double)(span + 2) * hmax * 9.5367431640625e-07;  // 2^-20
-    const double band = 2.0 * 1.7320508075688772 * (P.r + edx) * edx + edx * edx * 3.0 +
-                        4.0 * 5.960464477539063e-08 * (P.r2 + 1e-300) + 1e-300;
+    const double hmax = fmax(fmax(fg.h[0] * (fg.eoff <= 0), fg.h[1] * (fg.eoff <= 1)), fg.h[2]);
+    const double edx = (double)(span + 2) * hmax * 9.5367431640625e-07;
+    const double band = 2.0 * 1.7320508075688772 * (P.r + edx) * edx + 3.0 * edx * edx +
+                        4.0 * 5.960464477539063e-08 * P.r2 + 1e-300;
     const float r2lo = __double2float_rd(fmax(P.r2 - band, 0.0));
     const float r2hi = __double2float_ru(P.r2 + band);
+    const float r2box = __double2float_ru((P.r2 + band) * (1.0 + 1e-6) + 1e-300);
     D4 xq;
-    xq.x = xq.y = xq.z = xq.w = 0.0;
+    bool have_xq = false;
     double acc64 = 0.0;
     int count = 0;
     int64_t out_off = 0;
     if (POL == POL_LIST && active) out_off = P.rowptr[qi];
 
-    for_each_segment(P, lo, hi, [&](uint32_t start, uint32_t end, const int *img, int du0,
-                                    int du1, int c2shift) {
-      const float o0 = (float)du0 * fg.hf[0];
-      const float o1 = (float)du1 * fg.hf[1];
-      for (uint32_t t = start; t < end; t += 32) {
-        const uint32_t k = t + lane;
-        if (k < end) {
+    for (int row0 = 0; row0 < nrows; row0 += 32) {
+      const int nseg = build_segments(P, lo, hi, a0, a1, R1, nrows, row0, ws, lane);
+      if (nseg == 0) continue;
+      const int total = ws.off[nseg];
+      for (int t0 = 0; t0 < total; t0 += 32) {
+        const int t = t0 + lane;
+        bool keep = false;
+        float4 st;
+        int k = 0, sidx = 0;
+        if (t < total) {
+          sidx = find_seg(ws, nseg, t);
+          const int4 sg = ws.seg[sidx];
+          k = sg.x + (t - ws.off[sidx]);
+          int img[3], du0, du1;
+          unpack_seg(sg.z, img, du0, du1);
           const float4 cl = P.cloc[k];
-          const int c2 = __float_as_int(cl.w);
-          float4 st;
-          st.x = cl.x + o0;
-          st.y = cl.y + o1;
-          st.z = fmaf((float)(c2 + c2shift), fg.hf[2], cl.z);
-          st.w = (POL == POL_MATVEC) ? P.b32[k] : 0.f;
-          sm.p[lane] = st;
-          sm.idx[lane] = (int)k;
+          st.x = fmaf((float)du0, fg.hf[0], cl.x);
+          st.y = fmaf((float)du1, fg.hf[1], cl.y);
+          st.z = fmaf((float)(__float_as_int(cl.w) + sg.w), fg.hf[2], cl.z);
+          const float e0 = fmaxf(fmaxf(bl0 - st.x, st.x - bh0), 0.f);
+          const float e1 = fmaxf(fmaxf(bl1 - st.y, st.y - bh1), 0.f);
+          const float e2 = fmaxf(fmaxf(bl2 - st.z, st.z - bh2), 0.f);
+          keep = fmaf(e2, e2, fmaf(e1, e1, e0 * e0)) <= r2box;
+          if (keep) st.w = (POL == POL_MATVEC) ? P.b32[k] : 0.f;
+        }
+        const unsigned km = __ballot_sync(0xffffffffu, keep);
+        if (keep) {
+          const int slot = __popc(km & lt);
+          sm.p[slot] = st;
+          sm.meta[slot] = make_int2(k, sidx);
         }
         __syncwarp();
-        const int nt = min(32u, end - t);
+        const int nt = __popc(km);
         float acc32 = 0.f;
+        bool need = false;
+#pragma unroll 4
         for (int j = 0; j < nt; ++j) {
           const float4 c = sm.p[j];
           const float d0 = c.x - pq0, d1 = c.y - pq1, d2v = c.z - pq2;
           const float dd = fmaf(d2v, d2v, fmaf(d1, d1, d0 * d0));
-          bool in = dd <= r2lo;
-          if (!in && dd <= r2hi) {
-            // rounding band: decide with the reference's FP64 test
-            if (xq.w == 0.0) {
+          const bool in = dd <= r2lo;
+          need |= (dd > r2lo) & (dd <= r2hi);
+          if (POL == POL_MATVEC) {
+            const float w = kern32<KIND>(dd, P);
+            acc32 = fmaf(in ? w : 0.f, c.w, acc32);
+          }
+          if (POL == POL_COUNT) count += in ? 1 : 0;
+          if (POL == POL_LIST && in && active) P.cols_out[out_off++] = (int32_t)P.cperm[sm.meta[j].x];
+        }
+        if (__any_sync(0xffffffffu, need)) {
+          // rare: decide the band pairs with the reference's FP64 test
+          if (need) {
+            if (!have_xq) {
               xq = P.qpos[qi];
-              xq.w = 1.0;
+              have_xq = true;
             }
-            const D4 xj = P.cpos[sm.idx[j]];
-            in = !(exact_d2(xq, xj, img, fg) > P.r2);
+            for (int j = 0; j < nt; ++j) {
+              const float4 c = sm.p[j];
+              const float d0 = c.x - pq0, d1 = c.y - pq1, d2v = c.z - pq2;
+              const float dd = fmaf(d2v, d2v, fmaf(d1, d1, d0 * d0));
+              if (dd > r2lo && dd <= r2hi) {
+                const int2 mt = sm.meta[j];
+                int img[3], du0, du1;
+                unpack_seg(ws.seg[mt.y].z, img, du0, du1);
+                if (!(exact_d2(xq, P.cpos[mt.x], img, fg) > P.r2)) {
+                  if (POL == POL_MATVEC) acc32 = fmaf(kern32<KIND>(dd, P), c.w, acc32);
+                  if (POL == POL_COUNT) ++count;
+                  if (POL == POL_LIST && active) P.cols_out[out_off++] = (int32_t)P.cperm[mt.x];
+                }
+              }
+            }
           }
-          if (in && active) {
-            if (POL == POL_MATVEC) acc32 = fmaf(kern32<KIND>(dd, P), c.w, acc32);
-            if (POL == POL_COUNT) ++count;
-            if (POL == POL_LIST) P.cols_out[out_off++] = (int32_t)P.cperm[sm.idx[j]];
-          }
+          __syncwarp();
         }
         if (POL == POL_MATVEC) acc64 += (double)acc32;
         __syncwarp();
       }
-    });
+    }
     if (active) {
       if (POL == POL_MATVEC) P.c[qi] = acc64;
       if (POL == POL_COUNT) P.counts[qi] = count;
@@ -541,13 +681,21 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32)
   }
 }
 
-// FP64 pair kernel: the reference's arithmetic for every pair.
+struct WarpTile64 {
+  double x[32], y[32], z[32], b[32], s[32];
+  int idx[32];
+  int sg[32];
+};
+
+// FP64 pair kernel: the reference's arithmetic for every candidate pair.
 template <int POL, int KIND>
-__global__ void __launch_bounds__(WARPS_PER_CTA * 32)
+__global__ void __launch_bounds__(WARPS_PER_CTA * 32, 8)
     k_pairs_fp64(KParams P) {
-  __shared__ WarpSmem64 sm_all[WARPS_PER_CTA];
+  __shared__ WarpSeg seg_all[WARPS_PER_CTA];
+  __shared__ WarpTile64 tile_all[WARPS_PER_CTA];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  WarpSmem64 &sm = sm_all[wid];
+  WarpSeg &ws = seg_all[wid];
+  WarpTile64 &sm = tile_all[wid];
   const FineGrid &fg = P.fg;
   for (;;) {
     int unit = 0;
@@ -558,40 +706,47 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32)
     const bool active = lane < U.y;
     const int qi = U.x + (active ? lane : 0);
     const int4 qc = P.qcell[qi];
-    int lo[3] = {qc.x, qc.y, qc.z}, hi[3] = {qc.x, qc.y, qc.z};
-#pragma unroll
-    for (int e = 0; e < 3; ++e) {
-      int a = active ? lo[e] : 0x7fffffff, b = active ? hi[e] : -0x7fffffff;
-      lo[e] = __reduce_min_sync(0xffffffffu, a);
-      hi[e] = __reduce_max_sync(0xffffffffu, b);
-    }
+    int lo[3], hi[3], a0, a1, R1, nrows;
+    unit_box(P, qc, active, lo, hi, a0, a1, R1, nrows);
     const D4 xq = P.qpos[qi];
+    const double q[3] = {xq.x, xq.y, xq.z};
     const double si = (KIND == ABX_K_SCALAR_SUM) ? P.s_row[qi] : 0.0;
     double acc = 0.0;
     int count = 0;
     int64_t out_off = 0;
     if (POL == POL_LIST && active) out_off = P.rowptr[qi];
-    for_each_segment(P, lo, hi, [&](uint32_t start, uint32_t end, const int *img, int, int, int) {
-      // image point x + I*L (src/Search.h:188-190), real dimensions only
-      double cur[3];
-      const double q[3] = {xq.x, xq.y, xq.z};
-#pragma unroll
-      for (int e = 0; e < 3; ++e)
-        cur[e] = __dadd_rn(q[e], __dmul_rn((double)img[e], fg.L[e]));
-      for (uint32_t t = start; t < end; t += 32) {
-        const uint32_t k = t + lane;
-        if (k < end) {
+    for (int row0 = 0; row0 < nrows; row0 += 32) {
+      const int nseg = build_segments(P, lo, hi, a0, a1, R1, nrows, row0, ws, lane);
+      if (nseg == 0) continue;
+      const int total = ws.off[nseg];
+      for (int t0 = 0; t0 < total; t0 += 32) {
+        const int t = t0 + lane;
+        if (t < total) {
+          const int sidx = find_seg(ws, nseg, t);
+          const int k = ws.seg[sidx].x + (t - ws.off[sidx]);
           const D4 p = P.cpos[k];
           sm.x[lane] = p.x;
           sm.y[lane] = p.y;
           sm.z[lane] = p.z;
           sm.b[lane] = (POL == POL_MATVEC) ? P.b64[k] : 0.0;
           sm.s[lane] = (KIND == ABX_K_SCALAR_SUM) ? P.s_col[k] : 0.0;
-          sm.idx[lane] = (int)k;
+          sm.idx[lane] = k;
+          sm.sg[lane] = sidx;
         }
         __syncwarp();
-        const int nt = min(32u, end - t);
+        const int nt = min(32, total - t0);
+        int cur_seg = -1;
+        double cur[3] = {0.0, 0.0, 0.0};
         for (int j = 0; j < nt; ++j) {
+          const int sj = sm.sg[j];
+          if (sj != cur_seg) {
+            // image point x + I*L of this segment (src/Search.h:188-190)
+            int img[3], du0, du1;
+            unpack_seg(ws.seg[sj].z, img, du0, du1);
+#pragma unroll
+            for (int e = 0; e < 3; ++e) cur[e] = __dadd_rn(q[e], __dmul_rn((double)img[e], fg.L[e]));
+            cur_seg = sj;
+          }
           const double pj[3] = {sm.x[j], sm.y[j], sm.z[j]};
           double a = 0.0;
 #pragma unroll
@@ -609,7 +764,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32)
         }
         __syncwarp();
       }
-    });
+    }
     if (active) {
       if (POL == POL_MATVEC) P.c[qi] = acc;
       if (POL == POL_COUNT) P.counts[qi] = count;
@@ -641,16 +796,38 @@ __global__ void k_scatter(const T *__restrict__ src, const uint32_t *__restrict_
   dst[perm[k]] = src[k];
 }
 
-KParams base_params(const PairLayout &L) {
-  KParams P{};
-  P.fg = L.fg;
-  P.r = L.r;
-  P.r2 = L.r * L.r;
+// Largest e2 gap (in cells) that keeps a cell within the pruning distance,
+// for every pair of e0/e1 gaps below EXT_TAB cells (-1: pruned).
+int build_ext_table(PairLayout &L, double prune2) {
+  std::vector<int> tab(EXT_TAB * EXT_TAB);
+  const FineGrid &fg = L.fg;
+  for (int a = 0; a < EXT_TAB; ++a)
+    for (int b = 0; b < EXT_TAB; ++b) {
+      const double g0 = a * fg.h[0], g1 = b * fg.h[1];
+      const double rem = prune2 - g0 * g0 - g1 * g1;
+      tab[a * EXT_TAB + b] =
+          rem < 0.0 ? -1 : std::min((int)std::floor(std::sqrt(rem) / fg.h[2]), fg.K[2]);
+    }
+  ABX_TRY(L.ext.reserve(tab.size()));
+  ABX_CHECK_CUDA(cudaMemcpy(L.ext.ptr, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice));
+  return ABX_OK;
+}
+
+double prune_distance2(const PairLayout &L) {
   double hmax = 0;
   for (int e = 0; e < 3; ++e)
     if (e >= L.fg.eoff) hmax = std::max(hmax, L.fg.h[e]);
   const double margin = L.r * 1e-9 + hmax * 1e-9;
-  P.prune2 = (L.r + margin) * (L.r + margin);
+  return (L.r + margin) * (L.r + margin);
+}
+
+KParams base_params(const PairLayout &L) {
+  KParams P{};
+  P.ext = L.ext.ptr;
+  P.fg = L.fg;
+  P.r = L.r;
+  P.r2 = L.r * L.r;
+  P.prune2 = prune_distance2(L);
   P.cloc = L.cols.loc.ptr;
   P.cpos = L.cols.posk.ptr;
   P.cell_start = L.cell_start.ptr;
@@ -715,6 +892,7 @@ int layout_build(abx_context *ctx, abx_particles *cols, double r, const double *
     L.rows = &L.rows_own;
   }
   ABX_TRY(build_units(ctx, L));
+  ABX_TRY(build_ext_table(L, prune_distance2(L)));
   return ABX_OK;
 }
 
