@@ -27,6 +27,7 @@
 //    pair evaluates the reference's formula exactly (no FMA contraction).
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -1083,3 +1084,109 @@ int abx_radius_query_csr(abx_particles *p, int64_t nq, const double *q, double r
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free sparse matvec (abx_operator_matvec_noalloc).
+//
+// Some callers cannot call cudaMalloc while they apply an operator: code that
+// runs under a device-memory budget owned by another runtime (a framework
+// with its own caching allocator, a solver embedded in a simulation that
+// pre-sizes everything at start-up), or a time-stepping loop that must not
+// pay cudaMalloc/cudaFree's implicit device-wide synchronisation.  For them
+// this entry point keeps the per-call scratch of the sparse matvec -- b
+// gathered into the operator's internal order, the result before it is
+// scattered back to storage order, and the work counter of the pair kernel
+// -- in one file-scope device array of fixed size instead of in buffers
+// owned by the operator.  Every GPU that loads the library holds this array
+// until the process exits.
+namespace abx {
+namespace {
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = size_t(32) << 20;  // 32 MiB
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+std::mutex g_noalloc_mutex;
+unsigned char *g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of g_noalloc_scratch on `device` (current), looked up once
+// per device.  In host code the symbol itself is only a host-side stand-in,
+// so kernels must be given this address, never the symbol.
+int noalloc_scratch(int device, unsigned char **out) {
+  ABX_REQUIRE(device >= 0 && device < NOALLOC_MAX_DEVICES, ABX_ERR_INVALID,
+              "device %d beyond the allocation-free entry point's table", device);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[device]) {
+    void *p = nullptr;
+    ABX_CHECK_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_addr[device] = (unsigned char *)p;
+  }
+  *out = g_noalloc_addr[device];
+  return ABX_OK;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+}  // namespace
+}  // namespace abx
+
+extern "C" int abx_operator_matvec_noalloc(abx_operator *op, const double *b, double *c) {
+  ABX_REQUIRE(op, ABX_ERR_INVALID, "null operator");
+  ABX_REQUIRE(op->kind == 0, ABX_ERR_INVALID,
+              "abx_operator_matvec_noalloc: only sparse operators are supported");
+  const int64_t nr = op->rows->n, nc = op->cols->n;
+  ABX_REQUIRE((b || nc == 0) && (c || nr == 0), ABX_ERR_INVALID, "null vector");
+  abx_context *ctx = op->rows->ctx;
+  ABX_TRY(ctx_activate(ctx));
+  ABX_REQUIRE(op->cols->searchable, ABX_ERR_STATE,
+              "init_neighbour_search not called on the column particle set");
+  // A stale layout would have to be rebuilt, which allocates: refuse.
+  ABX_REQUIRE(op->pairs && op->pairs->cols_version == op->cols->version &&
+                  op->pairs->rows_version == op->rows->version,
+              ABX_ERR_STATE,
+              "abx_operator_matvec_noalloc: the particle sets changed since the operator was "
+              "built; rebuild it (or call abx_operator_matvec once) before calling this");
+  ABX_REQUIRE((nc == 0 || is_device_ptr(b)) && (nr == 0 || is_device_ptr(c)), ABX_ERR_INVALID,
+              "abx_operator_matvec_noalloc: b and c must be device memory (host vectors "
+              "would need staging buffers)");
+  if (nr == 0) return ABX_OK;
+  const bool mixed = op->precision == ABX_PREC_MIXED && op->k.kind != ABX_K_SCALAR_SUM;
+  const size_t need = align256((size_t)nc * (mixed ? sizeof(float) : sizeof(double))) +
+                      align256((size_t)nr * sizeof(double)) + 256;
+  ABX_REQUIRE(need <= NOALLOC_SCRATCH_BYTES, ABX_ERR_CAPACITY,
+              "abx_operator_matvec_noalloc: needs %zu bytes of scratch (%lld rows, %lld "
+              "columns) but the fixed array holds %zu bytes",
+              need, (long long)nr, (long long)nc, NOALLOC_SCRATCH_BYTES);
+  unsigned char *base = nullptr;
+  ABX_TRY(noalloc_scratch(ctx->device, &base));
+  const size_t bbytes = align256((size_t)nc * (mixed ? sizeof(float) : sizeof(double)));
+  void *bk = base;
+  double *ck = (double *)(base + bbytes);
+  int *counter = (int *)(base + bbytes + align256((size_t)nr * sizeof(double)));
+  cudaStream_t s = ctx->stream;
+  PairLayout &L = *op->pairs;
+  if (nc == 0) {
+    ABX_CHECK_CUDA(cudaMemsetAsync(c, 0, nr * sizeof(double), s));
+    return ABX_OK;
+  }
+  k_gather_b<<<ceil_div(nc, TPB), TPB, 0, s>>>(b, L.cols.perm.ptr, nc,
+                                               mixed ? (float *)bk : nullptr,
+                                               mixed ? nullptr : (double *)bk);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  KParams P = base_params(L);
+  P.kind = op->k.kind;
+  P.p0 = op->k.p[0];
+  P.p0f = (float)op->k.p[0];
+  P.c_exp2 = (float)(-op->k.p[0] * 1.4426950408889634);
+  P.b32 = mixed ? (const float *)bk : nullptr;
+  P.b64 = mixed ? nullptr : (const double *)bk;
+  P.s_col = L.sk.ptr;
+  P.s_row = L.sq.ptr;
+  P.c = ck;
+  P.counter = counter;  // zeroed by the launch helper before every launch
+  ABX_TRY(launch_pairs_kind<POL_MATVEC>(ctx, P, mixed));
+  k_scatter_c<<<ceil_div(nr, TPB), TPB, 0, s>>>(ck, L.rows->perm.ptr, nr, c);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  return ABX_OK;
+}

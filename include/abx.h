@@ -138,6 +138,28 @@ ABX_API int64_t abx_operator_cols(const abx_operator *op);
 /* c = K*b (Eigen assignment semantics, generic_product_impl::scaleAndAddTo
  * src/detail/Operators.h:207-229 with alpha == 1 on a zeroed destination). */
 ABX_API int abx_operator_matvec(abx_operator *op, const double *b, double *c);
+/* Allocation-free variant of abx_operator_matvec for sparse operators (no
+ * counterpart in the reference).  For callers that must not allocate device
+ * memory while applying an operator -- code running under a device-memory
+ * budget owned by another runtime, or a time-stepping loop that cannot pay
+ * cudaMalloc/cudaFree's implicit device-wide synchronisation.  It calls no
+ * cudaMalloc, cudaFree or allocating library routine: the per-call scratch
+ * lives in one fixed 32 MiB device array inside the library, which every GPU
+ * that loads the library holds until the process exits.
+ *   - b and c must be device memory; host vectors are rejected (ABX_ERR_INVALID).
+ *   - The scratch needed is 4 B (mixed precision) or 8 B (FP64) per column plus
+ *     8 B per row, each rounded up to 256 B, plus 256 B; larger operators are
+ *     rejected with ABX_ERR_CAPACITY (about 2.7M particles for a square mixed
+ *     operator).
+ *   - The operator must be current: if its particle sets were re-searched since
+ *     it was built, the call fails with ABX_ERR_STATE instead of rebuilding.
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   - All calls share the one array and it keeps the last call's contents, so
+ *     calls that overlap on the GPU (other streams, other host threads) race;
+ *     serialise them on one stream.
+ */
+ABX_API int abx_operator_matvec_noalloc(abx_operator *op, const double *b, double *c);
 /* Pair work of the last matvec: candidate pairs tested and pairs accepted. */
 ABX_API int abx_operator_last_stats(abx_operator *op, int64_t *candidates, int64_t *pairs);
 
