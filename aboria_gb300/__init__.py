@@ -25,7 +25,8 @@ __all__ = [
     "ABXError", "Context", "Particles", "Kernel", "Operator", "create_sparse_operator",
     "create_dense_operator", "radius_count", "radius_query_csr", "PREC_FP64", "PREC_MIXED",
     "K_CONST", "K_GAUSSIAN", "K_WENDLAND_C2", "K_COMPACT_GAUSSIAN", "K_LAPLACE",
-    "K_MULTIQUADRIC", "K_SCALAR_SUM", "default_context",
+    "K_MULTIQUADRIC", "K_SCALAR_SUM", "default_context", "Preconditioner",
+    "schwarz_preconditioner", "spai_preconditioner", "gmres",
 ]
 
 PREC_FP64, PREC_MIXED = 0, 1
@@ -136,6 +137,26 @@ class Particles:
                                                          float(n_particles_in_leaf)),
                "abx_particles_init_neighbour_search")
         return self
+
+    def init_octree(self, lo, hi, periodic, n_particles_in_leaf: float = 10.0):
+        """``Particles<..., HyperOctree>::init_neighbour_search``."""
+        lo = np.ascontiguousarray(lo, dtype=np.float64)
+        hi = np.ascontiguousarray(hi, dtype=np.float64)
+        per = np.ascontiguousarray([1 if p else 0 for p in periodic], dtype=np.int32)
+        _check(lib().abx_particles_init_octree(self._h, _ptr(lo), _ptr(hi), _ptr(per),
+                                               float(n_particles_in_leaf)),
+               "abx_particles_init_octree")
+        return self
+
+    def tree_leaves(self):
+        """Octree leaves: (level, tag, begin, end) arrays in creation order."""
+        n = C.c_int64()
+        _check(lib().abx_particles_get_tree_leaves(self._h, C.byref(n), None, None, None, None, 0),
+               "get_tree_leaves")
+        out = [np.empty(n.value, dtype=np.int32) for _ in range(4)]
+        _check(lib().abx_particles_get_tree_leaves(self._h, C.byref(n), *map(_ptr, out), n.value),
+               "get_tree_leaves")
+        return tuple(out)
 
     def update_positions(self):
         _check(lib().abx_particles_update_positions(self._h), "abx_particles_update_positions")
@@ -271,3 +292,79 @@ def create_dense_operator(rows: Particles, cols: Particles, kernel: Kernel,
     _check(lib().abx_create_dense_operator(rows._h, cols._h, C.byref(kernel), C.byref(h)),
            "abx_create_dense_operator")
     return Operator(h, rows, cols).set_precision(precision)
+
+
+class Preconditioner:
+    """``x = M b``: SchwartzPreconditioner or a sparse approximate inverse."""
+
+    def __init__(self, h, ctx, n, keep=()):
+        self._h = h
+        self.ctx = ctx
+        self.n = n
+        self._keep = keep
+
+    def __del__(self):
+        try:
+            if self._h:
+                lib().abx_precond_destroy(self._h)
+        except Exception:
+            pass
+
+    def solve(self, b, out=None):
+        if isinstance(b, np.ndarray):
+            b = np.ascontiguousarray(b, dtype=np.float64)
+            out = np.empty(self.n) if out is None else out
+        elif out is None:
+            import torch
+            out = torch.empty(self.n, dtype=torch.float64, device=b.device)
+        _check(lib().abx_precond_apply(self._h, _ptr(b), _ptr(out)), "abx_precond_apply")
+        if not isinstance(out, np.ndarray):
+            self.ctx.synchronize()
+        return out
+
+    def stats(self):
+        nd, ms, el = C.c_int64(), C.c_int64(), C.c_int64()
+        t = C.c_double()
+        _check(lib().abx_precond_stats(self._h, C.byref(nd), C.byref(ms), C.byref(el), C.byref(t)),
+               "abx_precond_stats")
+        return {"domains": nd.value, "max_size": ms.value, "elements": el.value,
+                "setup_s": t.value}
+
+
+def schwarz_preconditioner(op: Operator, precision: int = PREC_FP64) -> Preconditioner:
+    """``SchwartzPreconditioner<LU>``: analyzePattern + factorize on ``op``."""
+    h = C.c_void_p()
+    _check(lib().abx_precond_create_schwarz(op._h, precision, C.byref(h)),
+           "abx_precond_create_schwarz")
+    return Preconditioner(h, op.rows.ctx, op.shape[0], keep=(op,))
+
+
+def spai_preconditioner(ctx: Context, cols, vals) -> Preconditioner:
+    """Sparse approximate inverse with ``k`` entries per row (cols, vals: n x k)."""
+    cols = np.ascontiguousarray(cols, dtype=np.int32)
+    vals = np.ascontiguousarray(vals, dtype=np.float64)
+    n, k = cols.shape
+    h = C.c_void_p()
+    _check(lib().abx_precond_create_spai(ctx._h, n, k, _ptr(cols), _ptr(vals), C.byref(h)),
+           "abx_precond_create_spai")
+    return Preconditioner(h, ctx, n)
+
+
+def gmres(A: Operator, b, x0=None, M: Preconditioner | None = None, restart: int = 100,
+          max_iters: int = 1000, tol: float = 1e-8, A_check: Operator | None = None):
+    """Restarted flexible GMRES; returns (x, iterations, relative residual)."""
+    n = A.shape[0]
+    if isinstance(b, np.ndarray):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64, copy=True)
+    else:
+        import torch
+        x = torch.zeros(n, dtype=torch.float64, device=b.device) if x0 is None else x0.clone()
+    it = C.c_int()
+    res = C.c_double()
+    _check(lib().abx_gmres_solve(A._h, A_check._h if A_check else None, M._h if M else None,
+                                 _ptr(b), _ptr(x), int(restart), int(max_iters), float(tol),
+                                 C.byref(it), C.byref(res)), "abx_gmres_solve")
+    if not isinstance(x, np.ndarray):
+        A.rows.ctx.synchronize()
+    return x, it.value, res.value

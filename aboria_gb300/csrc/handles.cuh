@@ -27,6 +27,19 @@ struct GridDesc {
   uint32_t ncells;
 };
 
+// HyperOctree (src/OctTree.h:328-475), kept on the host in the reference's
+// layout: nodes level by level, every internal node owning 2^D consecutive
+// child slots (empty children included); leaves in the order they are
+// created.  Particle ranges index the tag-sorted storage order.
+struct OctTree {
+  int max_level = 0;
+  int dim = 3;
+  std::vector<int> tag, level, begin, end, kind, first_child, parent;  // per node
+  std::vector<int> leaves;                                              // node ids
+  // geometric box of a node (bisection as in point_to_tag)
+  void box(const GridDesc &g, int node, double *lo, double *hi) const;
+};
+
 }  // namespace abx
 
 struct abx_particles {
@@ -48,6 +61,8 @@ struct abx_particles {
   int64_t n_alive_prev = 0;                     // m_alive_indices.size()
   abx::DevBuf<uint32_t> keys;                   // sorted bucket key per particle
   abx::DevBuf<uint32_t> bucket_begin, bucket_end;
+  int search_kind = 0;  // 0: CellListOrdered, 1: HyperOctree
+  abx::OctTree tree;
   uint64_t version = 0;  // bumped by every rebuild; operators check it
   abx::HostStage stage_a, stage_b;
 };
@@ -67,6 +82,22 @@ struct abx_operator {
   abx::PairLayout *pairs = nullptr;
   abx::HostStage stage_b, stage_c;
   int64_t last_candidates = 0, last_pairs = 0;
+};
+
+namespace abx {
+struct Schwarz;  // solver.cu
+struct Spai;     // spai.cu
+}  // namespace abx
+
+// A preconditioner x = M b (restricted additive Schwarz or a sparse
+// approximate inverse), applied by abx_gmres_solve.
+struct abx_precond {
+  int kind = 0;  // 1 Schwarz, 2 sparse approximate inverse
+  abx::Schwarz *schwarz = nullptr;
+  abx::Spai *spai = nullptr;
+  abx_context *ctx = nullptr;
+  int64_t n = 0;
+  abx::HostStage stage_b, stage_x;
 };
 
 namespace abx {

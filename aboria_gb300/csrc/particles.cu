@@ -12,6 +12,7 @@
 //       sort_by_key (stable, as Thrust)      -> radix_sort_pairs
 //       lower_bound / upper_bound per bucket -> k_count_cells + scan
 //   Particles::reorder (src/Particles.h:694-726) -> k_gather_*
+#include <algorithm>
 #include <cmath>
 
 #include "common.cuh"
@@ -61,6 +62,39 @@ __device__ __forceinline__ uint32_t bucket_key(const double *x, const GridDesc &
     key += mult * (uint32_t)v;
   }
   return key;
+}
+
+// point_to_tag (src/detail/SpatialUtil.h:255-286): per level, one bit per
+// dimension (dimension 0 most significant) from p < mid, bisecting the box.
+__global__ void k_tag(const double *__restrict__ pos, int64_t n, GridDesc g, int max_level,
+                      const uint32_t *__restrict__ idx, int64_t na, uint32_t *__restrict__ keys,
+                      uint32_t *__restrict__ vals) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= na) return;
+  const uint32_t i = idx[k];
+  double p[3], bmin[3], bmax[3];
+  for (int d = 0; d < g.dim; ++d) {
+    p[d] = pos[(int64_t)d * n + i];
+    bmin[d] = g.lo[d];
+    bmax[d] = g.hi[d];
+  }
+  int result = 0;
+  for (int level = 1; level <= max_level; ++level) {
+    int hh[3];
+    double mid[3];
+    for (int d = 0; d < g.dim; ++d) {
+      mid[d] = __dmul_rn(0.5, __dadd_rn(bmin[d], bmax[d]));
+      hh[d] = (p[d] < mid[d]) ? 0 : 1;
+      result |= hh[d];
+      result <<= 1;
+    }
+    for (int d = 0; d < g.dim; ++d) {
+      if (hh[d]) bmin[d] = mid[d]; else bmax[d] = mid[d];
+    }
+  }
+  result >>= 1;
+  keys[k] = (uint32_t)result;
+  vals[k] = i;
 }
 
 __global__ void k_hash(const double *__restrict__ pos, int64_t n, GridDesc g,
@@ -175,6 +209,49 @@ bool set_domain_impl(abx_particles *p, size_t n) {
   return true;
 }
 
+// HyperOctree::build_tree (src/OctTree.h:328-475) on the sorted tags.
+void build_octree(abx_particles *p, const std::vector<int> &tags) {
+  OctTree &T = p->tree;
+  const int D = p->dim;
+  const int nchild = 1 << D;
+  T = OctTree();
+  T.dim = D;
+  T.max_level = 32 / D - 2;
+  auto add = [&](int tag, int level, int b, int e, int kind, int parent) {
+    T.tag.push_back(tag);
+    T.level.push_back(level);
+    T.begin.push_back(b);
+    T.end.push_back(e);
+    T.kind.push_back(kind);
+    T.first_child.push_back(-1);
+    T.parent.push_back(parent);
+    return (int)T.tag.size() - 1;
+  };
+  add(0, 0, 0, (int)tags.size(), 2, -1);  // root
+  std::vector<int> active(1, 0);
+  for (int level = 1; !active.empty(); ++level) {
+    const int shift = (T.max_level - level) * D;
+    const int length = (1 << shift) - 1;
+    std::vector<int> next;
+    for (int a : active) {
+      T.first_child[a] = (int)T.tag.size();
+      for (int c = 0; c < nchild; ++c) {
+        const int mask = T.tag[a] | (c << shift);
+        const int lb = (int)(std::lower_bound(tags.begin(), tags.end(), mask) - tags.begin());
+        const int ub =
+            (int)(std::upper_bound(tags.begin(), tags.end(), mask + length) - tags.begin());
+        const int count = ub - lb;
+        int kind = 0;
+        if (count > 0) kind = (level == T.max_level || count <= p->n_leaf) ? 1 : 2;
+        const int id = add(mask, level, lb, ub, kind, a);
+        if (kind == 1) T.leaves.push_back(id);
+        if (kind == 2) next.push_back(id);
+      }
+    }
+    active.swap(next);
+  }
+}
+
 int update_positions(abx_particles *p) {
   abx_context *ctx = p->ctx;
   cudaStream_t s = ctx->stream;
@@ -183,6 +260,7 @@ int update_positions(abx_particles *p) {
   p->searchable = false;
   ++p->version;
   if (n == 0) {
+    if (p->search_kind == 1) build_octree(p, std::vector<int>());
     set_domain_impl(p, 0);
     p->n_alive_prev = 0;
     ABX_TRY(p->bucket_begin.reserve(p->grid.ncells));
@@ -229,12 +307,30 @@ int update_positions(abx_particles *p) {
   k_compact<<<ceil_div(n, TPB), TPB, 0, s>>>(alive, scan, n, idx);
   ABX_CHECK_CUDA(cudaGetLastError());
 
+  uint32_t *keys = nullptr;
+  if (p->search_kind == 1) {
+    // HyperOctree: tags, stable sort, tree built on the host from the tags.
+    g = p->grid;
+    const int max_level = 32 / D - 2;
+    ABX_TRY(p->keys.reserve(na > 0 ? na : 1));
+    keys = p->keys.ptr;
+    if (na > 0) {
+      k_tag<<<ceil_div(na, TPB), TPB, 0, s>>>(p->pos.ptr, n, g, max_level, idx, na, keys, vals);
+      ABX_CHECK_CUDA(cudaGetLastError());
+      ABX_TRY(radix_sort_pairs(keys, vals, na, max_level * D, keys_alt, vals_alt, rtmp, s));
+    }
+    std::vector<int> tags(na);
+    if (na > 0)
+      ABX_CHECK_CUDA(cudaMemcpyAsync(tags.data(), keys, na * 4, cudaMemcpyDeviceToHost, s));
+    ABX_CHECK_CUDA(cudaStreamSynchronize(s));
+    build_octree(p, tags);
+  } else {
   set_domain_impl(p, (size_t)na);
   g = p->grid;
   ABX_TRY(p->keys.reserve(na > 0 ? na : 1));
   ABX_TRY(p->bucket_begin.reserve(g.ncells));
   ABX_TRY(p->bucket_end.reserve(g.ncells));
-  uint32_t *keys = p->keys.ptr;
+  keys = p->keys.ptr;
   if (na > 0) {
     k_hash<<<ceil_div(na, TPB), TPB, 0, s>>>(p->pos.ptr, n, g, idx, na, keys, vals);
     ABX_CHECK_CUDA(cudaGetLastError());
@@ -276,6 +372,7 @@ int update_positions(abx_particles *p) {
   k_bucket_end<<<ceil_div(g.ncells, TPB), TPB, 0, s>>>(bb, counts, g.ncells, be);
   ABX_CHECK_CUDA(cudaGetLastError());
 
+  }
   // reorder (gather) every column into cell order; dead particles are dropped
   ABX_TRY(p->pos_alt.reserve((size_t)D * (na > 0 ? na : 1)));
   ABX_TRY(p->ids_alt.reserve(na > 0 ? na : 1));
@@ -305,6 +402,21 @@ int update_positions(abx_particles *p) {
 }
 
 }  // namespace
+
+void OctTree::box(const GridDesc &g, int node, double *lo, double *hi) const {
+  for (int d = 0; d < dim; ++d) {
+    lo[d] = g.lo[d];
+    hi[d] = g.hi[d];
+  }
+  const int L = level[node], t = tag[node];
+  for (int l = 1; l <= L; ++l) {
+    for (int d = 0; d < dim; ++d) {
+      const int bit = (t >> ((max_level - l) * dim + (dim - 1 - d))) & 1;
+      const double mid = 0.5 * (lo[d] + hi[d]);
+      if (bit) lo[d] = mid; else hi[d] = mid;
+    }
+  }
+}
 
 int particles_grid_desc(const abx_particles *p, GridDesc *g) {
   ABX_REQUIRE(p && p->searchable, ABX_ERR_STATE,
@@ -450,6 +562,49 @@ int abx_particles_init_neighbour_search(abx_particles *p, const double *lo, cons
   // alive count (src/NeighbourSearchBase.h:252-268), then update_positions.
   set_domain_impl(p, (size_t)p->n_alive_prev);
   return update_positions(p);
+}
+
+int abx_particles_init_octree(abx_particles *p, const double *lo, const double *hi,
+                              const int *periodic, double n_leaf) {
+  ABX_REQUIRE(p && lo && hi && periodic, ABX_ERR_INVALID, "null argument");
+  ABX_REQUIRE(n_leaf >= 1, ABX_ERR_INVALID, "n_particles_in_leaf must be >= 1");
+  for (int d = 0; d < p->dim; ++d)
+    ABX_REQUIRE(hi[d] > lo[d], ABX_ERR_INVALID, "empty domain in dimension %d", d);
+  ABX_TRY(ctx_activate(p->ctx));
+  for (int d = 0; d < 3; ++d) {
+    const bool real = d < p->dim;
+    p->grid.lo[d] = real ? lo[d] : 0.0;
+    p->grid.hi[d] = real ? hi[d] : 1.0;
+    p->grid.periodic[d] = real && periodic[d] ? 1 : 0;
+    p->grid.size[d] = 1;
+    p->grid.side[d] = real ? hi[d] - lo[d] : 1.0;
+    p->grid.inv_side[d] = 1.0 / p->grid.side[d];
+  }
+  p->grid.dim = p->dim;
+  p->grid.ncells = 1;
+  p->n_leaf = n_leaf;
+  p->domain_set = true;
+  p->search_kind = 1;
+  return update_positions(p);
+}
+
+int abx_particles_get_tree_leaves(abx_particles *p, int64_t *nleaves, int32_t *level,
+                                  int32_t *tag, int32_t *begin, int32_t *end, int64_t cap) {
+  ABX_REQUIRE(p && nleaves, ABX_ERR_INVALID, "null argument");
+  ABX_REQUIRE(p->searchable && p->search_kind == 1, ABX_ERR_STATE,
+              "the particle set has no octree (call abx_particles_init_octree)");
+  const OctTree &T = p->tree;
+  *nleaves = (int64_t)T.leaves.size();
+  if (!level && !tag && !begin && !end) return ABX_OK;
+  ABX_REQUIRE(cap >= (int64_t)T.leaves.size(), ABX_ERR_CAPACITY, "leaf capacity too small");
+  for (size_t i = 0; i < T.leaves.size(); ++i) {
+    const int nd = T.leaves[i];
+    if (level) level[i] = T.level[nd];
+    if (tag) tag[i] = T.tag[nd];
+    if (begin) begin[i] = T.begin[nd];
+    if (end) end[i] = T.end[nd];
+  }
+  return ABX_OK;
 }
 
 int abx_particles_set_positions(abx_particles *p, const double *pos) {

@@ -102,6 +102,19 @@ ABX_API int abx_particles_init_neighbour_search(abx_particles *p, const double *
  * replaced with abx_particles_set_positions (same n, current storage order). */
 ABX_API int abx_particles_set_positions(abx_particles *p, const double *pos);
 ABX_API int abx_particles_update_positions(abx_particles *p);
+/* Particles<..., HyperOctree>::init_neighbour_search (src/OctTree.h:168-226):
+ * domain enforcement as above, then storage reordered by octree tag
+ * (src/detail/SpatialUtil.h:255-286, stable) and the tree built level by level
+ * with leaves of <= n_particles_in_leaf particles (src/OctTree.h:328-475).
+ * The radius search and the operators work on either search structure. */
+ABX_API int abx_particles_init_octree(abx_particles *p, const double *lo, const double *hi,
+                                      const int *periodic, double n_particles_in_leaf);
+/* Leaves of the octree in the reference's creation order (level by level):
+ * level, tag, and the [begin, end) range in storage order.  Pass NULL arrays
+ * to query *nleaves only. */
+ABX_API int abx_particles_get_tree_leaves(abx_particles *p, int64_t *nleaves, int32_t *level,
+                                          int32_t *tag, int32_t *begin, int32_t *end,
+                                          int64_t cap);
 /* Grid of the cell list: size[dim], side[dim], total bucket count. */
 ABX_API int abx_particles_get_grid(abx_particles *p, uint32_t *size, double *side, uint32_t *ncells);
 /* bucket_begin/bucket_end (src/CellListOrdered.h:231-239), ncells each, and
@@ -162,6 +175,38 @@ ABX_API int abx_operator_matvec(abx_operator *op, const double *b, double *c);
 ABX_API int abx_operator_matvec_noalloc(abx_operator *op, const double *b, double *c);
 /* Pair work of the last matvec: candidate pairs tested and pairs accepted. */
 ABX_API int abx_operator_last_stats(abx_operator *op, int64_t *candidates, int64_t *pairs);
+
+/* ---------------------------------------------------------- solvers --
+ * Preconditioners (x = M b) and restarted flexible GMRES. */
+typedef struct abx_precond abx_precond;
+/* SchwartzPreconditioner<LU> (src/Preconditioners.h:1121-1537): one domain per
+ * non-empty octree leaf of the operator's particle set (rows == cols, set up
+ * with abx_particles_init_octree); the block over the leaf's particles plus
+ * those of every touching leaf is assembled with coeff (strict |dx| < r,
+ * src/detail/Kernels.h:336-368) and LU-factorised in FP64.  precision
+ * ABX_PREC_MIXED keeps FP32 copies of the factors for the apply.  Apply is
+ * restricted additive Schwarz (src/Preconditioners.h:1477-1522). */
+ABX_API int abx_precond_create_schwarz(abx_operator *op, int precision, abx_precond **out);
+/* Sparse approximate inverse with k entries per row: x_i = sum_j vals[i*k+j] *
+ * b[cols[i*k+j]] (the row form of CardinalFunctionsPreconditioner,
+ * src/Preconditioners.h:1025-1103). */
+ABX_API int abx_precond_create_spai(abx_context *ctx, int64_t n, int k, const int32_t *cols,
+                                    const double *vals, abx_precond **out);
+ABX_API int abx_precond_destroy(abx_precond *pc);
+ABX_API int abx_precond_apply(abx_precond *pc, const double *b, double *x);
+ABX_API int abx_precond_stats(abx_precond *pc, int64_t *ndomains, int64_t *max_size,
+                              int64_t *elements, double *setup_seconds);
+/* Solve A x = b (x holds the initial guess) with restarted, right-
+ * preconditioned flexible GMRES(restart): CGS2 orthogonalisation and Givens
+ * rotations in FP64.  At every restart the true residual b - A_check x is
+ * recomputed with A_check (NULL: A); iteration stops when its norm relative to
+ * |b| is <= tol or after max_iters inner iterations.  Passing a mixed-precision
+ * A and an FP64 A_check gives iterative refinement with an FP64-checked
+ * residual.  The reference's solvers are Eigen's (third party), used as
+ * gmres.compute(W); gmres.solve(phi) in tests/rbf_interpolation.h:360-370. */
+ABX_API int abx_gmres_solve(abx_operator *A, abx_operator *A_check, abx_precond *M,
+                            const double *b, double *x, int restart, int max_iters, double tol,
+                            int *iterations, double *rel_residual);
 
 #ifdef __cplusplus
 }

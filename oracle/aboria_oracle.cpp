@@ -550,3 +550,207 @@ void orc_brute_counts(int D, int64_t n, const double *pos, const double *lo,
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ octree --
+// HyperOctree (src/OctTree.h:168-560): point_to_tag (src/detail/SpatialUtil.h:
+// 255-286), stable sort by tag, then build_tree level by level
+// (src/OctTree.h:328-475): children of every active node get the tag range
+// [mask, mask + 2^((max_level-level)*D) - 1], lower/upper bounds give their
+// particle ranges, and a child is EMPTY (no particles), a LEAF (count <= n_leaf
+// or last level) or a NODE.
+namespace {
+int point_to_tag(const double *p, const double *lo, const double *hi, int D, int max_level) {
+  double bmin[3], bmax[3];
+  for (int i = 0; i < D; ++i) {
+    bmin[i] = lo[i];
+    bmax[i] = hi[i];
+  }
+  int result = 0;
+  for (int level = 1; level <= max_level; ++level) {
+    double mid[3];
+    int hi_half[3];
+    for (int i = 0; i < D; ++i) {
+      mid[i] = 0.5 * (bmin[i] + bmax[i]);
+      hi_half[i] = (p[i] < mid[i]) ? 0 : 1;
+      result |= hi_half[i];
+      result <<= 1;
+    }
+    for (int i = 0; i < D; ++i) {
+      bmin[i] = hi_half[i] ? mid[i] : bmin[i];
+      bmax[i] = hi_half[i] ? bmax[i] : mid[i];
+    }
+  }
+  result >>= 1;
+  return result;
+}
+}  // namespace
+
+extern "C" {
+
+// pos: n*D (already domain-enforced; no deletion here).  Outputs: perm (n),
+// tags (n, sorted), and the leaves in the reference's order (level by level,
+// child order): leaf_level, leaf_tag, leaf_begin, leaf_end (capacity cap).
+// Returns the number of leaves (or -1 if cap is too small).
+int64_t orc_octree_build(int D, int64_t n, const double *pos, const double *lo, const double *hi,
+                         double n_leaf, int64_t *perm, int32_t *tags_out, int32_t *leaf_level,
+                         int32_t *leaf_tag, int32_t *leaf_begin, int32_t *leaf_end, int64_t cap) {
+  const int max_level = 32 / D - 2;
+  const int nchild = 1 << D;
+  std::vector<std::pair<int, int64_t>> kv(n);
+  for (int64_t i = 0; i < n; ++i) kv[i] = {point_to_tag(pos + i * D, lo, hi, D, max_level), i};
+  std::stable_sort(kv.begin(), kv.end(),
+                   [](const std::pair<int, int64_t> &a, const std::pair<int, int64_t> &b) {
+                     return a.first < b.first;
+                   });
+  std::vector<int> tags(n);
+  for (int64_t i = 0; i < n; ++i) {
+    tags[i] = kv[i].first;
+    perm[i] = kv[i].second;
+    tags_out[i] = kv[i].first;
+  }
+  std::vector<int> active(1, 0);
+  int64_t nleaves = 0;
+  for (int level = 1; !active.empty(); ++level) {
+    const int shift = (max_level - level) * D;
+    const int length = (1 << shift) - 1;
+    std::vector<int> next;
+    for (int a : active) {
+      for (int c = 0; c < nchild; ++c) {
+        const int mask = a | (c << shift);
+        const int lb = (int)(std::lower_bound(tags.begin(), tags.end(), mask) - tags.begin());
+        const int ub = (int)(std::upper_bound(tags.begin(), tags.end(), mask + length) - tags.begin());
+        const int count = ub - lb;
+        if (count == 0) continue;
+        if (level == max_level || count <= n_leaf) {
+          if (nleaves >= cap) return -1;
+          leaf_level[nleaves] = level;
+          leaf_tag[nleaves] = mask;
+          leaf_begin[nleaves] = lb;
+          leaf_end[nleaves] = ub;
+          ++nleaves;
+        } else {
+          next.push_back(mask);
+        }
+      }
+    }
+    active.swap(next);
+  }
+  return nleaves;
+}
+
+}  // extern "C"
+
+// ----------------------------------------------------------------- Schwarz --
+// SchwartzPreconditioner (src/Preconditioners.h:1121-1537) restated for the
+// oracle: domains from octree leaves (analyze_impl_block :1170-1316), blocks
+// assembled with coeff (strict <, periodic-corrected dx: src/detail/Kernels.h:
+// 336-368, src/Particles.h:480-496), LU with partial pivoting (the role of
+// Eigen's dense solver), and restricted additive application (_solve_impl
+// :1477-1522).
+namespace {
+void leaf_box(int D, const double *lo, const double *hi, int max_level, int level, int tag,
+              double *blo, double *bhi) {
+  for (int d = 0; d < D; ++d) {
+    blo[d] = lo[d];
+    bhi[d] = hi[d];
+  }
+  for (int l = 1; l <= level; ++l)
+    for (int d = 0; d < D; ++d) {
+      const int bit = (tag >> ((max_level - l) * D + (D - 1 - d))) & 1;
+      const double mid = 0.5 * (blo[d] + bhi[d]);
+      if (bit) blo[d] = mid; else bhi[d] = mid;
+    }
+}
+
+void lu_factor(std::vector<double> &A, int n, std::vector<int> &piv) {  // column-major
+  piv.resize(n);
+  for (int c = 0; c < n; ++c) {
+    int p = c;
+    double best = std::fabs(A[(size_t)c * n + c]);
+    for (int r = c + 1; r < n; ++r)
+      if (std::fabs(A[(size_t)c * n + r]) > best) {
+        best = std::fabs(A[(size_t)c * n + r]);
+        p = r;
+      }
+    piv[c] = p;
+    if (p != c)
+      for (int j = 0; j < n; ++j) std::swap(A[(size_t)j * n + c], A[(size_t)j * n + p]);
+    const double d = A[(size_t)c * n + c];
+    if (d != 0.0)
+      for (int r = c + 1; r < n; ++r) A[(size_t)c * n + r] /= d;
+    for (int j = c + 1; j < n; ++j) {
+      const double u = A[(size_t)j * n + c];
+      for (int r = c + 1; r < n; ++r) A[(size_t)j * n + r] -= A[(size_t)c * n + r] * u;
+    }
+  }
+}
+
+void lu_solve(const std::vector<double> &A, int n, const std::vector<int> &piv, double *y) {
+  for (int c = 0; c < n; ++c)
+    if (piv[c] != c) std::swap(y[c], y[piv[c]]);
+  for (int c = 0; c < n; ++c)
+    for (int r = c + 1; r < n; ++r) y[r] -= A[(size_t)c * n + r] * y[c];
+  for (int c = n - 1; c >= 0; --c) {
+    y[c] /= A[(size_t)c * n + c];
+    for (int r = 0; r < c; ++r) y[r] -= A[(size_t)c * n + r] * y[c];
+  }
+}
+}  // namespace
+
+extern "C" {
+
+// pos: tree-ordered positions (n*D); leaves as returned by orc_octree_build.
+void orc_schwarz_apply(int D, int64_t n, const double *pos, const double *lo, const double *hi,
+                       const int *periodic, int64_t nleaves, const int32_t *leaf_level,
+                       const int32_t *leaf_tag, const int32_t *leaf_begin,
+                       const int32_t *leaf_end, double radius, int kind, const double *params,
+                       const double *b, double *x) {
+  const int max_level = 32 / D - 2;
+  const double buf = 1e5 * std::numeric_limits<double>::epsilon();
+  KDesc k{kind, {params[0], params[1], params[2], params[3]}, nullptr, nullptr};
+  std::vector<double> blo(nleaves * 3), bhi(nleaves * 3);
+  for (int64_t l = 0; l < nleaves; ++l)
+    leaf_box(D, lo, hi, max_level, leaf_level[l], leaf_tag[l], &blo[l * 3], &bhi[l * 3]);
+  for (int64_t i = 0; i < n; ++i) x[i] = b[i];
+  const double r2 = radius * radius;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t l = 0; l < nleaves; ++l) {
+    if (leaf_end[l] <= leaf_begin[l]) continue;
+    std::vector<int64_t> idx;
+    for (int64_t i = leaf_begin[l]; i < leaf_end[l]; ++i) idx.push_back(i);
+    const size_t own = idx.size();
+    for (int64_t m = 0; m < nleaves; ++m) {
+      if (m == l) continue;
+      bool touch = true;
+      for (int d = 0; d < D; ++d)
+        if (bhi[m * 3 + d] < blo[l * 3 + d] - buf || blo[m * 3 + d] > bhi[l * 3 + d] + buf)
+          touch = false;
+      if (touch)
+        for (int64_t i = leaf_begin[m]; i < leaf_end[m]; ++i) idx.push_back(i);
+    }
+    const int nd = (int)idx.size();
+    std::vector<double> A((size_t)nd * nd);
+    for (int c = 0; c < nd; ++c)
+      for (int r = 0; r < nd; ++r) {
+        double dx[3], s = 0.0;
+        for (int d = 0; d < D; ++d) {
+          dx[d] = pos[idx[c] * D + d] - pos[idx[r] * D + d];
+          if (periodic[d]) {
+            const double w = hi[d] - lo[d];
+            while (dx[d] > w / 2) dx[d] -= w;
+            while (dx[d] <= -w / 2) dx[d] += w;
+          }
+          s = s + dx[d] * dx[d];
+        }
+        A[(size_t)c * nd + r] = s < r2 ? kernel_eval(k, dx, D, 0, 0) : 0.0;
+      }
+    std::vector<int> piv;
+    lu_factor(A, nd, piv);
+    std::vector<double> y(nd);
+    for (int i = 0; i < nd; ++i) y[i] = b[idx[i]];
+    lu_solve(A, nd, piv, y.data());
+    for (size_t i = 0; i < own; ++i) x[idx[i]] = y[i];
+  }
+}
+
+}  // extern "C"

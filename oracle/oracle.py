@@ -36,8 +36,9 @@ def lib():
         _lib.orc_collapse.restype = C.c_uint32
         _lib.orc_point_to_bucket.restype = C.c_int
         _lib.orc_celllist_build.restype = C.c_int64
+        _lib.orc_octree_build.restype = C.c_int64
         _lib.orc_num_threads.restype = C.c_int
-        for name in ("orc_radius_count", "orc_radius_lists", "orc_sparse_matvec",
+        for name in ("orc_radius_count", "orc_radius_lists", "orc_sparse_matvec", "orc_schwarz_apply",
                      "orc_dense_matvec", "orc_brute_counts", "orc_set_num_threads",
                      "orc_reassemble"):
             getattr(_lib, name).restype = None
@@ -221,3 +222,48 @@ def brute_counts(pos, lo, hi, periodic: bool, r):
     lib().orc_brute_counts(C.c_int(dim), C.c_int64(n), _p(pos), _p(lo), _p(hi),
                            C.c_int(1 if periodic else 0), C.c_double(r), _p(out))
     return out
+
+
+@dataclass
+class Octree:
+    perm: np.ndarray
+    tags: np.ndarray
+    leaf_level: np.ndarray
+    leaf_tag: np.ndarray
+    leaf_begin: np.ndarray
+    leaf_end: np.ndarray
+
+
+def octree_build(pos, lo, hi, n_leaf):
+    """HyperOctree on already domain-enforced positions (no deletion)."""
+    pos = np.ascontiguousarray(pos, np.float64)
+    n, dim = pos.shape
+    lo = np.ascontiguousarray(lo, np.float64)
+    hi = np.ascontiguousarray(hi, np.float64)
+    perm = np.zeros(n, np.int64)
+    tags = np.zeros(n, np.int32)
+    cap = max(16, n) * 2
+    lv, lt, lb, le = (np.zeros(cap, np.int32) for _ in range(4))
+    nl = lib().orc_octree_build(C.c_int(dim), C.c_int64(n), _p(pos), _p(lo), _p(hi),
+                                C.c_double(n_leaf), _p(perm), _p(tags), _p(lv), _p(lt), _p(lb),
+                                _p(le), C.c_int64(cap))
+    assert nl >= 0
+    return Octree(perm, tags, lv[:nl].copy(), lt[:nl].copy(), lb[:nl].copy(), le[:nl].copy())
+
+
+def schwarz_apply(pos, lo, hi, periodic, tree: Octree, radius, kind, params, b):
+    """Restricted additive Schwarz on octree leaves (tree-ordered positions)."""
+    pos = np.ascontiguousarray(pos, np.float64)
+    n, dim = pos.shape
+    lo = np.ascontiguousarray(lo, np.float64)
+    hi = np.ascontiguousarray(hi, np.float64)
+    per = np.ascontiguousarray([1 if p else 0 for p in periodic], np.int32)
+    prm = np.zeros(4)
+    prm[:len(params)] = params
+    b = np.ascontiguousarray(b, np.float64)
+    x = np.zeros(n)
+    lib().orc_schwarz_apply(C.c_int(dim), C.c_int64(n), _p(pos), _p(lo), _p(hi), _p(per),
+                            C.c_int64(len(tree.leaf_level)), _p(tree.leaf_level),
+                            _p(tree.leaf_tag), _p(tree.leaf_begin), _p(tree.leaf_end),
+                            C.c_double(radius), C.c_int(kind), _p(prm), _p(b), _p(x))
+    return x

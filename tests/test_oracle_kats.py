@@ -116,3 +116,17 @@ def test_periodic_wrap_and_deletion():
     assert got == sorted([(0.25, 0.5), (0.75, 0.5), (0.5, 0.5)])
     cl = oracle.celllist_build(pos, [0, 0], [1, 1], [False, False], 1.0)
     assert cl.n == 1  # outside a non-periodic domain -> deleted
+
+
+def test_octree_leaves_partition_and_sizes():
+    pos = workloads.uniform(20000, 3, seed=60)
+    t = oracle.octree_build(pos, [0] * 3, [1] * 3, 64)
+    assert np.all(np.diff(t.tags) >= 0)
+    order = np.argsort(t.leaf_begin)
+    b, e = t.leaf_begin[order], t.leaf_end[order]
+    assert b[0] == 0 and e[-1] == 20000 and np.array_equal(b[1:], e[:-1])
+    assert np.all(e - b <= 64)
+    # a leaf's particles all carry its tag prefix
+    for i in range(0, len(t.leaf_tag), 37):
+        shift = (8 - t.leaf_level[i]) * 3
+        assert np.all((t.tags[t.leaf_begin[i]:t.leaf_end[i]] >> shift) == (t.leaf_tag[i] >> shift))
