@@ -19,7 +19,7 @@ from pathlib import Path
 
 import numpy as np
 
-from ._lib import ABXError, lib, load_library  # noqa: F401
+from ._lib import ABXError, closing, lib, load_library  # noqa: F401
 
 __all__ = [
     "ABXError", "Context", "Particles", "Kernel", "Operator", "create_sparse_operator",
@@ -67,9 +67,9 @@ class Context:
         _check(lib().abx_context_synchronize(self._h), "abx_context_synchronize")
 
     def close(self):
-        if self._h:
+        if self._h and not closing():
             lib().abx_context_destroy(self._h)
-            self._h = C.c_void_p()
+        self._h = C.c_void_p()
 
     def __del__(self):
         try:
@@ -100,7 +100,7 @@ class Particles:
 
     def __del__(self):
         try:
-            if self._h:
+            if self._h and not closing():
                 lib().abx_particles_destroy(self._h)
         except Exception:
             pass
@@ -243,7 +243,7 @@ class Operator:
 
     def __del__(self):
         try:
-            if self._h:
+            if self._h and not closing():
                 lib().abx_operator_destroy(self._h)
         except Exception:
             pass
@@ -305,7 +305,7 @@ class Preconditioner:
 
     def __del__(self):
         try:
-            if self._h:
+            if self._h and not closing():
                 lib().abx_precond_destroy(self._h)
         except Exception:
             pass

@@ -64,6 +64,19 @@ def parse_header(path: Path = HEADER):
 
 
 _lib = None
+_closing = False
+
+
+def _mark_closing():
+    global _closing
+    _closing = True
+
+
+def closing() -> bool:
+    """True once the interpreter is shutting down: handle finalizers must not
+    call into the library then (its CUDA runtime may already be torn down)."""
+    import sys
+    return _closing or sys.is_finalizing()
 
 
 def load_library(path: Path | None = None):
@@ -79,6 +92,8 @@ def load_library(path: Path | None = None):
         fn.restype = res
         fn.argtypes = args
     _lib = lib_
+    import atexit
+    atexit.register(_mark_closing)
     return _lib
 
 

@@ -298,10 +298,11 @@ __global__ void k_copy(const double *__restrict__ a, int64_t n, double *__restri
   if (i < n) b[i] = a[i];
 }
 
-__global__ void k_axpby(int64_t n, double a, const double *__restrict__ x, double bcoef,
+// y = a x (y is not read: it may hold uninitialised memory)
+__global__ void k_scale(int64_t n, double a, const double *__restrict__ x,
                         double *__restrict__ y) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) y[i] = a * x[i] + bcoef * y[i];
+  if (i < n) y[i] = a * x[i];
 }
 
 __global__ void k_sub(int64_t n, const double *__restrict__ a, const double *__restrict__ b,
@@ -638,13 +639,16 @@ int gmres_solve(abx_operator *A, abx_operator *Acheck, abx_precond *M, const dou
       return ABX_ERR_NUMERIC;
     }
     if (rel <= tol || total >= max_iters) break;
-    k_axpby<<<nb, TPB, 0, s>>>(n, 1.0 / beta, W.r.ptr, 0.0, W.V.ptr);
+    k_scale<<<nb, TPB, 0, s>>>(n, 1.0 / beta, W.r.ptr, W.V.ptr);
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
     int j = 0;
-    // inner tolerance: the Arnoldi estimate cannot go below the inner
-    // operator's accuracy; stop the cycle when it reaches the target
-    const double target = tol * bnorm;
+    // inner tolerance: when the Krylov operator is less accurate than the
+    // checking operator (mixed precision), its Arnoldi estimate cannot go far
+    // below that accuracy, so each cycle only reduces the residual by 1e-5 and
+    // the restart (a refinement step against A_check) does the rest.
+    const bool refining = Acheck != A && Acheck->precision != A->precision;
+    const double target = std::max(tol * bnorm, refining ? 1e-5 * beta : 0.0);
     for (; j < m && total < max_iters; ++j, ++total) {
       double *vj = W.V.ptr + (size_t)j * n;
       double *zj = W.Z.ptr + (size_t)j * n;
@@ -664,7 +668,7 @@ int gmres_solve(abx_operator *A, abx_operator *Acheck, abx_precond *M, const dou
       double hn;
       ABX_TRY(norm(W.w.ptr, hn));
       hcol[j + 1] = hn;
-      if (hn > 0.0) k_axpby<<<nb, TPB, 0, s>>>(n, 1.0 / hn, W.w.ptr, 0.0, W.V.ptr + (size_t)(j + 1) * n);
+      if (hn > 0.0) k_scale<<<nb, TPB, 0, s>>>(n, 1.0 / hn, W.w.ptr, W.V.ptr + (size_t)(j + 1) * n);
       // apply previous rotations, then a new one
       for (int i = 0; i < j; ++i) {
         const double t = cs[i] * hcol[i] + sn[i] * hcol[i + 1];

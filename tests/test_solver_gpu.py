@@ -64,32 +64,71 @@ def test_schwarz_mixed_factors_close():
     assert np.linalg.norm(x32 - x64) / np.linalg.norm(x64) < 1e-3
 
 
-@pytest.mark.parametrize("use_precond", [False, True])
-def test_gmres_vs_dense_solve(use_precond):
+def numpy_gmres(A, b, m, maxit):
+    """Textbook restarted GMRES(m) (MGS Arnoldi, least squares per cycle)."""
+    x = np.zeros(len(b))
+    tot = 0
+    while True:
+        r = b - A @ x
+        beta = np.linalg.norm(r)
+        if tot >= maxit:
+            return x, beta / np.linalg.norm(b)
+        V = [r / beta]
+        H = np.zeros((m + 1, m))
+        for j in range(m):
+            w = A @ V[j]
+            for i in range(j + 1):
+                H[i, j] = V[i] @ w
+                w = w - H[i, j] * V[i]
+            H[j + 1, j] = np.linalg.norm(w)
+            V.append(w / H[j + 1, j])
+            tot += 1
+        e = np.zeros(m + 1)
+        e[0] = beta
+        x = x + np.array(V[:m]).T @ np.linalg.lstsq(H, e, rcond=None)[0]
+
+
+def test_gmres_matches_textbook_algorithm():
     n, r = 2000, 0.1
     p = octree_particles(workloads.uniform(n, 2, seed=74), 64)
-    kern = ab.Kernel.make(ab.K_WENDLAND_C2, 1 / r)
-    K = ab.create_sparse_operator(p, p, r, kern)
+    K = ab.create_sparse_operator(p, p, r, ab.Kernel.make(ab.K_WENDLAND_C2, 1 / r))
     A = dense_matrix(p.positions, r, ab.K_WENDLAND_C2, [1 / r])
     b = np.random.default_rng(75).standard_normal(n)
-    M = ab.schwarz_preconditioner(K) if use_precond else None
-    x, it, res = ab.gmres(K, b, M=M, restart=50, max_iters=2000, tol=1e-10)
-    assert res <= 1e-10
+    x, it, res = ab.gmres(K, b, restart=50, max_iters=300, tol=1e-14)
+    xr, resr = numpy_gmres(A, b, 50, 300)
+    assert it == 300
+    # CGS2 (GPU) and MGS (numpy) Arnoldi differ only by rounding over 300 steps
+    assert abs(res - resr) / resr < 1e-4
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 1e-4
+
+
+def test_gmres_schwarz_vs_dense_solve():
+    n, r = 2000, 0.1
+    p = octree_particles(workloads.uniform(n, 2, seed=74), 64)
+    K = ab.create_sparse_operator(p, p, r, ab.Kernel.make(ab.K_WENDLAND_C2, 1 / r))
+    A = dense_matrix(p.positions, r, ab.K_WENDLAND_C2, [1 / r])
+    b = np.random.default_rng(75).standard_normal(n)
+    x, it, res = ab.gmres(K, b, M=ab.schwarz_preconditioner(K), restart=50, max_iters=2000,
+                          tol=1e-10)
+    assert res <= 1e-10 and it < 200
     xd = np.linalg.solve(A, b)
     assert np.linalg.norm(x - xd) / np.linalg.norm(xd) < 1e-7
     assert np.linalg.norm(A @ x - b) / np.linalg.norm(b) < 1e-9
 
 
 def test_mixed_gmres_refined_to_fp64_residual():
-    n, r = 20000, 0.04
+    n, r = 20000, 0.08
     p = octree_particles(workloads.uniform(n, 2, seed=76), 128)
-    kern = ab.Kernel.make(ab.K_COMPACT_GAUSSIAN, 100.0)
+    kern = ab.Kernel.make(ab.K_WENDLAND_C2, 1 / r)
     K64 = ab.create_sparse_operator(p, p, r, kern)
     K32 = ab.create_sparse_operator(p, p, r, kern, ab.PREC_MIXED)
     M = ab.schwarz_preconditioner(K64)
     b = np.random.default_rng(77).standard_normal(n)
     x, it, res = ab.gmres(K32, b, M=M, restart=100, max_iters=3000, tol=1e-8, A_check=K64)
-    assert res <= 1e-8
+    assert res <= 1e-8, (it, res)
+    # each refinement cycle contracts the FP64 residual by about
+    # cond(A) * (FP32 operator error) ~ 0.1 for this matrix
+    assert it < 400
     r64 = b - K64 * x
     assert np.linalg.norm(r64) / np.linalg.norm(b) <= 1.0001e-8
 
