@@ -26,7 +26,8 @@ __all__ = [
     "create_dense_operator", "radius_count", "radius_query_csr", "PREC_FP64", "PREC_MIXED",
     "K_CONST", "K_GAUSSIAN", "K_WENDLAND_C2", "K_COMPACT_GAUSSIAN", "K_LAPLACE",
     "K_MULTIQUADRIC", "K_SCALAR_SUM", "default_context", "Preconditioner",
-    "schwarz_preconditioner", "spai_preconditioner", "gmres",
+    "schwarz_preconditioner", "spai_preconditioner", "gmres", "knn", "spai_exact_rows", "MLP",
+    "spai_features", "learned_preconditioner", "spai_rows", "gmres_with_fallback",
 ]
 
 PREC_FP64, PREC_MIXED = 0, 1
@@ -368,3 +369,149 @@ def gmres(A: Operator, b, x0=None, M: Preconditioner | None = None, restart: int
     if not isinstance(x, np.ndarray):
         A.rows.ctx.synchronize()
     return x, it.value, res.value
+
+
+def knn(p: Particles, k: int = 32):
+    """k nearest neighbours of every stored particle: (idx, d2), each n x k."""
+    n = len(p)
+    idx = np.empty((n, k), dtype=np.int32)
+    d2 = np.empty((n, k), dtype=np.float64)
+    _check(lib().abx_knn(p._h, int(k), _ptr(idx), _ptr(d2)), "abx_knn")
+    return idx, d2
+
+
+def spai_exact_rows(op: Operator, k: int = 32):
+    """Exact least-squares approximate-inverse rows on the k-NN support."""
+    n = op.shape[0]
+    cols = np.empty((n, k), dtype=np.int32)
+    vals = np.empty((n, k), dtype=np.float64)
+    _check(lib().abx_spai_exact_rows(op._h, int(k), _ptr(cols), _ptr(vals)), "abx_spai_exact_rows")
+    return cols, vals
+
+
+class MLP:
+    """The learned preconditioner's model (``abx_mlp``)."""
+
+    def __init__(self, h, ctx, out_dim):
+        self._h = h
+        self.ctx = ctx
+        self.out_dim = out_dim
+
+    @classmethod
+    def create(cls, in_dim, hidden=128, nhidden=3, out_dim=32, seed=0, ctx=None):
+        ctx = ctx or default_context()
+        h = C.c_void_p()
+        _check(lib().abx_mlp_create(ctx._h, int(in_dim), int(hidden), int(nhidden), int(out_dim),
+                                    C.c_uint64(seed), C.byref(h)), "abx_mlp_create")
+        return cls(h, ctx, int(out_dim))
+
+    @classmethod
+    def load(cls, path, ctx=None):
+        ctx = ctx or default_context()
+        h = C.c_void_p()
+        _check(lib().abx_mlp_load(ctx._h, str(path).encode(), C.byref(h)), "abx_mlp_load")
+        with open(path, "rb") as f:
+            head = np.frombuffer(f.read(8 + 4 + 4 * 17), dtype=np.uint8)
+        nl = int(np.frombuffer(head[8:12].tobytes(), np.int32)[0])
+        dims = np.frombuffer(head[12:12 + 4 * (nl + 1)].tobytes(), np.int32)
+        return cls(h, ctx, int(dims[-1]))
+
+    def __del__(self):
+        try:
+            if self._h and not closing():
+                lib().abx_mlp_destroy(self._h)
+        except Exception:
+            pass
+
+    @property
+    def num_params(self):
+        return int(lib().abx_mlp_num_params(self._h))
+
+    def save(self, path):
+        _check(lib().abx_mlp_save(self._h, str(path).encode()), "abx_mlp_save")
+
+    def set_normalization(self, in_scale, out_scale, out_shift):
+        sc = np.ascontiguousarray(out_scale, dtype=np.float32)
+        sh = np.ascontiguousarray(out_shift, dtype=np.float32)
+        _check(lib().abx_mlp_set_normalization(self._h, float(in_scale), _ptr(sc), _ptr(sh)),
+               "abx_mlp_set_normalization")
+
+    def set_output_transform(self, kind, c=1.0):
+        _check(lib().abx_mlp_set_output_transform(self._h, int(kind), float(c)),
+               "abx_mlp_set_output_transform")
+
+    @property
+    def params(self):
+        out = np.empty(self.num_params, dtype=np.float32)
+        _check(lib().abx_mlp_get_params(self._h, _ptr(out)), "abx_mlp_get_params")
+        return out
+
+    @params.setter
+    def params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        _check(lib().abx_mlp_set_params(self._h, _ptr(p)), "abx_mlp_set_params")
+
+    def gradients(self, x, y):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        g = np.empty(self.num_params, dtype=np.float32)
+        loss = C.c_float()
+        _check(lib().abx_mlp_gradients(self._h, _ptr(x), _ptr(y), x.shape[0], _ptr(g),
+                                       C.byref(loss)), "abx_mlp_gradients")
+        return loss.value, g
+
+    def train_step(self, x, y, lr):
+        loss = C.c_float()
+        if isinstance(x, np.ndarray):
+            x = np.ascontiguousarray(x, dtype=np.float32)
+            y = np.ascontiguousarray(y, dtype=np.float32)
+        _check(lib().abx_mlp_train_step(self._h, _ptr(x), _ptr(y), int(x.shape[0]), float(lr),
+                                        C.byref(loss)), "abx_mlp_train_step")
+        return loss.value
+
+    def forward(self, x, precision=PREC_MIXED):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.empty((x.shape[0], self.out_dim), dtype=np.float32)
+        _check(lib().abx_mlp_forward(self._h, _ptr(x), x.shape[0], _ptr(y), int(precision)),
+               "abx_mlp_forward")
+        return y
+
+
+def spai_features(p: Particles, knn_idx, eps):
+    knn_idx = np.ascontiguousarray(knn_idx, dtype=np.int32)
+    n, k = knn_idx.shape
+    out = np.empty((n, k * p.dim), dtype=np.float32)
+    _check(lib().abx_spai_features(p._h, _ptr(knn_idx), int(k), float(eps), _ptr(out)),
+           "abx_spai_features")
+    return out
+
+
+def learned_preconditioner(op: Operator, mlp: MLP, eps: float, k: int = 32,
+                           precision: int = PREC_MIXED) -> Preconditioner:
+    h = C.c_void_p()
+    _check(lib().abx_precond_create_learned(op._h, mlp._h, float(eps), int(k), int(precision),
+                                            C.byref(h)), "abx_precond_create_learned")
+    return Preconditioner(h, op.rows.ctx, op.shape[0], keep=(op, mlp))
+
+
+def spai_rows(pc: Preconditioner, k: int = 32):
+    cols = np.empty((pc.n, k), dtype=np.int32)
+    vals = np.empty((pc.n, k), dtype=np.float64)
+    _check(lib().abx_precond_get_spai(pc._h, _ptr(cols), _ptr(vals)), "abx_precond_get_spai")
+    return cols, vals
+
+
+def gmres_with_fallback(A: Operator, b, M_learned: Preconditioner | None, A_fallback: Operator,
+                        restart=100, learned_max_iters=300, max_iters=2000, tol=1e-8,
+                        A_check: Operator | None = None):
+    """Learned preconditioner first; restricted additive Schwarz if it fails."""
+    n = A.shape[0]
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros(n)
+    it, res, fb = C.c_int(), C.c_double(), C.c_int()
+    _check(lib().abx_gmres_solve_fallback(A._h, A_check._h if A_check else None,
+                                          M_learned._h if M_learned else None, A_fallback._h,
+                                          _ptr(b), _ptr(x), int(restart), int(learned_max_iters),
+                                          int(max_iters), float(tol), C.byref(it), C.byref(res),
+                                          C.byref(fb)), "abx_gmres_solve_fallback")
+    return x, it.value, res.value, bool(fb.value)

@@ -26,6 +26,8 @@ _TYPES = {
     "int": C.c_int,
     "double": C.c_double,
     "int64_t": C.c_int64,
+    "uint64_t": C.c_uint64,
+    "float": C.c_float,
     "uint32_t": C.c_uint32,
     "const char *": C.c_char_p,
 }

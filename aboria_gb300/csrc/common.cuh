@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -88,6 +89,7 @@ struct Scratch {
 }  // namespace abx
 
 struct abx_context {
+  std::atomic<int> refs{1};  // the caller's handle + every object created on it
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
@@ -114,6 +116,11 @@ template <class T> size_t carve_size(size_t &off, size_t n) {
 }
 
 int ctx_activate(abx_context *ctx);
+// Handles are reference counted so that they can be destroyed in any order:
+// a context lives while any object created on it does, a particle set while
+// any operator built on it does.
+void ctx_retain(abx_context *ctx);
+void ctx_release(abx_context *ctx);
 // Returns 1 if p is device-accessible memory (device or managed), 0 if it is
 // host memory (pageable or pinned).
 int is_device_ptr(const void *p);

@@ -18,6 +18,19 @@ void set_error(const char *fmt, ...) {
 
 void clear_error() { g_err[0] = 0; }
 
+void ctx_retain(abx_context *ctx) { ctx->refs.fetch_add(1); }
+
+void ctx_release(abx_context *ctx) {
+  if (!ctx || ctx->refs.fetch_sub(1) != 1) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  ctx->scratch.release();
+  ctx->staging.release();
+  ctx->dev_flag.release();
+  if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
 int ctx_activate(abx_context *ctx) {
   ABX_REQUIRE(ctx, ABX_ERR_INVALID, "null context");
   ABX_CHECK_CUDA(cudaSetDevice(ctx->device));
@@ -111,14 +124,7 @@ int abx_context_create(int device, void *stream, abx_context **out) {
 }
 
 int abx_context_destroy(abx_context *ctx) {
-  if (!ctx) return ABX_OK;
-  cudaSetDevice(ctx->device);
-  cudaStreamSynchronize(ctx->stream);
-  ctx->scratch.release();
-  ctx->staging.release();
-  ctx->dev_flag.release();
-  if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
-  delete ctx;
+  ctx_release(ctx);  // freed once every object created on it is gone
   return ABX_OK;
 }
 

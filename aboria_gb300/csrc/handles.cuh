@@ -43,6 +43,7 @@ struct OctTree {
 }  // namespace abx
 
 struct abx_particles {
+  std::atomic<int> refs{1};
   abx_context *ctx = nullptr;
   int dim = 3;
   int64_t n = 0;
@@ -101,6 +102,8 @@ struct abx_precond {
 };
 
 namespace abx {
+void particles_retain(abx_particles *p);
+void particles_release(abx_particles *p);
 int particles_grid_desc(const abx_particles *p, GridDesc *g);
 // pairs.cu
 int pair_layout_build(abx_operator *op);

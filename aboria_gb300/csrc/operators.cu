@@ -219,6 +219,8 @@ int abx_create_sparse_operator(abx_particles *rows, abx_particles *cols, double 
     delete op;
     return st;
   }
+  particles_retain(rows);
+  particles_retain(cols);
   *out = op;
   return ABX_OK;
 }
@@ -234,16 +236,21 @@ int abx_create_dense_operator(abx_particles *rows, abx_particles *cols, const ab
   op->rows = rows;
   op->cols = cols;
   op->k = *k;
+  particles_retain(rows);
+  particles_retain(cols);
   *out = op;
   return ABX_OK;
 }
 
 int abx_operator_destroy(abx_operator *op) {
   if (!op) return ABX_OK;
-  cudaSetDevice(op->rows->ctx->device);
-  cudaStreamSynchronize(op->rows->ctx->stream);
+  abx_particles *rows = op->rows, *cols = op->cols;
+  cudaSetDevice(rows->ctx->device);
+  cudaStreamSynchronize(rows->ctx->stream);
   if (op->pairs) pair_layout_free(op->pairs);
   delete op;
+  particles_release(rows);
+  particles_release(cols);
   return ABX_OK;
 }
 

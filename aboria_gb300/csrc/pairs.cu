@@ -1064,6 +1064,141 @@ int radius_query(abx_particles *p, int64_t nq, const double *q_host_or_dev, doub
   return ABX_OK;
 }
 
+// Storage-order CSR of the neighbour lists of a particle set with itself at
+// radius r (device arrays; used by the exact least-squares SPAI rows).
+int self_csr_device(abx_particles *p, double r, DevBuf<int64_t> &rowptr, DevBuf<int32_t> &cols,
+                    int64_t &nnz) {
+  abx_context *ctx = p->ctx;
+  cudaStream_t s = ctx->stream;
+  const int64_t n = p->n;
+  PairLayout L;
+  ABX_TRY(layout_build(ctx, p, r, nullptr, n, n, L));
+  ABX_TRY(rowptr.reserve(n + 1));
+  DevBuf<int32_t> cnt_k;
+  ABX_TRY(cnt_k.reserve(n + 1));
+  KParams P = base_params(L);
+  P.kind = ABX_K_CONST;
+  P.counts = cnt_k.ptr;
+  ABX_CHECK_CUDA(cudaMemsetAsync(cnt_k.ptr, 0, (n + 1) * 4, s));
+  if (n > 0) ABX_TRY(launch_pairs<POL_COUNT, ABX_K_CONST>(ctx, P, true));
+  DevBuf<int64_t> rc;
+  ABX_TRY(rc.reserve(n + 1));
+  if (n) k_count_to_i64<<<ceil_div(n, TPB), TPB, 0, s>>>(cnt_k.ptr, L.rows->perm.ptr, n, rc.ptr);
+  std::vector<int64_t> h(n + 1);
+  if (n) ABX_CHECK_CUDA(cudaMemcpyAsync(h.data(), rc.ptr, n * 8, cudaMemcpyDeviceToHost, s));
+  ABX_CHECK_CUDA(cudaStreamSynchronize(s));
+  int64_t run = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t c = h[i];
+    h[i] = run;
+    run += c;
+  }
+  h[n] = run;
+  nnz = run;
+  ABX_CHECK_CUDA(cudaMemcpy(rowptr.ptr, h.data(), (n + 1) * 8, cudaMemcpyHostToDevice));
+  ABX_TRY(cols.reserve(run + 1));
+  if (n > 0 && run > 0) {
+    DevBuf<int64_t> rpk;
+    ABX_TRY(rpk.reserve(n));
+    k_rowptr_to_kernel<<<ceil_div(n, TPB), TPB, 0, s>>>(rowptr.ptr, L.rows->perm.ptr, n, rpk.ptr);
+    P.rowptr = rpk.ptr;
+    P.cols_out = cols.ptr;
+    ABX_TRY(launch_pairs<POL_LIST, ABX_K_CONST>(ctx, P, true));
+    ABX_CHECK_CUDA(cudaStreamSynchronize(s));
+  }
+  return ABX_OK;
+}
+
+namespace {
+constexpr int KNN_MAX = 64;
+
+// k nearest neighbours (FP64 distance with periodic images, ties broken by
+// storage index) of every particle of the layout's column set, by rings of
+// fine cells around the particle's anchor cell.  One thread per particle.
+__global__ void k_knn(KParams P, int k, int64_t n, int32_t *__restrict__ idx_out,
+                      double *__restrict__ d2_out) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const FineGrid &fg = P.fg;
+  double bd[KNN_MAX];
+  int bi[KNN_MAX];
+  int cnt = 0;
+  const int4 qc = P.qcell[q];
+  const D4 xq = P.qpos[q];
+  const int c[3] = {qc.x, qc.y, qc.z};
+  const double qx[3] = {xq.x, xq.y, xq.z};
+  double hmin = 1e300;
+  int Rmax = 0;
+  for (int e = 0; e < 3; ++e) {
+    if (e < fg.eoff) continue;
+    hmin = fmin(hmin, fg.h[e]);
+    Rmax = max(Rmax, fg.m[e]);
+  }
+  for (int R = 0; R <= Rmax; ++R) {
+    for (int o0 = -R; o0 <= R; ++o0) {
+      if (fg.m[0] == 1 && o0 != 0) continue;
+      for (int o1 = -R; o1 <= R; ++o1) {
+        if (fg.m[1] == 1 && o1 != 0) continue;
+        const bool edge01 = (abs(o0) == R) || (abs(o1) == R);
+        for (int o2 = -R; o2 <= R; o2 += (edge01 ? 1 : max(2 * R, 1))) {
+          int u[3] = {c[0] + o0, c[1] + o1, c[2] + o2}, img[3] = {0, 0, 0};
+          bool ok = true;
+          for (int e = 0; e < 3; ++e) {
+            if (u[e] >= 0 && u[e] < fg.m[e]) continue;
+            if (!fg.periodic[e] || u[e] < -fg.m[e] || u[e] >= 2 * fg.m[e]) { ok = false; break; }
+            if (u[e] < 0) { u[e] += fg.m[e]; img[e] = 1; } else { u[e] -= fg.m[e]; img[e] = -1; }
+          }
+          if (!ok) continue;
+          const uint32_t cell = ((uint32_t)u[0] * fg.m[1] + u[1]) * fg.m[2] + u[2];
+          const uint32_t b = P.cell_start[cell], e = P.cell_start[cell + 1];
+          for (uint32_t j = b; j < e; ++j) {
+            const double d2 = exact_d2(xq, P.cpos[j], img, fg);
+            const int sj = (int)P.cperm[j];
+            if (cnt == k && (d2 > bd[k - 1] || (d2 == bd[k - 1] && sj > bi[k - 1]))) continue;
+            int pos = cnt < k ? cnt++ : k - 1;
+            while (pos > 0 && (bd[pos - 1] > d2 || (bd[pos - 1] == d2 && bi[pos - 1] > sj))) {
+              bd[pos] = bd[pos - 1];
+              bi[pos] = bi[pos - 1];
+              --pos;
+            }
+            bd[pos] = d2;
+            bi[pos] = sj;
+          }
+        }
+      }
+    }
+    // every point of ring R+1 or beyond is at least R*h away
+    const double reach = fmax(R * hmin * (1.0 - 1e-9), 0.0);
+    if (cnt == k && bd[k - 1] <= reach * reach) break;
+  }
+  const int64_t row = P.cperm[q];
+  for (int j = 0; j < k; ++j) {
+    idx_out[row * k + j] = j < cnt ? bi[j] : -1;
+    if (d2_out) d2_out[row * k + j] = j < cnt ? bd[j] : -1.0;
+  }
+  (void)qx;
+}
+}  // namespace
+
+int knn_device(abx_particles *p, int k, int32_t *idx, double *d2) {
+  abx_context *ctx = p->ctx;
+  ABX_REQUIRE(k >= 1 && k <= KNN_MAX, ABX_ERR_INVALID, "k must be in 1..%d", KNN_MAX);
+  GridDesc g;
+  ABX_TRY(particles_grid_desc(p, &g));
+  const int64_t n = p->n;
+  if (n == 0) return ABX_OK;
+  double vol = 1.0;
+  for (int d = 0; d < p->dim; ++d) vol *= g.hi[d] - g.lo[d];
+  const double h = std::pow(std::max(1.0, k / 4.0) * vol / (double)n, 1.0 / p->dim);
+  PairLayout L;
+  ABX_TRY(layout_build(ctx, p, 3.0 * h, nullptr, n, n, L));
+  KParams P = base_params(L);
+  k_knn<<<ceil_div(n, 128), 128, 0, ctx->stream>>>(P, k, n, idx, d2);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  ABX_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  return ABX_OK;
+}
+
 }  // namespace abx
 
 using namespace abx;
@@ -1188,5 +1323,20 @@ extern "C" int abx_operator_matvec_noalloc(abx_operator *op, const double *b, do
   ABX_TRY(launch_pairs_kind<POL_MATVEC>(ctx, P, mixed));
   k_scatter_c<<<ceil_div(nr, TPB), TPB, 0, s>>>(ck, L.rows->perm.ptr, nr, c);
   ABX_CHECK_CUDA(cudaGetLastError());
+  return ABX_OK;
+}
+
+extern "C" int abx_knn(abx_particles *p, int k, int32_t *idx, double *d2) {
+  ABX_REQUIRE(p && (idx || p->n == 0), ABX_ERR_INVALID, "null argument");
+  ABX_REQUIRE(p->searchable, ABX_ERR_STATE, "init_neighbour_search not called on this particle set");
+  ABX_TRY(ctx_activate(p->ctx));
+  const int64_t n = p->n;
+  HostStage si, sd;
+  void *di, *dd = nullptr;
+  ABX_TRY(si.out(p->ctx, idx, (size_t)n * k * 4, &di));
+  if (d2) ABX_TRY(sd.out(p->ctx, d2, (size_t)n * k * 8, &dd));
+  ABX_TRY(knn_device(p, k, (int32_t *)di, (double *)dd));
+  ABX_TRY(si.finish(p->ctx, idx, (size_t)n * k * 4));
+  if (d2) ABX_TRY(sd.finish(p->ctx, d2, (size_t)n * k * 8));
   return ABX_OK;
 }

@@ -418,6 +418,17 @@ void OctTree::box(const GridDesc &g, int node, double *lo, double *hi) const {
   }
 }
 
+void particles_retain(abx_particles *p) { p->refs.fetch_add(1); }
+
+void particles_release(abx_particles *p) {
+  if (!p || p->refs.fetch_sub(1) != 1) return;
+  abx_context *ctx = p->ctx;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  delete p;
+  ctx_release(ctx);
+}
+
 int particles_grid_desc(const abx_particles *p, GridDesc *g) {
   ABX_REQUIRE(p && p->searchable, ABX_ERR_STATE,
               "init_neighbour_search not called on this particle set");
@@ -444,15 +455,13 @@ int abx_particles_create(abx_context *ctx, int dim, abx_particles **out) {
   }
   p->grid.dim = dim;
   p->grid.ncells = 1;
+  ctx_retain(ctx);
   *out = p;
   return ABX_OK;
 }
 
 int abx_particles_destroy(abx_particles *p) {
-  if (!p) return ABX_OK;
-  cudaSetDevice(p->ctx->device);
-  cudaStreamSynchronize(p->ctx->stream);
-  delete p;
+  particles_release(p);  // freed once no operator refers to it
   return ABX_OK;
 }
 

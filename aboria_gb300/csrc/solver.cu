@@ -728,17 +728,20 @@ int abx_precond_create_schwarz(abx_operator *op, int precision, abx_precond **ou
   pc->schwarz = S;
   pc->ctx = op->rows->ctx;
   pc->n = op->rows->n;
+  ctx_retain(pc->ctx);
   *out = pc;
   return ABX_OK;
 }
 
 int abx_precond_destroy(abx_precond *pc) {
   if (!pc) return ABX_OK;
-  cudaSetDevice(pc->ctx->device);
-  cudaStreamSynchronize(pc->ctx->stream);
+  abx_context *ctx = pc->ctx;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
   if (pc->schwarz) delete pc->schwarz;
   if (pc->spai) spai_free(pc);
   delete pc;
+  ctx_release(ctx);
   return ABX_OK;
 }
 
@@ -795,3 +798,51 @@ int abx_gmres_solve(abx_operator *A, abx_operator *A_check, abx_precond *M, cons
 }
 
 }  // extern "C"
+
+extern "C" int abx_gmres_solve_fallback(abx_operator *A, abx_operator *A_check,
+                                        abx_precond *M_learned, abx_operator *A_fallback,
+                                        const double *b, double *x, int restart,
+                                        int learned_max_iters, int max_iters, double tol,
+                                        int *iterations, double *rel_residual,
+                                        int *used_fallback) {
+  ABX_REQUIRE(A && b && x && iterations && rel_residual && used_fallback, ABX_ERR_INVALID,
+              "null argument");
+  abx_context *ctx = A->rows->ctx;
+  ABX_TRY(ctx_activate(ctx));
+  const int64_t n = A->rows->n;
+  HostStage sb, sx;
+  const void *bd, *x_in;
+  ABX_TRY(sb.in(ctx, b, n * sizeof(double), &bd));
+  ABX_TRY(sx.in(ctx, x, n * sizeof(double), &x_in));
+  double *xd = (double *)const_cast<void *>(x_in);
+  int it1 = 0, it2 = 0, restarts = 0;
+  double res = 1.0;
+  *used_fallback = 0;
+  if (M_learned) {
+    ABX_TRY(gmres_solve(A, A_check, M_learned, (const double *)bd, xd, restart,
+                        std::min(learned_max_iters, max_iters), tol, &it1, &res, &restarts));
+  }
+  if (!(res <= tol) && A_fallback) {
+    *used_fallback = 1;
+    Schwarz *S = nullptr;
+    if (!A_fallback->pairs) ABX_TRY(pair_layout_build(A_fallback));
+    ABX_TRY(schwarz_build(A_fallback, ABX_PREC_FP64, S));
+    abx_precond pc;
+    pc.kind = 1;
+    pc.schwarz = S;
+    pc.ctx = ctx;
+    pc.n = n;
+    const int st = gmres_solve(A, A_check, &pc, (const double *)bd, xd, restart,
+                               std::max(0, max_iters - it1), tol, &it2, &res, &restarts);
+    pc.schwarz = nullptr;
+    delete S;
+    if (st != ABX_OK) return st;
+  }
+  *iterations = it1 + it2;
+  *rel_residual = res;
+  if ((void *)xd != (void *)x) {
+    ABX_CHECK_CUDA(cudaMemcpyAsync(x, xd, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    ABX_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  return ABX_OK;
+}

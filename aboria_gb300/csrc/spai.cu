@@ -73,6 +73,451 @@ extern "C" int abx_precond_create_spai(abx_context *ctx, int64_t n, int k, const
   pc->spai = S;
   pc->ctx = ctx;
   pc->n = n;
+  ctx_retain(ctx);
   *out = pc;
+  return ABX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Exact local least-squares rows: CardinalFunctionsPreconditioner::factorize
+// (src/Preconditioners.h:1025-1082) restricted to a k-nearest-neighbour
+// support.  For row i with support S (its k nearest neighbours, i first), the
+// weights solve min_w || A(S,:)^T w - e_i ||_2 over all columns; only columns
+// in U = union of the kernel neighbourhoods of S carry non-zeros, so the
+// problem is the |U| x k system B w = e_i with B(u,s) = coeff(s, u)
+// (strict |dx| < r, periodic-corrected dx).  It is solved by Householder QR
+// with column pivoting (the reference calls colPivHouseholderQr).
+//
+// One CTA per row (persistent grid): U is collected in a shared-memory hash
+// set, B lives in a per-CTA global scratch slot (column-major), the QR steps
+// are warp-per-column reductions, the 32x32 back substitution is serial.
+namespace abx {
+namespace {
+
+constexpr int LS_T = 256;
+constexpr int LS_HT = 8192;   // hash slots
+constexpr int LS_MCAP = 3072; // max |U|
+constexpr int LS_K = 32;
+
+struct LsParams {
+  int dim, kind;
+  double p0, r2;
+  double L[3];
+  int periodic[3];
+  const double *pos;  // SoA storage order
+  int64_t n;
+  const int64_t *rowptr;
+  const int32_t *cols;
+  const int32_t *knn;  // n * k
+  int k;
+  double *scratch;     // gridDim.x * LS_MCAP * LS_K
+  double *vals;        // n * k
+  int *counter;
+  int *status;         // 0 ok; 1 |U| over capacity
+};
+
+template <int KIND> __device__ __forceinline__ double ls_coeff(const LsParams &P, int a, int b) {
+  double d2 = 0.0;
+  for (int d = 0; d < P.dim; ++d) {
+    double dx = __dsub_rn(P.pos[(int64_t)d * P.n + b], P.pos[(int64_t)d * P.n + a]);
+    if (P.periodic[d]) {
+      const double w = P.L[d];
+      while (dx > w / 2) dx -= w;
+      while (dx <= -w / 2) dx += w;
+    }
+    d2 = __dadd_rn(d2, __dmul_rn(dx, dx));
+  }
+  if (!(d2 < P.r2)) return 0.0;
+  if (KIND == ABX_K_CONST) return P.p0;
+  if (KIND == ABX_K_GAUSSIAN || KIND == ABX_K_COMPACT_GAUSSIAN) return exp(-d2 * P.p0);
+  if (KIND == ABX_K_WENDLAND_C2) {
+    const double q = sqrt(d2) * P.p0;
+    if (q >= 1.0) return 0.0;
+    const double t = 1.0 - q;
+    return t * t * t * t * (4.0 * q + 1.0);
+  }
+  if (KIND == ABX_K_LAPLACE) return 1.0 / (sqrt(d2) + P.p0);
+  if (KIND == ABX_K_MULTIQUADRIC) return sqrt(d2 + P.p0);
+  return 0.0;
+}
+
+__device__ __forceinline__ double block_sum(double v, double *red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int i = 0; i < LS_T / 32; ++i) t += red[i];
+  return t;
+}
+
+constexpr size_t LS_SMEM = (size_t)LS_MCAP * 2 * sizeof(double) + (size_t)LS_HT * sizeof(int) +
+                           (size_t)LS_MCAP * sizeof(int);
+
+template <int KIND> __global__ void __launch_bounds__(LS_T) k_spai_ls(LsParams P) {
+  extern __shared__ __align__(16) unsigned char ls_smem[];
+  double *e = (double *)ls_smem;
+  double *v = e + LS_MCAP;
+  int *hset = (int *)(v + LS_MCAP);
+  int *U = hset + LS_HT;
+  __shared__ double red[LS_T / 32];
+  __shared__ double cn[LS_K];
+  __shared__ int S[LS_K], perm[LS_K];
+  __shared__ int s_m, s_row, s_pi, s_rank;
+  __shared__ double s_alpha;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int k = P.k;
+  double *B = P.scratch + (size_t)blockIdx.x * LS_MCAP * LS_K;
+  for (;;) {
+    if (tid == 0) s_row = atomicAdd(P.counter, 1);
+    __syncthreads();
+    const int i = s_row;
+    if (i >= P.n) break;
+    for (int h = tid; h < LS_HT; h += LS_T) hset[h] = -1;
+    if (tid < k) {
+      S[tid] = P.knn[(int64_t)i * k + tid];
+      perm[tid] = tid;
+    }
+    if (tid == 0) s_m = 0;
+    __syncthreads();
+    // U: union of the support's kernel neighbourhoods (hash set)
+    for (int s = 0; s < k; ++s) {
+      const int a = S[s];
+      if (a < 0) continue;
+      for (int64_t t = P.rowptr[a] + tid; t < P.rowptr[a + 1]; t += LS_T) {
+        const int c = P.cols[t];
+        unsigned hsh = ((unsigned)c * 2654435761u) & (LS_HT - 1);
+        for (int probe = 0; probe < LS_HT; ++probe) {
+          const int old = atomicCAS(&hset[hsh], -1, c);
+          if (old == -1) {
+            const int slot = atomicAdd(&s_m, 1);
+            if (slot < LS_MCAP) U[slot] = c;
+            break;
+          }
+          if (old == c) break;
+          hsh = (hsh + 1) & (LS_HT - 1);
+        }
+      }
+    }
+    __syncthreads();
+    const int m = s_m;
+    if (m > LS_MCAP) {
+      if (tid == 0) atomicExch(P.status, 1);
+      __syncthreads();
+      continue;
+    }
+    // B(u, s) = coeff(S[s], U[u]); rhs e = e_i
+    for (int64_t t = tid; t < (int64_t)m * k; t += LS_T) {
+      const int s = (int)(t / m), u = (int)(t % m);
+      B[(size_t)s * LS_MCAP + u] = S[s] >= 0 ? ls_coeff<KIND>(P, S[s], U[u]) : 0.0;
+    }
+    for (int u = tid; u < m; u += LS_T) {
+      e[u] = (U[u] == i) ? 1.0 : 0.0;
+      if (U[u] == i) s_pi = u;
+    }
+    if (tid == 0) s_rank = k;
+    __syncthreads();
+    double r00 = 0.0;
+    for (int j = 0; j < k; ++j) {
+      // squared norms of the remaining columns over rows j..m-1
+      for (int c = j + warp; c < k; c += LS_T / 32) {
+        double sacc = 0.0;
+        for (int u = j + lane; u < m; u += 32) {
+          const double b = B[(size_t)c * LS_MCAP + u];
+          sacc = fma(b, b, sacc);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
+        if (lane == 0) cn[c] = sacc;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        int p = j;
+        for (int c = j + 1; c < k; ++c)
+          if (cn[c] > cn[p]) p = c;
+        red[0] = (double)p;
+      }
+      __syncthreads();
+      const int p = (int)red[0];
+      __syncthreads();
+      if (p != j) {
+        for (int u = tid; u < m; u += LS_T) {
+          const double t = B[(size_t)j * LS_MCAP + u];
+          B[(size_t)j * LS_MCAP + u] = B[(size_t)p * LS_MCAP + u];
+          B[(size_t)p * LS_MCAP + u] = t;
+        }
+        if (tid == 0) {
+          const int t = perm[j];
+          perm[j] = perm[p];
+          perm[p] = t;
+          const double c = cn[j];
+          cn[j] = cn[p];
+          cn[p] = c;
+        }
+      }
+      __syncthreads();
+      const double nrm = sqrt(cn[j]);
+      if (j == 0) r00 = nrm;
+      if (nrm <= 1e-13 * r00 || nrm == 0.0 || j >= m) {
+        if (tid == 0) s_rank = j;
+        __syncthreads();
+        break;
+      }
+      // Householder vector v = x - alpha e1, alpha = -sign(x0) |x|
+      const double x0 = B[(size_t)j * LS_MCAP + j];
+      const double alpha = x0 > 0 ? -nrm : nrm;
+      for (int u = j + tid; u < m; u += LS_T) v[u] = B[(size_t)j * LS_MCAP + u];
+      __syncthreads();
+      if (tid == 0) {
+        v[j] = x0 - alpha;
+        s_alpha = alpha;
+      }
+      __syncthreads();
+      double vv = 0.0;
+      for (int u = j + tid; u < m; u += LS_T) vv = fma(v[u], v[u], vv);
+      vv = block_sum(vv, red);
+      const double tau = vv > 0 ? 2.0 / vv : 0.0;
+      // apply to columns j+1..k-1 (warp per column) and to e
+      for (int c = j + 1 + warp; c < k; c += LS_T / 32) {
+        double sacc = 0.0;
+        for (int u = j + lane; u < m; u += 32) sacc = fma(v[u], B[(size_t)c * LS_MCAP + u], sacc);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
+        const double f = tau * sacc;
+        for (int u = j + lane; u < m; u += 32) B[(size_t)c * LS_MCAP + u] -= f * v[u];
+      }
+      double se = 0.0;
+      for (int u = j + tid; u < m; u += LS_T) se = fma(v[u], e[u], se);
+      se = block_sum(se, red);
+      for (int u = j + tid; u < m; u += LS_T) e[u] -= tau * se * v[u];
+      __syncthreads();
+      if (tid == 0) B[(size_t)j * LS_MCAP + j] = s_alpha;
+      __syncthreads();
+    }
+    __syncthreads();
+    if (tid == 0) {
+      const int rk = s_rank;
+      double w[LS_K];
+      for (int j = k - 1; j >= 0; --j) {
+        if (j >= rk) {
+          w[j] = 0.0;
+          continue;
+        }
+        double t = e[j];
+        for (int c = j + 1; c < rk; ++c) t -= B[(size_t)c * LS_MCAP + j] * w[c];
+        w[j] = t / B[(size_t)j * LS_MCAP + j];
+      }
+      for (int j = 0; j < k; ++j) P.vals[(int64_t)i * k + perm[j]] = w[j];
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+// Exact least-squares SPAI rows for the sparse operator `op` (rows == cols)
+// on the k-nearest-neighbour support; outputs device arrays cols (n*k) and
+// vals (n*k) in storage order.
+int self_csr_device(abx_particles *p, double r, DevBuf<int64_t> &rowptr, DevBuf<int32_t> &cols,
+                    int64_t &nnz);
+int knn_device(abx_particles *p, int k, int32_t *idx, double *d2);
+
+int spai_exact_rows(abx_operator *op, int k, int32_t *cols_out, double *vals_out) {
+  abx_particles *p = op->rows;
+  abx_context *ctx = p->ctx;
+  cudaStream_t s = ctx->stream;
+  ABX_REQUIRE(op->kind == 0 && op->rows == op->cols, ABX_ERR_INVALID,
+              "SPAI rows need a square sparse operator (rows == cols)");
+  ABX_REQUIRE(k >= 1 && k <= LS_K, ABX_ERR_INVALID, "k must be in 1..%d", LS_K);
+  ABX_REQUIRE(op->k.kind != ABX_K_SCALAR_SUM, ABX_ERR_INVALID, "kernel not supported");
+  const int64_t n = p->n;
+  if (n == 0) return ABX_OK;
+  ABX_TRY(knn_device(p, k, cols_out, nullptr));
+  DevBuf<int64_t> rowptr;
+  DevBuf<int32_t> cols;
+  int64_t nnz = 0;
+  ABX_TRY(self_csr_device(p, op->radius, rowptr, cols, nnz));
+  const int grid = (int)std::min<int64_t>(n, (int64_t)ctx->num_sms * 2);
+  DevBuf<double> scratch;
+  DevBuf<int> flags;
+  ABX_TRY(scratch.reserve((size_t)grid * LS_MCAP * LS_K));
+  ABX_TRY(flags.reserve(2));
+  ABX_CHECK_CUDA(cudaMemsetAsync(flags.ptr, 0, 2 * sizeof(int), s));
+  LsParams P{};
+  P.dim = p->dim;
+  P.kind = op->k.kind;
+  P.p0 = op->k.p[0];
+  P.r2 = op->radius * op->radius;
+  for (int d = 0; d < 3; ++d) {
+    P.L[d] = p->grid.hi[d] - p->grid.lo[d];
+    P.periodic[d] = d < p->dim ? p->grid.periodic[d] : 0;
+  }
+  P.pos = p->pos.ptr;
+  P.n = n;
+  P.rowptr = rowptr.ptr;
+  P.cols = cols.ptr;
+  P.knn = cols_out;
+  P.k = k;
+  P.scratch = scratch.ptr;
+  P.vals = vals_out;
+  P.counter = flags.ptr;
+  P.status = flags.ptr + 1;
+  auto launch = [&](auto kern) -> int {
+    ABX_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)LS_SMEM));
+    kern<<<grid, LS_T, LS_SMEM, s>>>(P);
+    return ABX_OK;
+  };
+  switch (P.kind) {
+  case ABX_K_CONST: ABX_TRY(launch(k_spai_ls<ABX_K_CONST>)); break;
+  case ABX_K_GAUSSIAN: ABX_TRY(launch(k_spai_ls<ABX_K_GAUSSIAN>)); break;
+  case ABX_K_WENDLAND_C2: ABX_TRY(launch(k_spai_ls<ABX_K_WENDLAND_C2>)); break;
+  case ABX_K_COMPACT_GAUSSIAN: ABX_TRY(launch(k_spai_ls<ABX_K_COMPACT_GAUSSIAN>)); break;
+  case ABX_K_LAPLACE: ABX_TRY(launch(k_spai_ls<ABX_K_LAPLACE>)); break;
+  case ABX_K_MULTIQUADRIC: ABX_TRY(launch(k_spai_ls<ABX_K_MULTIQUADRIC>)); break;
+  }
+  ABX_CHECK_CUDA(cudaGetLastError());
+  int st[2];
+  ABX_CHECK_CUDA(cudaMemcpyAsync(st, flags.ptr, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  ABX_CHECK_CUDA(cudaStreamSynchronize(s));
+  ABX_REQUIRE(st[1] == 0, ABX_ERR_CAPACITY,
+              "SPAI least squares: a row's column set exceeds %d entries", LS_MCAP);
+  return ABX_OK;
+}
+
+}  // namespace abx
+
+extern "C" int abx_spai_exact_rows(abx_operator *op, int k, int32_t *cols, double *vals) {
+  ABX_REQUIRE(op && cols && vals, ABX_ERR_INVALID, "null argument");
+  ABX_TRY(ctx_activate(op->rows->ctx));
+  const int64_t n = op->rows->n;
+  HostStage sc, sv;
+  void *dc, *dv;
+  ABX_TRY(sc.out(op->rows->ctx, cols, (size_t)n * k * 4, &dc));
+  ABX_TRY(sv.out(op->rows->ctx, vals, (size_t)n * k * 8, &dv));
+  ABX_TRY(spai_exact_rows(op, k, (int32_t *)dc, (double *)dv));
+  ABX_TRY(sc.finish(op->rows->ctx, cols, (size_t)n * k * 4));
+  ABX_TRY(sv.finish(op->rows->ctx, vals, (size_t)n * k * 8));
+  return ABX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Learned approximate inverse: features -> MLP (BF16 tensor cores) -> weights.
+namespace abx {
+int mlp_infer_bf16(abx_mlp *M, const float *x, int64_t n, float *y);
+int mlp_infer_fp32(abx_mlp *M, const float *x, int64_t n, float *y);
+
+namespace {
+// feats[i][j*D + d] = eps * (x_{S_ij} - x_i)_d with periodic minimum image.
+__global__ void k_spai_features(const double *__restrict__ pos, int64_t n, int dim,
+                                const int32_t *__restrict__ knn, int k, double eps, GridDesc g,
+                                float *__restrict__ feats) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * k) return;
+  const int64_t i = t / k;
+  const int j = (int)(t % k);
+  const int s = knn[t];
+  for (int d = 0; d < dim; ++d) {
+    double dx = s >= 0 ? pos[(int64_t)d * n + s] - pos[(int64_t)d * n + i] : 0.0;
+    if (g.periodic[d]) {
+      const double w = g.hi[d] - g.lo[d];
+      while (dx > w / 2) dx -= w;
+      while (dx <= -w / 2) dx += w;
+    }
+    feats[t * dim + d] = (float)(eps * dx);
+  }
+}
+
+__global__ void k_f2d_masked(const float *__restrict__ y, const int32_t *__restrict__ cols,
+                             int64_t n, double *__restrict__ vals) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) vals[i] = cols[i] >= 0 ? (double)y[i] : 0.0;
+}
+}  // namespace
+
+int knn_device(abx_particles *p, int k, int32_t *idx, double *d2);
+
+int spai_features_device(abx_particles *p, const int32_t *knn, int k, double eps, float *feats) {
+  const int64_t n = p->n;
+  if (n == 0) return ABX_OK;
+  k_spai_features<<<ceil_div((size_t)n * k, 256), 256, 0, p->ctx->stream>>>(
+      p->pos.ptr, n, p->dim, knn, k, eps, p->grid, feats);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  return ABX_OK;
+}
+
+}  // namespace abx
+
+extern "C" int abx_spai_features(abx_particles *p, const int32_t *knn, int k, double eps,
+                                 float *feats) {
+  ABX_REQUIRE(p && (p->n == 0 || (knn && feats)), ABX_ERR_INVALID, "null argument");
+  ABX_TRY(ctx_activate(p->ctx));
+  const int64_t n = p->n;
+  HostStage a, b;
+  const void *dk;
+  void *df;
+  ABX_TRY(a.in(p->ctx, knn, (size_t)n * k * 4, &dk));
+  ABX_TRY(b.out(p->ctx, feats, (size_t)n * k * p->dim * 4, &df));
+  ABX_TRY(spai_features_device(p, (const int32_t *)dk, k, eps, (float *)df));
+  ABX_TRY(b.finish(p->ctx, feats, (size_t)n * k * p->dim * 4));
+  ABX_CHECK_CUDA(cudaStreamSynchronize(p->ctx->stream));
+  return ABX_OK;
+}
+
+extern "C" int abx_precond_create_learned(abx_operator *op, abx_mlp *mlp, double eps, int k,
+                                          int precision, abx_precond **out) {
+  ABX_REQUIRE(op && mlp && out, ABX_ERR_INVALID, "null argument");
+  ABX_REQUIRE(op->rows == op->cols, ABX_ERR_INVALID, "needs a square operator");
+  abx_particles *p = op->rows;
+  ABX_REQUIRE(p->searchable, ABX_ERR_STATE, "init_neighbour_search not called");
+  ABX_REQUIRE(k >= 1 && k <= 64, ABX_ERR_INVALID, "k must be in 1..64");
+  ABX_TRY(ctx_activate(p->ctx));
+  const int64_t n = p->n;
+  abx_precond *pc = new abx_precond();
+  pc->kind = 2;
+  pc->ctx = p->ctx;
+  pc->n = n;
+  pc->spai = new Spai();
+  Spai *S = pc->spai;
+  S->n = n;
+  S->k = k;
+  int st = ABX_OK;
+  DevBuf<float> feats, y;
+  if ((st = S->cols.reserve((size_t)n * k + 1)) || (st = S->vals.reserve((size_t)n * k + 1)) ||
+      (st = feats.reserve((size_t)n * k * p->dim + 1)) || (st = y.reserve((size_t)n * k + 1)) ||
+      (n > 0 && ((st = knn_device(p, k, S->cols.ptr, nullptr)) ||
+                 (st = spai_features_device(p, S->cols.ptr, k, eps, feats.ptr)) ||
+                 (st = precision == ABX_PREC_FP64
+                           ? mlp_infer_fp32(mlp, feats.ptr, n, y.ptr)
+                           : mlp_infer_bf16(mlp, feats.ptr, n, y.ptr))))) {
+    delete pc->spai;
+    delete pc;
+    return st;
+  }
+  if (n > 0) {
+    k_f2d_masked<<<ceil_div((size_t)n * k, 256), 256, 0, p->ctx->stream>>>(y.ptr, S->cols.ptr,
+                                                                          (size_t)n * k,
+                                                                          S->vals.ptr);
+    cudaError_t e = cudaStreamSynchronize(p->ctx->stream);
+    if (e != cudaSuccess) {
+      delete pc->spai;
+      delete pc;
+      set_error("learned preconditioner: %s", cudaGetErrorString(e));
+      return ABX_ERR_CUDA;
+    }
+  }
+  ctx_retain(pc->ctx);
+  *out = pc;
+  return ABX_OK;
+}
+
+extern "C" int abx_precond_get_spai(abx_precond *pc, int32_t *cols, double *vals) {
+  ABX_REQUIRE(pc && pc->kind == 2 && pc->spai, ABX_ERR_INVALID, "not a sparse approximate inverse");
+  ABX_TRY(ctx_activate(pc->ctx));
+  const size_t nk = (size_t)pc->spai->n * pc->spai->k;
+  if (cols) ABX_CHECK_CUDA(cudaMemcpy(cols, pc->spai->cols.ptr, nk * 4, cudaMemcpyDefault));
+  if (vals) ABX_CHECK_CUDA(cudaMemcpy(vals, pc->spai->vals.ptr, nk * 8, cudaMemcpyDefault));
   return ABX_OK;
 }

@@ -134,6 +134,13 @@ ABX_API int abx_radius_count(abx_particles *p, int64_t nq, const double *q, doub
 ABX_API int abx_radius_query_csr(abx_particles *p, int64_t nq, const double *q, double r,
                          int64_t *rowptr, int32_t *cols, int64_t cap);
 
+/* k nearest neighbours of every stored particle among the stored particles
+ * (itself included, FP64 distances with periodic images, ties by storage
+ * index), k <= 64: idx[i*k + j] storage indices in increasing distance, d2
+ * (optional) the squared distances.  No counterpart in the reference; used to
+ * build the support of the learned sparse approximate inverse. */
+ABX_API int abx_knn(abx_particles *p, int k, int32_t *idx, double *d2);
+
 /* -------------------------------------------------------------- operators --
  * create_sparse_operator (src/Operators.h:478-515, KernelSparseConst
  * src/Kernels.h:754-776), create_dense_operator (src/Operators.h:312-318,
@@ -192,6 +199,25 @@ ABX_API int abx_precond_create_schwarz(abx_operator *op, int precision, abx_prec
  * src/Preconditioners.h:1025-1103). */
 ABX_API int abx_precond_create_spai(abx_context *ctx, int64_t n, int k, const int32_t *cols,
                                     const double *vals, abx_precond **out);
+/* Exact FP64 least-squares approximate-inverse rows on a k-nearest-neighbour
+ * support (k <= 32): CardinalFunctionsPreconditioner::factorize
+ * (src/Preconditioners.h:1025-1082) with the support restricted to the k
+ * nearest neighbours of each particle; column-pivoted Householder QR.  cols
+ * and vals are n*k (storage indices / weights), usable with
+ * abx_precond_create_spai; they are also the learned model's training
+ * labels. */
+ABX_API int abx_spai_exact_rows(abx_operator *op, int k, int32_t *cols, double *vals);
+/* Features of the learned approximate inverse: feats[i][j*dim + d] =
+ * eps * (x_{knn[i][j]} - x_i)_d (periodic minimum image), n*k*dim floats. */
+ABX_API int abx_spai_features(abx_particles *p, const int32_t *knn, int k, double eps,
+                              float *feats);
+/* Learned sparse approximate inverse (no counterpart in the reference): k-NN
+ * support, features as above, weights from the MLP (precision ABX_PREC_MIXED:
+ * BF16 tensor-core inference; ABX_PREC_FP64: FP32 SIMT inference). */
+typedef struct abx_mlp abx_mlp;
+ABX_API int abx_precond_create_learned(abx_operator *op, abx_mlp *mlp, double eps, int k,
+                                       int precision, abx_precond **out);
+ABX_API int abx_precond_get_spai(abx_precond *pc, int32_t *cols, double *vals);
 ABX_API int abx_precond_destroy(abx_precond *pc);
 ABX_API int abx_precond_apply(abx_precond *pc, const double *b, double *x);
 ABX_API int abx_precond_stats(abx_precond *pc, int64_t *ndomains, int64_t *max_size,
@@ -207,6 +233,45 @@ ABX_API int abx_precond_stats(abx_precond *pc, int64_t *ndomains, int64_t *max_s
 ABX_API int abx_gmres_solve(abx_operator *A, abx_operator *A_check, abx_precond *M,
                             const double *b, double *x, int restart, int max_iters, double tol,
                             int *iterations, double *rel_residual);
+
+/* ---------------------------------------------------------------- MLP --
+ * The learned preconditioner's model (no counterpart in the reference):
+ * in_dim -> nhidden x hidden (SiLU) -> out_dim, FP32 parameters, trained with
+ * the library's own forward/backward/Adam kernels on normalised targets
+ * ((y - out_shift) / out_scale), inference in BF16 on the tensor cores. */
+ABX_API int abx_mlp_create(abx_context *ctx, int in_dim, int hidden, int nhidden, int out_dim,
+                           uint64_t seed, abx_mlp **out);
+ABX_API int abx_mlp_destroy(abx_mlp *mlp);
+ABX_API int64_t abx_mlp_num_params(const abx_mlp *mlp);
+ABX_API int abx_mlp_set_normalization(abx_mlp *mlp, float in_scale, const float *out_scale,
+                                      const float *out_shift);
+/* Output transform applied after denormalisation at inference: kind 0 none,
+ * kind 1 y -> c * sinh(y) (for targets trained as asinh(w / c)). */
+ABX_API int abx_mlp_set_output_transform(abx_mlp *mlp, int kind, float c);
+ABX_API int abx_mlp_get_params(abx_mlp *mlp, float *params);
+ABX_API int abx_mlp_set_params(abx_mlp *mlp, const float *params);
+/* Loss (mean squared error on normalised targets) and its gradient w.r.t.
+ * the flat parameters for one batch, without updating. */
+ABX_API int abx_mlp_gradients(abx_mlp *mlp, const float *x, const float *y, int64_t batch,
+                              float *grads, float *loss);
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on one batch. */
+ABX_API int abx_mlp_train_step(abx_mlp *mlp, const float *x, const float *y, int64_t batch,
+                               float lr, float *loss);
+/* y = model(x) (denormalised); precision ABX_PREC_MIXED = BF16 tensor cores. */
+ABX_API int abx_mlp_forward(abx_mlp *mlp, const float *x, int64_t n, float *y, int precision);
+ABX_API int abx_mlp_save(abx_mlp *mlp, const char *path);
+ABX_API int abx_mlp_load(abx_context *ctx, const char *path, abx_mlp **out);
+
+/* Learned-then-fallback solve: GMRES with M_learned for at most
+ * learned_max_iters iterations; if that does not reach tol, the restricted
+ * additive Schwarz preconditioner of A_fallback (an FP64 sparse operator on
+ * an octree particle set) is built and GMRES continues from the current x.
+ * *used_fallback reports which preconditioner finished the solve. */
+ABX_API int abx_gmres_solve_fallback(abx_operator *A, abx_operator *A_check, abx_precond *M_learned,
+                                     abx_operator *A_fallback, const double *b, double *x,
+                                     int restart, int learned_max_iters, int max_iters,
+                                     double tol, int *iterations, double *rel_residual,
+                                     int *used_fallback);
 
 #ifdef __cplusplus
 }

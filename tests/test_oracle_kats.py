@@ -130,3 +130,21 @@ def test_octree_leaves_partition_and_sizes():
     for i in range(0, len(t.leaf_tag), 37):
         shift = (8 - t.leaf_level[i]) * 3
         assert np.all((t.tags[t.leaf_begin[i]:t.leaf_end[i]] >> shift) == (t.leaf_tag[i] >> shift))
+
+
+def test_mlp_oracle_gradient_matches_finite_differences():
+    import mlp_oracle
+    rng = np.random.default_rng(90)
+    dims = [6, 5, 5, 3]
+    n = sum(dims[i] * dims[i + 1] + dims[i + 1] for i in range(3))
+    p = rng.standard_normal(n) * 0.5
+    x = rng.standard_normal((7, 6))
+    y = rng.standard_normal((7, 3))
+    sc, sh = np.array([2.0, 1.0, 0.5]), np.array([0.1, -0.2, 0.0])
+    loss, g = mlp_oracle.loss_and_grad(p, dims, x, y, sc, sh)
+    for i in rng.choice(n, 12, replace=False):
+        e = np.zeros(n)
+        e[i] = 1e-6
+        lp, _ = mlp_oracle.loss_and_grad(p + e, dims, x, y, sc, sh)
+        lm, _ = mlp_oracle.loss_and_grad(p - e, dims, x, y, sc, sh)
+        assert abs((lp - lm) / 2e-6 - g[i]) < 1e-6 * max(1.0, abs(g[i]))
