@@ -27,7 +27,7 @@ __all__ = [
     "K_CONST", "K_GAUSSIAN", "K_WENDLAND_C2", "K_COMPACT_GAUSSIAN", "K_LAPLACE",
     "K_MULTIQUADRIC", "K_SCALAR_SUM", "default_context", "Preconditioner",
     "schwarz_preconditioner", "spai_preconditioner", "gmres", "knn", "spai_exact_rows", "MLP",
-    "spai_features", "learned_preconditioner", "spai_rows", "gmres_with_fallback",
+    "spai_features", "learned_preconditioner", "spai_local_inverse_rows", "spai_rows", "gmres_with_fallback",
 ]
 
 PREC_FP64, PREC_MIXED = 0, 1
@@ -378,6 +378,16 @@ def knn(p: Particles, k: int = 32):
     d2 = np.empty((n, k), dtype=np.float64)
     _check(lib().abx_knn(p._h, int(k), _ptr(idx), _ptr(d2)), "abx_knn")
     return idx, d2
+
+
+def spai_local_inverse_rows(op: Operator, k: int = 32):
+    """Rows of the k-NN local block inverses (Schwarz block solves)."""
+    n = op.shape[0]
+    cols = np.empty((n, k), dtype=np.int32)
+    vals = np.empty((n, k), dtype=np.float64)
+    _check(lib().abx_spai_local_inverse_rows(op._h, int(k), _ptr(cols), _ptr(vals)),
+           "abx_spai_local_inverse_rows")
+    return cols, vals
 
 
 def spai_exact_rows(op: Operator, k: int = 32):

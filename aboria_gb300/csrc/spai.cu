@@ -114,6 +114,7 @@ struct LsParams {
   double *vals;        // n * k
   int *counter;
   int *status;         // 0 ok; 1 |U| over capacity
+  int local;           // 1: U = S (row of the local block inverse)
 };
 
 template <int KIND> __device__ __forceinline__ double ls_coeff(const LsParams &P, int a, int b) {
@@ -182,8 +183,12 @@ template <int KIND> __global__ void __launch_bounds__(LS_T) k_spai_ls(LsParams P
     }
     if (tid == 0) s_m = 0;
     __syncthreads();
+    if (P.local) {  // square local system: U = S
+      if (tid < k) U[tid] = S[tid] >= 0 ? S[tid] : -1 - tid;
+      if (tid == 0) s_m = k;
+    }
     // U: union of the support's kernel neighbourhoods (hash set)
-    for (int s = 0; s < k; ++s) {
+    for (int s = 0; s < k && !P.local; ++s) {
       const int a = S[s];
       if (a < 0) continue;
       for (int64_t t = P.rowptr[a] + tid; t < P.rowptr[a + 1]; t += LS_T) {
@@ -211,7 +216,7 @@ template <int KIND> __global__ void __launch_bounds__(LS_T) k_spai_ls(LsParams P
     // B(u, s) = coeff(S[s], U[u]); rhs e = e_i
     for (int64_t t = tid; t < (int64_t)m * k; t += LS_T) {
       const int s = (int)(t / m), u = (int)(t % m);
-      B[(size_t)s * LS_MCAP + u] = S[s] >= 0 ? ls_coeff<KIND>(P, S[s], U[u]) : 0.0;
+      B[(size_t)s * LS_MCAP + u] = (S[s] >= 0 && U[u] >= 0) ? ls_coeff<KIND>(P, S[s], U[u]) : 0.0;
     }
     for (int u = tid; u < m; u += LS_T) {
       e[u] = (U[u] == i) ? 1.0 : 0.0;
@@ -324,7 +329,7 @@ int self_csr_device(abx_particles *p, double r, DevBuf<int64_t> &rowptr, DevBuf<
                     int64_t &nnz);
 int knn_device(abx_particles *p, int k, int32_t *idx, double *d2);
 
-int spai_exact_rows(abx_operator *op, int k, int32_t *cols_out, double *vals_out) {
+int spai_exact_rows(abx_operator *op, int k, int32_t *cols_out, double *vals_out, int local) {
   abx_particles *p = op->rows;
   abx_context *ctx = p->ctx;
   cudaStream_t s = ctx->stream;
@@ -364,6 +369,7 @@ int spai_exact_rows(abx_operator *op, int k, int32_t *cols_out, double *vals_out
   P.vals = vals_out;
   P.counter = flags.ptr;
   P.status = flags.ptr + 1;
+  P.local = local;
   auto launch = [&](auto kern) -> int {
     ABX_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)LS_SMEM));
@@ -397,7 +403,7 @@ extern "C" int abx_spai_exact_rows(abx_operator *op, int k, int32_t *cols, doubl
   void *dc, *dv;
   ABX_TRY(sc.out(op->rows->ctx, cols, (size_t)n * k * 4, &dc));
   ABX_TRY(sv.out(op->rows->ctx, vals, (size_t)n * k * 8, &dv));
-  ABX_TRY(spai_exact_rows(op, k, (int32_t *)dc, (double *)dv));
+  ABX_TRY(spai_exact_rows(op, k, (int32_t *)dc, (double *)dv, 0));
   ABX_TRY(sc.finish(op->rows->ctx, cols, (size_t)n * k * 4));
   ABX_TRY(sv.finish(op->rows->ctx, vals, (size_t)n * k * 8));
   return ABX_OK;
@@ -519,5 +525,19 @@ extern "C" int abx_precond_get_spai(abx_precond *pc, int32_t *cols, double *vals
   const size_t nk = (size_t)pc->spai->n * pc->spai->k;
   if (cols) ABX_CHECK_CUDA(cudaMemcpy(cols, pc->spai->cols.ptr, nk * 4, cudaMemcpyDefault));
   if (vals) ABX_CHECK_CUDA(cudaMemcpy(vals, pc->spai->vals.ptr, nk * 8, cudaMemcpyDefault));
+  return ABX_OK;
+}
+
+extern "C" int abx_spai_local_inverse_rows(abx_operator *op, int k, int32_t *cols, double *vals) {
+  ABX_REQUIRE(op && cols && vals, ABX_ERR_INVALID, "null argument");
+  ABX_TRY(ctx_activate(op->rows->ctx));
+  const int64_t n = op->rows->n;
+  HostStage sc, sv;
+  void *dc, *dv;
+  ABX_TRY(sc.out(op->rows->ctx, cols, (size_t)n * k * 4, &dc));
+  ABX_TRY(sv.out(op->rows->ctx, vals, (size_t)n * k * 8, &dv));
+  ABX_TRY(spai_exact_rows(op, k, (int32_t *)dc, (double *)dv, 1));
+  ABX_TRY(sc.finish(op->rows->ctx, cols, (size_t)n * k * 4));
+  ABX_TRY(sv.finish(op->rows->ctx, vals, (size_t)n * k * 8));
   return ABX_OK;
 }

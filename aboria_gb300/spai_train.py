@@ -1,15 +1,20 @@
 """Train the learned sparse-approximate-inverse model on the GPU.
 
-Training data: exact FP64 least-squares approximate-inverse rows
-(``abx_spai_exact_rows``: CardinalFunctionsPreconditioner::factorize,
-src/Preconditioners.h:1025-1082, on a 32-nearest-neighbour support) of
-compactly supported Gaussian RBF operators exp(-(eps |dx|)^2), cut where the
+Training data: exact FP64 Schwarz block-solve rows on the 32-nearest-neighbour
+domain of each particle (``abx_spai_local_inverse_rows``: row i of the local
+block inverse), of compactly supported Gaussian RBF operators
+exp(-(eps |dx|)^2), cut where the
 Gaussian has decayed to e^-16 (r = 4/eps), on seeded training instances:
 2-D point sets, uniform or an 8-component Gaussian mixture (sigma 0.05), with
-the scaled shape parameter eps*h drawn uniform on [0.9, 1.6] (h = N^-1/2 the
-mean spacing; below eps*h ~ 0.75 the truncated Gaussian matrix is indefinite
-or numerically singular and no preconditioner reaches 1e-8).  Rows whose
-weights exceed 1e3 in magnitude (locally ill-posed clusters) are dropped.  Instance seeds start at 1000, disjoint from every test seed.
+the scaled shape parameter eps*h drawn uniform on [2, 3] (h = N^-1/2 the mean
+spacing).  Below eps*h ~ 0.75 the truncated Gaussian matrix is indefinite or
+numerically singular and no preconditioner reaches 1e-8; between ~0.75 and 2
+its local inverses have weights up to 1e5 (near-coincident points) and a
+sparse approximate inverse stops working once its weights carry ~0.3% error,
+which no regression reaches.  The least-squares rows
+(``abx_spai_exact_rows``) depend on geometry beyond the 32 neighbours the
+features describe, so they are not used as labels.  Rows whose weights exceed
+1e3 in magnitude are dropped.  Instance seeds start at 1000, disjoint from every test seed.
 Features are the 32 neighbours' relative positions scaled by eps; targets are
 the 32 weights w, trained as asinh(w / c) (c the median |w|, which compresses
 the heavy tails of ill-conditioned rows) normalised per output by mean and
@@ -41,7 +46,7 @@ def instance(seed, n, dim=2):
         centres = rng.uniform(0.15, 0.85, size=(8, dim))
         pos = centres[rng.integers(0, 8, size=n)] + 0.05 * rng.standard_normal((n, dim))
         pos = np.clip(pos, 0.0, np.nextafter(1.0, 0.0))
-    eh = rng.uniform(0.9, 1.6)
+    eh = rng.uniform(2.0, 3.0)
     eps = eh * np.sqrt(n)
     return pos, eps
 
@@ -51,7 +56,7 @@ def make_rows(seed, n, dim=2):
     p = ab.Particles(dim).set(pos)
     p.init_octree([0.0] * dim, [1.0] * dim, [False] * dim, 256)
     op = ab.create_sparse_operator(p, p, 4.0 / eps, ab.Kernel.make(ab.K_COMPACT_GAUSSIAN, eps * eps))
-    cols, vals = ab.spai_exact_rows(op, K)
+    cols, vals = ab.spai_local_inverse_rows(op, K)
     feats = ab.spai_features(p, cols, eps)
     return feats, vals.astype(np.float32)
 

@@ -207,6 +207,12 @@ ABX_API int abx_precond_create_spai(abx_context *ctx, int64_t n, int k, const in
  * abx_precond_create_spai; they are also the learned model's training
  * labels. */
 ABX_API int abx_spai_exact_rows(abx_operator *op, int k, int32_t *cols, double *vals);
+/* Schwarz block-solve rows on the k-nearest-neighbour domain: row i of
+ * (A_SS)^{-1} restricted to i, i.e. the solve of the k x k local block
+ * (SchwartzPreconditioner::factorize + _solve_impl, src/Preconditioners.h:
+ * 1403-1522, with a one-particle restriction).  These are the learned
+ * model's training labels. */
+ABX_API int abx_spai_local_inverse_rows(abx_operator *op, int k, int32_t *cols, double *vals);
 /* Features of the learned approximate inverse: feats[i][j*dim + d] =
  * eps * (x_{knn[i][j]} - x_i)_d (periodic minimum image), n*k*dim floats. */
 ABX_API int abx_spai_features(abx_particles *p, const int32_t *knn, int k, double eps,
