@@ -27,7 +27,7 @@ __all__ = [
     "K_CONST", "K_GAUSSIAN", "K_WENDLAND_C2", "K_COMPACT_GAUSSIAN", "K_LAPLACE",
     "K_MULTIQUADRIC", "K_SCALAR_SUM", "default_context", "Preconditioner",
     "schwarz_preconditioner", "spai_preconditioner", "gmres", "knn", "spai_exact_rows", "MLP",
-    "spai_features", "learned_preconditioner", "spai_local_inverse_rows", "spai_rows", "gmres_with_fallback",
+    "spai_features", "learned_preconditioner", "spai_local_inverse_rows", "create_fmm_operator", "fmm_stats", "spai_rows", "gmres_with_fallback",
 ]
 
 PREC_FP64, PREC_MIXED = 0, 1
@@ -525,3 +525,19 @@ def gmres_with_fallback(A: Operator, b, M_learned: Preconditioner | None, A_fall
                                           int(max_iters), float(tol), C.byref(it), C.byref(res),
                                           C.byref(fb)), "abx_gmres_solve_fallback")
     return x, it.value, res.value, bool(fb.value)
+
+
+def create_fmm_operator(p: Particles, kernel: Kernel, order: int = 3,
+                        precision: int = PREC_FP64) -> Operator:
+    """``create_fmm_operator<order>`` on the octree of ``p``."""
+    h = C.c_void_p()
+    _check(lib().abx_create_fmm_operator(p._h, C.byref(kernel), int(order), C.byref(h)),
+           "abx_create_fmm_operator")
+    return Operator(h, p, p).set_precision(precision)
+
+
+def fmm_stats(op: Operator):
+    a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+    t = C.c_double()
+    _check(lib().abx_fmm_stats(op._h, C.byref(a), C.byref(b), C.byref(c), C.byref(t)), "fmm_stats")
+    return {"m2l_pairs": a.value, "matrices": b.value, "leaves": c.value, "plan_s": t.value}

@@ -1,0 +1,805 @@
+// Black-box Chebyshev FMM operator (create_fmm_operator, src/Operators.h:
+// 401-407; KernelFMM src/Kernels.h:533-576).
+//
+// Reference algorithm (restated, not translated):
+//  * expansions: BlackBoxExpansions (src/detail/FastMultipoleMethod.h:96-368)
+//    with Chebyshev interpolation (src/detail/Chebyshev.h:84-153, 245-294):
+//    R_j(x) = prod_d S_{m_d(j)}(x_d), nodes in lattice order (last dim fastest);
+//  * traversal: FastMultipoleMethod::matrix_vector_multiply
+//    (src/FastMultipoleMethod.h:111-548) with theta_condition
+//    (src/detail/FastMultipoleMethod.h:1249-1279), P2P at target leaves over
+//    the connected list (leaf or whole subtree).
+//
+// GB300 design: the traversal runs once per operator on the host and is
+// flattened into per-level lists (M2L pairs, P2P leaf pairs, parent/child
+// links); translation operators are precomputed instead of re-evaluating the
+// kernel at node pairs on every call: one M2M/L2L matrix per child octant
+// (the Chebyshev interpolation is scale invariant) and one M2L matrix per
+// (level, box offset) -- M2L pairs at one level differ only by an integer box
+// offset in [-3, 3]^D.  Each matvec is five passes of device kernels: P2M,
+// M2M (bottom-up), M2L, L2L (top-down), then L2P+P2P per target leaf.
+//
+// M2L in the mixed-precision mode runs as a GEMM per (level, offset) on the
+// tensor cores (3xTF32 split with FP32 accumulation, mma.sync m16n8k8):
+//   G[:, targets] += K_o * W[:, sources]  (one CTA per 16-row x 64-target tile)
+// and P2P in FP32; the FP64 mode keeps every pass in FP64.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <functional>
+#include <map>
+#include <vector>
+
+#include "common.cuh"
+#include "handles.cuh"
+
+namespace abx {
+
+struct FmmPlan {
+  int D = 3, n = 3, ncheb = 27, nchild = 8;
+  int nnodes = 0;
+  int kind = 0;
+  double p0 = 0.0;
+  std::vector<int> mi;  // ncheb x D multi-indices
+  // device
+  DevBuf<double> W, G;            // nnodes x ncheb
+  DevBuf<double> Tc;              // nchild x ncheb x ncheb (child->parent interpolation)
+  DevBuf<double> box;             // nnodes x 6 (lo[3], hi[3])
+  DevBuf<int> leaf_ids;           // leaves (node ids)
+  DevBuf<int> node_begin, node_end;
+  // per level: nodes with children (M2M/L2L), (parent, child, octant) links
+  std::vector<int> max_level;
+  std::vector<std::vector<int>> level_links;  // host: flattened (parent, child, octant)
+  DevBuf<int> links;                          // all levels concatenated
+  std::vector<int> link_off, link_cnt;
+  // M2L: pairs (target, source, matrix id), grouped by level
+  DevBuf<int> m2l;
+  int n_m2l = 0;
+  DevBuf<double> Km;      // nmat x ncheb x ncheb
+  DevBuf<float> Km32;     // FP32 copy (mixed precision)
+  int nmat = 0;
+  // M2L grouped by matrix (for the tensor-core GEMM): per matrix a list of
+  // (target, source)
+  DevBuf<int2> m2l_by_mat;
+  std::vector<int> mat_off, mat_cnt;
+  DevBuf<int> mat_off_d;
+  // P2P: CSR over target leaves of source leaves
+  DevBuf<int> p2p_rowptr, p2p_src;
+  int nleaves = 0;
+  double build_s = 0.0;
+  double chebsetup_s = 0.0;
+  DevBuf<float> W32, G32;
+  DevBuf<int> mi_d;                 // ncheb x 3 multi-indices
+  DevBuf<int> tile_mat, tile_first; // tensor-core M2L tiles
+  int ntiles = 0;
+};
+
+void fmm_plan_free(FmmPlan *P) { delete P; }
+
+namespace {
+
+constexpr double PI = 3.14159265358979323846;
+
+// S_m(x), m = 0..n-1 (chebyshev_Sn: Clenshaw, src/detail/Chebyshev.h:135-153)
+__host__ __device__ inline void cheb_sn(double x, int n, double *S) {
+  const double invn = 1.0 / n;
+  for (int m = 0; m < n; ++m) {
+    double b1 = 0.0, b2 = 0.0;
+    for (int k = n - 1; k >= 1; --k) {
+      const double bk = 2 * invn * cos(k * (2.0 * m + 1.0) * (PI / 2) * invn) + 2.0 * x * b1 - b2;
+      b2 = b1;
+      b1 = bk;
+    }
+    S[m] = invn + x * b1 - b2;
+  }
+}
+
+__host__ __device__ inline double cheb_node(int m, int n) { return cos((2.0 * m + 1.0) * PI / (2.0 * n)); }
+
+__host__ __device__ inline double shift_coord(double p, double lo, double hi) {
+  const double span = hi - lo;
+  return span > 0.0 ? (2 * p - lo - hi) / span : 0.0;
+}
+
+template <int KIND> __device__ __forceinline__ double fmm_k64(double d2, double p0) {
+  if (KIND == ABX_K_GAUSSIAN || KIND == ABX_K_COMPACT_GAUSSIAN) return exp(-d2 * p0);
+  if (KIND == ABX_K_LAPLACE) return 1.0 / (sqrt(d2) + p0);
+  if (KIND == ABX_K_MULTIQUADRIC) return sqrt(d2 + p0);
+  if (KIND == ABX_K_CONST) return p0;
+  return 0.0;
+}
+
+template <int KIND> __device__ __forceinline__ float fmm_k32(float d2, float p0) {
+  if (KIND == ABX_K_GAUSSIAN || KIND == ABX_K_COMPACT_GAUSSIAN) return __expf(-d2 * p0);
+  if (KIND == ABX_K_LAPLACE) return __fdividef(1.0f, sqrtf(d2) + p0);
+  if (KIND == ABX_K_MULTIQUADRIC) return sqrtf(d2 + p0);
+  if (KIND == ABX_K_CONST) return p0;
+  return 0.0f;
+}
+
+// ---------------------------------------------------------------- P2M ---
+constexpr int FT = 128;
+constexpr int MAXN = 8;     // max Chebyshev order
+constexpr int MAXC = 512;   // max nodes (8^3)
+
+__global__ void __launch_bounds__(FT) k_p2m(int D, int n, int ncheb, const int *__restrict__ leaves,
+                                            const int *__restrict__ nb, const int *__restrict__ ne,
+                                            const double *__restrict__ box,
+                                            const double *__restrict__ pos, int64_t npos,
+                                            const double *__restrict__ b, const int *__restrict__ mi,
+                                            double *__restrict__ W) {
+  __shared__ double S[FT][MAXN * 3];
+  __shared__ double sb[FT];
+  const int leaf = leaves[blockIdx.x];
+  const double *bx = box + (size_t)leaf * 6;
+  double acc[MAXC / FT];
+  for (int q = 0; q < MAXC / FT; ++q) acc[q] = 0.0;
+  for (int i0 = nb[leaf]; i0 < ne[leaf]; i0 += FT) {
+    const int i = i0 + threadIdx.x;
+    if (i < ne[leaf]) {
+      for (int d = 0; d < D; ++d) {
+        const double x = shift_coord(pos[(int64_t)d * npos + i], bx[d], bx[3 + d]);
+        cheb_sn(x, n, &S[threadIdx.x][d * MAXN]);
+      }
+      sb[threadIdx.x] = b[i];
+    }
+    __syncthreads();
+    const int cnt = min(FT, ne[leaf] - i0);
+    for (int q = 0; q < MAXC / FT; ++q) {
+      const int j = threadIdx.x + q * FT;
+      if (j >= ncheb) break;
+      double a = 0.0;
+      for (int p = 0; p < cnt; ++p) {
+        double r = sb[p];
+        for (int d = 0; d < D; ++d) r *= S[p][d * MAXN + mi[j * 3 + d]];
+        a += r;
+      }
+      acc[q] += a;
+    }
+    __syncthreads();
+  }
+  for (int q = 0; q < MAXC / FT; ++q) {
+    const int j = threadIdx.x + q * FT;
+    if (j < ncheb) W[(size_t)leaf * ncheb + j] = acc[q];
+  }
+}
+
+// ------------------------------------------------------------ M2M / L2L ---
+// links: (parent, child, octant); one CTA per link group of one parent.
+// M2M: W[p][i] += sum_j Tc[o][i][j] W[c][j]   (atomic over children)
+__global__ void __launch_bounds__(FT) k_m2m(int ncheb, const int *__restrict__ links, int nlinks,
+                                            const double *__restrict__ Tc, double *__restrict__ W) {
+  const int l = blockIdx.x;
+  if (l >= nlinks) return;
+  const int p = links[3 * l], c = links[3 * l + 1], o = links[3 * l + 2];
+  __shared__ double wc[MAXC];
+  for (int j = threadIdx.x; j < ncheb; j += FT) wc[j] = W[(size_t)c * ncheb + j];
+  __syncthreads();
+  const double *T = Tc + (size_t)o * ncheb * ncheb;
+  for (int i = threadIdx.x; i < ncheb; i += FT) {
+    double a = 0.0;
+    for (int j = 0; j < ncheb; ++j) a += T[(size_t)i * ncheb + j] * wc[j];
+    atomicAdd(&W[(size_t)p * ncheb + i], a);
+  }
+}
+
+// L2L: G[c][i] += sum_j Tc[o][j][i] G[p][j]
+__global__ void __launch_bounds__(FT) k_l2l(int ncheb, const int *__restrict__ links, int nlinks,
+                                            const double *__restrict__ Tc, double *__restrict__ G) {
+  const int l = blockIdx.x;
+  if (l >= nlinks) return;
+  const int p = links[3 * l], c = links[3 * l + 1], o = links[3 * l + 2];
+  __shared__ double gp[MAXC];
+  for (int j = threadIdx.x; j < ncheb; j += FT) gp[j] = G[(size_t)p * ncheb + j];
+  __syncthreads();
+  const double *T = Tc + (size_t)o * ncheb * ncheb;
+  for (int i = threadIdx.x; i < ncheb; i += FT) {
+    double a = 0.0;
+    for (int j = 0; j < ncheb; ++j) a += T[(size_t)j * ncheb + i] * gp[j];
+    G[(size_t)c * ncheb + i] += a;
+  }
+}
+
+// --------------------------------------------------------------- M2L ---
+// FP64, one CTA per M2L pair: G[t] += K[m] W[s] (atomic: several sources per
+// target run concurrently).
+__global__ void __launch_bounds__(FT) k_m2l64(int ncheb, const int *__restrict__ pairs, int npairs,
+                                              const double *__restrict__ Km,
+                                              const double *__restrict__ W,
+                                              double *__restrict__ G) {
+  const int q = blockIdx.x;
+  if (q >= npairs) return;
+  const int t = pairs[3 * q], s = pairs[3 * q + 1], m = pairs[3 * q + 2];
+  __shared__ double ws[MAXC];
+  for (int j = threadIdx.x; j < ncheb; j += FT) ws[j] = W[(size_t)s * ncheb + j];
+  __syncthreads();
+  const double *K = Km + (size_t)m * ncheb * ncheb;
+  for (int i = threadIdx.x; i < ncheb; i += FT) {
+    double a = 0.0;
+    for (int j = 0; j < ncheb; ++j) a += K[(size_t)i * ncheb + j] * ws[j];
+    atomicAdd(&G[(size_t)t * ncheb + i], a);
+  }
+}
+
+// Mixed precision M2L on the tensor cores: for one matrix K (ncheb x ncheb,
+// FP32) and a tile of 64 (target, source) pairs sharing it:
+//   C[16 x 64] (rows i0..i0+15) = K[i0:i0+16, :] * W[:, sources]
+// as 3xTF32 (a = ah + al, b = bh + bl; ah*bh + ah*bl + al*bh) on
+// mma.sync.m16n8k8.tf32 with FP32 accumulation, then atomically added to G.
+__device__ __forceinline__ uint32_t f2tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void mma_tf32(float c[4], const uint32_t a[4], const uint32_t b[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+constexpr int TC_PAIRS = 64;  // pairs per CTA
+constexpr int TC_KP = 8;      // k step
+
+__global__ void __launch_bounds__(128) k_m2l_tc(int ncheb, int kpad, const float *__restrict__ Km32,
+                                                const int2 *__restrict__ pairs,
+                                                const int *__restrict__ mat_off,
+                                                const int *__restrict__ tile_mat,
+                                                const int *__restrict__ tile_first,
+                                                const float *__restrict__ W32,
+                                                float *__restrict__ G32) {
+  // one CTA = one (matrix, 64-pair tile); 4 warps each own 16 of the 64 pairs
+  // (n dimension) and loop over 16-row blocks of K
+  extern __shared__ float sm[];
+  float *sW = sm;  // [kpad][TC_PAIRS + 4]  gathered source expansions (hi part)
+  const int tile = blockIdx.x;
+  const int m = tile_mat[tile];
+  const int p0 = tile_first[tile];
+  const int pend = mat_off[m + 1];
+  const int np = min(TC_PAIRS, pend - p0);
+  const int ldw = TC_PAIRS + 4;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int e = tid; e < kpad * TC_PAIRS; e += 128) {
+    const int k = e / TC_PAIRS, q = e % TC_PAIRS;
+    float v = 0.f;
+    if (q < np && k < ncheb) v = W32[(size_t)pairs[p0 + q].y * ncheb + k];
+    sW[k * ldw + q] = v;
+  }
+  __syncthreads();
+  const float *K = Km32 + (size_t)m * ncheb * ncheb;
+  const int g = lane >> 2, t4 = lane & 3;
+  const int nbase = warp * 16;  // 16 pairs per warp = 2 n-tiles of 8
+  for (int i0 = 0; i0 < ncheb; i0 += 16) {
+    float c[2][4] = {};
+    for (int k0 = 0; k0 < kpad; k0 += TC_KP) {
+      // A fragment (16x8 row-major): rows i0+g, i0+g+8; cols k0+t4, k0+t4+4
+      float af[4];
+      const int r0 = i0 + g, r1 = i0 + g + 8, ca = k0 + t4, cb = k0 + t4 + 4;
+      af[0] = (r0 < ncheb && ca < ncheb) ? K[(size_t)r0 * ncheb + ca] : 0.f;
+      af[1] = (r1 < ncheb && ca < ncheb) ? K[(size_t)r1 * ncheb + ca] : 0.f;
+      af[2] = (r0 < ncheb && cb < ncheb) ? K[(size_t)r0 * ncheb + cb] : 0.f;
+      af[3] = (r1 < ncheb && cb < ncheb) ? K[(size_t)r1 * ncheb + cb] : 0.f;
+      uint32_t ah[4], al[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        ah[q] = f2tf32(af[q]);
+        al[q] = f2tf32(af[q] - __uint_as_float(ah[q]));
+      }
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt) {
+        // B fragment (8x8 col): rows k0+t4, k0+t4+4; col n = nbase + nt*8 + g
+        const int col = nbase + nt * 8 + g;
+        const float b0 = sW[(k0 + t4) * ldw + col], b1 = sW[(k0 + t4 + 4) * ldw + col];
+        uint32_t bh[2] = {f2tf32(b0), f2tf32(b1)};
+        uint32_t bl[2] = {f2tf32(b0 - __uint_as_float(bh[0])), f2tf32(b1 - __uint_as_float(bh[1]))};
+        mma_tf32(c[nt], al, bh);
+        mma_tf32(c[nt], ah, bl);
+        mma_tf32(c[nt], ah, bh);
+      }
+    }
+    // C fragment: rows i0+g (c0,c1), i0+g+8 (c2,c3); cols 2*t4, 2*t4+1
+#pragma unroll
+    for (int nt = 0; nt < 2; ++nt) {
+      const int cbase = nbase + nt * 8 + 2 * t4;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int q = cbase + h;
+        if (q >= np) continue;
+        const int tgt = pairs[p0 + q].x;
+        const int ra = i0 + g, rb = i0 + g + 8;
+        if (ra < ncheb) atomicAdd(&G32[(size_t)tgt * ncheb + ra], c[nt][h]);
+        if (rb < ncheb) atomicAdd(&G32[(size_t)tgt * ncheb + rb], c[nt][2 + h]);
+      }
+    }
+  }
+}
+
+__global__ void k_f64_to_f32(const double *__restrict__ a, int64_t n, float *__restrict__ b) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+__global__ void k_add_f32_to_f64(const float *__restrict__ a, int64_t n, double *__restrict__ b) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] += (double)a[i];
+}
+
+// ----------------------------------------------------------- L2P + P2P ---
+template <int KIND, bool MIXED>
+__global__ void __launch_bounds__(FT) k_l2p_p2p(int D, int n, int ncheb, const int *__restrict__ leaves,
+                                                const int *__restrict__ nb,
+                                                const int *__restrict__ ne,
+                                                const double *__restrict__ box,
+                                                const double *__restrict__ pos, int64_t npos,
+                                                const double *__restrict__ b,
+                                                const int *__restrict__ mi,
+                                                const double *__restrict__ G,
+                                                const int *__restrict__ rp,
+                                                const int *__restrict__ src, double p0,
+                                                double *__restrict__ c) {
+  __shared__ double sg[MAXC];
+  __shared__ double sx[FT], sy[FT], sz[FT], sbv[FT];
+  __shared__ int sid[FT];
+  const int li = blockIdx.x;
+  const int leaf = leaves[li];
+  const double *bx = box + (size_t)leaf * 6;
+  for (int j = threadIdx.x; j < ncheb; j += FT) sg[j] = G[(size_t)leaf * ncheb + j];
+  __syncthreads();
+  for (int i0 = nb[leaf]; i0 < ne[leaf]; i0 += FT) {
+    const int i = i0 + threadIdx.x;
+    const bool act = i < ne[leaf];
+    double xi[3] = {0, 0, 0};
+    double acc = 0.0;
+    if (act) {
+      for (int d = 0; d < D; ++d) xi[d] = pos[(int64_t)d * npos + i];
+      double S[3][MAXN];
+      for (int d = 0; d < D; ++d) cheb_sn(shift_coord(xi[d], bx[d], bx[3 + d]), n, S[d]);
+      for (int j = 0; j < ncheb; ++j) {
+        double r = sg[j];
+        for (int d = 0; d < D; ++d) r *= S[d][mi[j * 3 + d]];
+        acc += r;
+      }
+    }
+    // P2P over the connected source leaves
+    for (int e = rp[li]; e < rp[li + 1]; ++e) {
+      const int sl = src[e];
+      for (int j0 = nb[sl]; j0 < ne[sl]; j0 += FT) {
+        __syncthreads();
+        const int j = j0 + threadIdx.x;
+        if (j < ne[sl]) {
+          sx[threadIdx.x] = pos[j];
+          sy[threadIdx.x] = D > 1 ? pos[npos + j] : 0.0;
+          sz[threadIdx.x] = D > 2 ? pos[2 * npos + j] : 0.0;
+          sbv[threadIdx.x] = b[j];
+          sid[threadIdx.x] = j;
+        }
+        __syncthreads();
+        const int cnt = min(FT, ne[sl] - j0);
+        if (act) {
+          if (MIXED) {
+            // FP32 pair terms summed per staged chunk, chunks summed in FP64;
+            // the self pair (a regularised singular kernel can be huge there)
+            // is evaluated in FP64.
+            float a = 0.f;
+            for (int q = 0; q < cnt; ++q) {
+              if (sid[q] == i) {
+                acc += fmm_k64<KIND>(0.0, p0) * sbv[q];
+                continue;
+              }
+              const float dx = (float)(sx[q] - xi[0]), dy = (float)(sy[q] - xi[1]),
+                          dz = (float)(sz[q] - xi[2]);
+              const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+              a = fmaf(fmm_k32<KIND>(d2, (float)p0), (float)sbv[q], a);
+            }
+            acc += (double)a;
+          } else {
+            for (int q = 0; q < cnt; ++q) {
+              const double dx = sx[q] - xi[0], dy = sy[q] - xi[1], dz = sz[q] - xi[2];
+              const double d2 = dx * dx + dy * dy + dz * dz;
+              acc += fmm_k64<KIND>(d2, p0) * sbv[q];
+            }
+          }
+        }
+      }
+    }
+    if (act) c[i] = acc;
+  }
+}
+
+// M2L matrices: for each (level box size, offset) K[i][j] = kernel(x_i^t, x_j^s)
+template <int KIND>
+__global__ void k_m2l_mats(int D, int n, int ncheb, const double *__restrict__ mat_desc,
+                           const int *__restrict__ mi, double p0, double *__restrict__ Km) {
+  // mat_desc per matrix: box size[3], offset[3] (source box lo - target box lo)
+  const int m = blockIdx.y;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (int64_t)ncheb * ncheb) return;
+  const int i = (int)(e / ncheb), j = (int)(e % ncheb);
+  const double *md = mat_desc + (size_t)m * 6;
+  double d2 = 0.0;
+  for (int d = 0; d < D; ++d) {
+    const double h = md[d];
+    const double pi = 0.5 * (cheb_node(mi[i * 3 + d], n) + 1) * h;
+    const double pj = 0.5 * (cheb_node(mi[j * 3 + d], n) + 1) * h + md[3 + d];
+    const double dx = pj - pi;
+    d2 += dx * dx;
+  }
+  Km[(size_t)m * ncheb * ncheb + e] = fmm_k64<KIND>(d2, p0);
+}
+
+}  // namespace
+
+// ----------------------------------------------------------- plan build ---
+int fmm_plan_build(abx_operator *op, int order, FmmPlan *&out) {
+  abx_particles *p = op->rows;
+  abx_context *ctx = p->ctx;
+  cudaStream_t s = ctx->stream;
+  ABX_REQUIRE(p->searchable && p->search_kind == 1, ABX_ERR_STATE,
+              "the FMM needs an octree: call abx_particles_init_octree first");
+  ABX_REQUIRE(order >= 2 && order <= MAXN, ABX_ERR_INVALID, "Chebyshev order must be in 2..%d", MAXN);
+  const auto t0 = std::chrono::steady_clock::now();
+  const OctTree &T = p->tree;
+  FmmPlan *P = new FmmPlan();
+  const int D = p->dim;
+  P->D = D;
+  P->n = order;
+  P->nchild = 1 << D;
+  P->ncheb = 1;
+  for (int d = 0; d < D; ++d) P->ncheb *= order;
+  P->kind = op->k.kind;
+  P->p0 = op->k.p[0];
+  const int nc = P->ncheb;
+  P->mi.assign((size_t)nc * 3, 0);
+  for (int j = 0; j < nc; ++j) {
+    int r = j;
+    for (int d = D - 1; d >= 0; --d) {
+      P->mi[j * 3 + d] = r % order;
+      r /= order;
+    }
+  }
+  const int NN = (int)T.tag.size();
+  P->nnodes = NN;
+  std::vector<double> boxes((size_t)NN * 6, 0.0);
+  for (int nd = 0; nd < NN; ++nd) {
+    double lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
+    T.box(p->grid, nd, lo, hi);
+    for (int d = 0; d < 3; ++d) {
+      boxes[nd * 6 + d] = d < D ? lo[d] : 0.0;
+      boxes[nd * 6 + 3 + d] = d < D ? hi[d] : 1.0;
+    }
+  }
+  // ---- traversal (host): M2L pairs and P2P connectivity
+  auto near = [&](int t, int sdx) {
+    double maxd = std::numeric_limits<double>::min();
+    for (int d = 0; d < D; ++d) maxd = std::max(maxd, boxes[t * 6 + 3 + d] - boxes[t * 6 + d]);
+    double dist2 = 0.0;
+    for (int d = 0; d < D; ++d) {
+      double dd = 0.0;
+      const double tlo = boxes[t * 6 + d], thi = boxes[t * 6 + 3 + d];
+      const double slo = boxes[sdx * 6 + d], shi = boxes[sdx * 6 + 3 + d];
+      if (thi < slo) dd = slo - thi;
+      else if (shi < tlo) dd = tlo - shi;
+      maxd = std::max(maxd, shi - slo);
+      dist2 += dd * dd;
+    }
+    return maxd * maxd > dist2;
+  };
+  std::vector<std::array<int, 2>> m2l;
+  std::vector<std::vector<int>> p2p_of(NN);
+  std::vector<std::array<int, 3>> links;  // parent, child, octant
+  std::function<void(int, std::vector<int> &)> leaves_of = [&](int nd, std::vector<int> &o) {
+    if (T.kind[nd] == 1) { o.push_back(nd); return; }
+    if (T.kind[nd] == 0) return;
+    for (int c = 0; c < P->nchild; ++c) leaves_of(T.first_child[nd] + c, o);
+  };
+  std::function<void(int, const std::vector<int> &, int)> down = [&](int t, const std::vector<int> &cp,
+                                                                    int parent) {
+    std::vector<int> conn;
+    if (parent < 0) {
+      for (int c = 0; c < P->nchild; ++c) {
+        const int sdx = T.first_child[0] + c;
+        if (T.kind[sdx] == 0) continue;
+        if (near(t, sdx)) conn.push_back(sdx); else m2l.push_back({t, sdx});
+      }
+    } else {
+      for (int sdx : cp) {
+        if (T.kind[sdx] == 1) { conn.push_back(sdx); continue; }
+        for (int c = 0; c < P->nchild; ++c) {
+          const int ch = T.first_child[sdx] + c;
+          if (T.kind[ch] == 0) continue;
+          if (near(t, ch)) conn.push_back(ch); else m2l.push_back({t, ch});
+        }
+      }
+    }
+    if (T.kind[t] == 2) {
+      for (int c = 0; c < P->nchild; ++c) {
+        const int ch = T.first_child[t] + c;
+        if (T.kind[ch] == 0) continue;
+        links.push_back({t, ch, c});
+        down(ch, conn, t);
+      }
+    } else {
+      for (int sdx : conn) leaves_of(sdx, p2p_of[t]);
+    }
+  };
+  std::vector<int> none;
+  if (NN > 1)
+    for (int c = 0; c < P->nchild; ++c) {
+      const int t = T.first_child[0] + c;
+      if (T.kind[t] != 0) down(t, none, -1);
+    }
+  // ---- links by level (M2M bottom-up uses deepest first)
+  int maxlev = 0;
+  for (auto &l : links) maxlev = std::max(maxlev, T.level[l[1]]);
+  std::vector<int> flat;
+  P->link_off.assign(maxlev + 2, 0);
+  P->link_cnt.assign(maxlev + 2, 0);
+  for (int lev = 1; lev <= maxlev; ++lev) {
+    P->link_off[lev] = (int)(flat.size() / 3);
+    for (auto &l : links)
+      if (T.level[l[1]] == lev) {
+        flat.push_back(l[0]);
+        flat.push_back(l[1]);
+        flat.push_back(l[2]);
+      }
+    P->link_cnt[lev] = (int)(flat.size() / 3) - P->link_off[lev];
+  }
+  // ---- M2L matrices keyed by (level, offset)
+  std::map<std::array<long long, 4>, int> matid;
+  std::vector<double> mdesc;
+  std::vector<int> trip;
+  for (auto &pr : m2l) {
+    const int t = pr[0], sdx = pr[1];
+    std::array<long long, 4> key{T.level[t], 0, 0, 0};
+    double hbox[3] = {1, 1, 1}, off[3] = {0, 0, 0};
+    for (int d = 0; d < D; ++d) {
+      hbox[d] = boxes[t * 6 + 3 + d] - boxes[t * 6 + d];
+      off[d] = boxes[sdx * 6 + d] - boxes[t * 6 + d];
+      key[1 + d] = std::llround(off[d] / hbox[d]);
+    }
+    auto it = matid.find(key);
+    int id;
+    if (it == matid.end()) {
+      id = (int)matid.size();
+      matid[key] = id;
+      for (int d = 0; d < 3; ++d) mdesc.push_back(hbox[d]);
+      for (int d = 0; d < 3; ++d) mdesc.push_back(d < D ? key[1 + d] * hbox[d] : 0.0);
+    } else {
+      id = it->second;
+    }
+    trip.push_back(t);
+    trip.push_back(sdx);
+    trip.push_back(id);
+  }
+  P->nmat = (int)matid.size();
+  P->n_m2l = (int)m2l.size();
+  // grouped by matrix for the tensor-core path
+  std::vector<std::vector<int2>> bym(P->nmat);
+  for (size_t q = 0; q < m2l.size(); ++q) bym[trip[3 * q + 2]].push_back(make_int2(trip[3 * q], trip[3 * q + 1]));
+  std::vector<int2> bymat;
+  P->mat_off.assign(P->nmat + 1, 0);
+  for (int m = 0; m < P->nmat; ++m) {
+    P->mat_off[m] = (int)bymat.size();
+    bymat.insert(bymat.end(), bym[m].begin(), bym[m].end());
+  }
+  P->mat_off[P->nmat] = (int)bymat.size();
+  // ---- P2P CSR over leaves
+  std::vector<int> leaves = T.leaves;
+  std::vector<int> rp(1, 0), srcs;
+  for (int lf : leaves) {
+    for (int sl : p2p_of[lf]) srcs.push_back(sl);
+    rp.push_back((int)srcs.size());
+  }
+  P->nleaves = (int)leaves.size();
+  // ---- child interpolation matrices Tc[o][i][j] = R_i(node j of child o; parent box)
+  std::vector<double> Tc((size_t)P->nchild * nc * nc);
+  for (int o = 0; o < P->nchild; ++o)
+    for (int j = 0; j < nc; ++j) {
+      double S[3][MAXN];
+      for (int d = 0; d < D; ++d) {
+        const int bit = (o >> (D - 1 - d)) & 1;  // child box in the unit parent box [-1,1]
+        const double clo = bit ? 0.0 : -1.0, chi = bit ? 1.0 : 0.0;
+        const double x = 0.5 * (cheb_node(P->mi[j * 3 + d], order) + 1) * (chi - clo) + clo;
+        cheb_sn(x, order, S[d]);
+      }
+      for (int i = 0; i < nc; ++i) {
+        double r = 1.0;
+        for (int d = 0; d < D; ++d) r *= S[d][P->mi[i * 3 + d]];
+        Tc[((size_t)o * nc + i) * nc + j] = r;
+      }
+    }
+  // ---- device upload
+  int st;
+  auto fail = [&](int e) {
+    delete P;
+    return e;
+  };
+  std::vector<int> nb(NN), ne(NN);
+  for (int nd = 0; nd < NN; ++nd) {
+    nb[nd] = T.begin[nd];
+    ne[nd] = T.end[nd];
+  }
+  if ((st = P->W.reserve((size_t)NN * nc)) || (st = P->G.reserve((size_t)NN * nc)) ||
+      (st = P->Tc.reserve(Tc.size())) || (st = P->box.reserve(boxes.size())) ||
+      (st = P->leaf_ids.reserve(leaves.size() + 1)) || (st = P->node_begin.reserve(NN)) ||
+      (st = P->node_end.reserve(NN)) || (st = P->links.reserve(flat.size() + 1)) ||
+      (st = P->m2l.reserve(trip.size() + 1)) ||
+      (st = P->Km.reserve((size_t)std::max(1, P->nmat) * nc * nc)) ||
+      (st = P->p2p_rowptr.reserve(rp.size())) || (st = P->p2p_src.reserve(srcs.size() + 1)) ||
+      (st = P->m2l_by_mat.reserve(bymat.size() + 1)) || (st = P->mat_off_d.reserve(P->nmat + 1)))
+    return fail(st);
+  DevBuf<double> md_d;
+  if ((st = P->mi_d.reserve(P->mi.size())) || (st = md_d.reserve(mdesc.size() + 1))) return fail(st);
+  // tensor-core M2L tiles: 64 pairs of one matrix each
+  std::vector<int> tmat, tfirst;
+  for (int m = 0; m < P->nmat; ++m)
+    for (int q = P->mat_off[m]; q < P->mat_off[m + 1]; q += TC_PAIRS) {
+      tmat.push_back(m);
+      tfirst.push_back(q);
+    }
+  P->ntiles = (int)tmat.size();
+  if ((st = P->tile_mat.reserve(tmat.size() + 1)) || (st = P->tile_first.reserve(tfirst.size() + 1)))
+    return fail(st);
+  auto up = [&](void *dst, const void *src, size_t bytes) {
+    if (bytes) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+  };
+  up(P->Tc.ptr, Tc.data(), Tc.size() * 8);
+  up(P->box.ptr, boxes.data(), boxes.size() * 8);
+  up(P->leaf_ids.ptr, leaves.data(), leaves.size() * 4);
+  up(P->node_begin.ptr, nb.data(), nb.size() * 4);
+  up(P->node_end.ptr, ne.data(), ne.size() * 4);
+  up(P->links.ptr, flat.data(), flat.size() * 4);
+  up(P->m2l.ptr, trip.data(), trip.size() * 4);
+  up(P->p2p_rowptr.ptr, rp.data(), rp.size() * 4);
+  up(P->p2p_src.ptr, srcs.data(), srcs.size() * 4);
+  up(P->m2l_by_mat.ptr, bymat.data(), bymat.size() * sizeof(int2));
+  up(P->mat_off_d.ptr, P->mat_off.data(), P->mat_off.size() * 4);
+  up(P->mi_d.ptr, P->mi.data(), P->mi.size() * 4);
+  up(P->tile_mat.ptr, tmat.data(), tmat.size() * 4);
+  up(P->tile_first.ptr, tfirst.data(), tfirst.size() * 4);
+  up(md_d.ptr, mdesc.data(), mdesc.size() * 8);
+  if (P->nmat > 0) {
+    dim3 grid(ceil_div((size_t)nc * nc, 256), P->nmat);
+    switch (P->kind) {
+    case ABX_K_LAPLACE: k_m2l_mats<ABX_K_LAPLACE><<<grid, 256, 0, s>>>(D, order, nc, md_d.ptr, P->mi_d.ptr, P->p0, P->Km.ptr); break;
+    case ABX_K_GAUSSIAN: k_m2l_mats<ABX_K_GAUSSIAN><<<grid, 256, 0, s>>>(D, order, nc, md_d.ptr, P->mi_d.ptr, P->p0, P->Km.ptr); break;
+    case ABX_K_COMPACT_GAUSSIAN: k_m2l_mats<ABX_K_COMPACT_GAUSSIAN><<<grid, 256, 0, s>>>(D, order, nc, md_d.ptr, P->mi_d.ptr, P->p0, P->Km.ptr); break;
+    case ABX_K_MULTIQUADRIC: k_m2l_mats<ABX_K_MULTIQUADRIC><<<grid, 256, 0, s>>>(D, order, nc, md_d.ptr, P->mi_d.ptr, P->p0, P->Km.ptr); break;
+    case ABX_K_CONST: k_m2l_mats<ABX_K_CONST><<<grid, 256, 0, s>>>(D, order, nc, md_d.ptr, P->mi_d.ptr, P->p0, P->Km.ptr); break;
+    default:
+      set_error("FMM: kernel kind %d not supported", P->kind);
+      return fail(ABX_ERR_INVALID);
+    }
+  }
+  if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+    set_error("FMM plan upload failed");
+    return fail(ABX_ERR_CUDA);
+  }
+  P->max_level.assign(1, maxlev);
+  P->build_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  out = P;
+  return ABX_OK;
+}
+
+namespace {
+template <int KIND>
+int launch_l2p_p2p(FmmPlan *P, cudaStream_t s, const double *pos, int64_t npos, const double *b,
+                   double *c, bool mixed) {
+  if (mixed)
+    k_l2p_p2p<KIND, true><<<P->nleaves, FT, 0, s>>>(
+        P->D, P->n, P->ncheb, P->leaf_ids.ptr, P->node_begin.ptr, P->node_end.ptr, P->box.ptr, pos,
+        npos, b, P->mi_d.ptr, P->G.ptr, P->p2p_rowptr.ptr, P->p2p_src.ptr, P->p0, c);
+  else
+    k_l2p_p2p<KIND, false><<<P->nleaves, FT, 0, s>>>(
+        P->D, P->n, P->ncheb, P->leaf_ids.ptr, P->node_begin.ptr, P->node_end.ptr, P->box.ptr, pos,
+        npos, b, P->mi_d.ptr, P->G.ptr, P->p2p_rowptr.ptr, P->p2p_src.ptr, P->p0, c);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  return ABX_OK;
+}
+}  // namespace
+
+// c = K b through the five FMM passes (storage order of the octree set).
+int fmm_matvec_device(abx_operator *op, const double *b, double *c) {
+  FmmPlan *P = op->fmm;
+  abx_particles *p = op->rows;
+  cudaStream_t s = p->ctx->stream;
+  const int nc = P->ncheb;
+  const int64_t npos = p->n;
+  if (npos == 0) return ABX_OK;
+  const bool mixed = op->precision == ABX_PREC_MIXED;
+  ABX_CHECK_CUDA(cudaMemsetAsync(P->W.ptr, 0, (size_t)P->nnodes * nc * 8, s));
+  ABX_CHECK_CUDA(cudaMemsetAsync(P->G.ptr, 0, (size_t)P->nnodes * nc * 8, s));
+  if (P->nleaves > 0)
+    k_p2m<<<P->nleaves, FT, 0, s>>>(P->D, P->n, nc, P->leaf_ids.ptr, P->node_begin.ptr,
+                                    P->node_end.ptr, P->box.ptr, p->pos.ptr, npos, b, P->mi_d.ptr,
+                                    P->W.ptr);
+  const int maxlev = P->max_level.empty() ? 0 : P->max_level[0];
+  for (int lev = maxlev; lev >= 1; --lev)
+    if (P->link_cnt[lev] > 0)
+      k_m2m<<<P->link_cnt[lev], FT, 0, s>>>(nc, P->links.ptr + 3 * P->link_off[lev],
+                                           P->link_cnt[lev], P->Tc.ptr, P->W.ptr);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  if (P->n_m2l > 0) {
+    if (mixed) {
+      const size_t tot = (size_t)P->nnodes * nc;
+      ABX_TRY(P->W32.reserve(tot));
+      ABX_TRY(P->G32.reserve(tot));
+      if (!P->Km32.ptr) {
+        ABX_TRY(P->Km32.reserve((size_t)P->nmat * nc * nc));
+        k_f64_to_f32<<<ceil_div((size_t)P->nmat * nc * nc, 256), 256, 0, s>>>(
+            P->Km.ptr, (size_t)P->nmat * nc * nc, P->Km32.ptr);
+      }
+      k_f64_to_f32<<<ceil_div(tot, 256), 256, 0, s>>>(P->W.ptr, tot, P->W32.ptr);
+      ABX_CHECK_CUDA(cudaMemsetAsync(P->G32.ptr, 0, tot * 4, s));
+      const int kpad = (nc + TC_KP - 1) / TC_KP * TC_KP;
+      const size_t smem = (size_t)kpad * (TC_PAIRS + 4) * sizeof(float);
+      ABX_CHECK_CUDA(cudaFuncSetAttribute(k_m2l_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
+      k_m2l_tc<<<P->ntiles, 128, smem, s>>>(nc, kpad, P->Km32.ptr, P->m2l_by_mat.ptr,
+                                             P->mat_off_d.ptr, P->tile_mat.ptr, P->tile_first.ptr,
+                                             P->W32.ptr, P->G32.ptr);
+      k_add_f32_to_f64<<<ceil_div(tot, 256), 256, 0, s>>>(P->G32.ptr, tot, P->G.ptr);
+    } else {
+      k_m2l64<<<P->n_m2l, FT, 0, s>>>(nc, P->m2l.ptr, P->n_m2l, P->Km.ptr, P->W.ptr, P->G.ptr);
+    }
+    ABX_CHECK_CUDA(cudaGetLastError());
+  }
+  for (int lev = 1; lev <= maxlev; ++lev)
+    if (P->link_cnt[lev] > 0)
+      k_l2l<<<P->link_cnt[lev], FT, 0, s>>>(nc, P->links.ptr + 3 * P->link_off[lev],
+                                           P->link_cnt[lev], P->Tc.ptr, P->G.ptr);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  if (P->nleaves == 0) return ABX_OK;
+  switch (P->kind) {
+  case ABX_K_LAPLACE: return launch_l2p_p2p<ABX_K_LAPLACE>(P, s, p->pos.ptr, npos, b, c, mixed);
+  case ABX_K_GAUSSIAN: return launch_l2p_p2p<ABX_K_GAUSSIAN>(P, s, p->pos.ptr, npos, b, c, mixed);
+  case ABX_K_COMPACT_GAUSSIAN:
+    return launch_l2p_p2p<ABX_K_COMPACT_GAUSSIAN>(P, s, p->pos.ptr, npos, b, c, mixed);
+  case ABX_K_MULTIQUADRIC:
+    return launch_l2p_p2p<ABX_K_MULTIQUADRIC>(P, s, p->pos.ptr, npos, b, c, mixed);
+  case ABX_K_CONST: return launch_l2p_p2p<ABX_K_CONST>(P, s, p->pos.ptr, npos, b, c, mixed);
+  }
+  set_error("FMM: unsupported kernel");
+  return ABX_ERR_INVALID;
+}
+
+}  // namespace abx
+
+using namespace abx;
+
+extern "C" int abx_create_fmm_operator(abx_particles *p, const abx_kernel *k, int order,
+                                       abx_operator **out) {
+  ABX_REQUIRE(p && k && out, ABX_ERR_INVALID, "null argument");
+  ABX_REQUIRE(k->kind == ABX_K_LAPLACE || k->kind == ABX_K_GAUSSIAN ||
+                  k->kind == ABX_K_COMPACT_GAUSSIAN || k->kind == ABX_K_MULTIQUADRIC ||
+                  k->kind == ABX_K_CONST,
+              ABX_ERR_INVALID, "FMM: kernel kind %d not supported", k->kind);
+  ABX_TRY(ctx_activate(p->ctx));
+  abx_operator *op = new abx_operator();
+  op->kind = 2;
+  op->rows = p;
+  op->cols = p;
+  op->k = *k;
+  FmmPlan *P = nullptr;
+  const int st = fmm_plan_build(op, order, P);
+  if (st != ABX_OK) {
+    delete op;
+    return st;
+  }
+  op->fmm = P;
+  particles_retain(p);
+  particles_retain(p);
+  *out = op;
+  return ABX_OK;
+}
+
+extern "C" int abx_fmm_stats(abx_operator *op, int64_t *m2l_pairs, int64_t *matrices,
+                             int64_t *leaves, double *plan_seconds) {
+  ABX_REQUIRE(op && op->kind == 2 && op->fmm, ABX_ERR_INVALID, "not an FMM operator");
+  if (m2l_pairs) *m2l_pairs = op->fmm->n_m2l;
+  if (matrices) *matrices = op->fmm->nmat;
+  if (leaves) *leaves = op->fmm->nleaves;
+  if (plan_seconds) *plan_seconds = op->fmm->build_s;
+  return ABX_OK;
+}

@@ -70,17 +70,18 @@ struct abx_particles {
 
 namespace abx {
 struct PairLayout;   // pairs.cu
-struct DenseLayout;  // dense.cu
+struct FmmPlan;      // fmm.cu
 }  // namespace abx
 
 struct abx_operator {
-  int kind = 0;  // 0 sparse, 1 dense
+  int kind = 0;  // 0 sparse, 1 dense, 2 black-box FMM
   abx_particles *rows = nullptr, *cols = nullptr;
   uint64_t rows_version = 0, cols_version = 0;
   double radius = 0.0;
   abx_kernel k{};
   int precision = ABX_PREC_FP64;
   abx::PairLayout *pairs = nullptr;
+  abx::FmmPlan *fmm = nullptr;
   abx::HostStage stage_b, stage_c;
   int64_t last_candidates = 0, last_pairs = 0;
 };
@@ -109,6 +110,9 @@ int particles_grid_desc(const abx_particles *p, GridDesc *g);
 int pair_layout_build(abx_operator *op);
 void pair_layout_free(PairLayout *L);
 int sparse_matvec_device(abx_operator *op, const double *b, double *c);
-// dense.cu
+// operators.cu
 int dense_matvec_device(abx_operator *op, const double *b, double *c);
+// fmm.cu
+int fmm_matvec_device(abx_operator *op, const double *b, double *c);
+void fmm_plan_free(FmmPlan *P);
 }  // namespace abx

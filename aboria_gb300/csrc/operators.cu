@@ -248,6 +248,7 @@ int abx_operator_destroy(abx_operator *op) {
   cudaSetDevice(rows->ctx->device);
   cudaStreamSynchronize(rows->ctx->stream);
   if (op->pairs) pair_layout_free(op->pairs);
+  if (op->fmm) fmm_plan_free(op->fmm);
   delete op;
   particles_release(rows);
   particles_release(cols);
@@ -280,8 +281,10 @@ int abx_operator_matvec(abx_operator *op, const double *b, double *c) {
   ABX_TRY(op->stage_c.out(ctx, c, (size_t)nr * sizeof(double), &cd));
   if (op->kind == 0)
     ABX_TRY(sparse_matvec_device(op, (const double *)bd, (double *)cd));
-  else
+  else if (op->kind == 1)
     ABX_TRY(dense_matvec_device(op, (const double *)bd, (double *)cd));
+  else
+    ABX_TRY(fmm_matvec_device(op, (const double *)bd, (double *)cd));
   ABX_TRY(op->stage_c.finish(ctx, c, (size_t)nr * sizeof(double)));
   return ABX_OK;
 }

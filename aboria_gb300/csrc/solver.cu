@@ -573,7 +573,9 @@ int precond_apply_device(abx_precond *pc, const double *b, double *x) {
 }
 
 int sparse_or_dense_matvec(abx_operator *op, const double *b, double *c) {
-  return op->kind == 0 ? sparse_matvec_device(op, b, c) : dense_matvec_device(op, b, c);
+  if (op->kind == 0) return sparse_matvec_device(op, b, c);
+  if (op->kind == 1) return dense_matvec_device(op, b, c);
+  return fmm_matvec_device(op, b, c);
 }
 
 // ------------------------------------------------------------- FGMRES ---

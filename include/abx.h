@@ -151,6 +151,17 @@ ABX_API int abx_create_sparse_operator(abx_particles *rows, abx_particles *cols,
                                const abx_kernel *k, abx_operator **out);
 ABX_API int abx_create_dense_operator(abx_particles *rows, abx_particles *cols, const abx_kernel *k,
                               abx_operator **out);
+/* create_fmm_operator (src/Operators.h:401-407, KernelFMM src/Kernels.h:
+ * 533-576): black-box Chebyshev FMM with `order` nodes per dimension on the
+ * octree of p (abx_particles_init_octree; leaves of <= n_particles_in_leaf).
+ * Kernels: ABX_K_LAPLACE, _GAUSSIAN, _COMPACT_GAUSSIAN (no cut-off),
+ * _MULTIQUADRIC, _CONST.  ABX_PREC_FP64: every pass in FP64;
+ * ABX_PREC_MIXED: M2L as 3xTF32 tensor-core GEMMs with FP32 accumulation and
+ * P2P in FP32. */
+ABX_API int abx_create_fmm_operator(abx_particles *p, const abx_kernel *k, int order,
+                                    abx_operator **out);
+ABX_API int abx_fmm_stats(abx_operator *op, int64_t *m2l_pairs, int64_t *matrices,
+                          int64_t *leaves, double *plan_seconds);
 ABX_API int abx_operator_destroy(abx_operator *op);
 ABX_API int abx_operator_set_precision(abx_operator *op, int mode);
 ABX_API int64_t abx_operator_rows(const abx_operator *op);

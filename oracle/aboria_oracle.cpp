@@ -15,6 +15,7 @@
 // without FMA on x86-64, and aarch64 g++ would otherwise fuse a*b+c.
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -750,6 +751,283 @@ void orc_schwarz_apply(int D, int64_t n, const double *pos, const double *lo, co
     for (int i = 0; i < nd; ++i) y[i] = b[idx[i]];
     lu_solve(A, nd, piv, y.data());
     for (size_t i = 0; i < own; ++i) x[idx[i]] = y[i];
+  }
+}
+
+}  // extern "C"
+
+// -------------------------------------------------------------------- FMM --
+// Black-box Chebyshev FMM restated from the reference:
+//  * BlackBoxExpansions P2M/M2M/M2L/L2L/L2P (src/detail/FastMultipoleMethod.h:
+//    96-368), kernel evaluated at Chebyshev node pairs on every call (M2L);
+//  * chebyshev_node / chebyshev_Sn (Clenshaw) / ChebyshevRnSingle
+//    (src/detail/Chebyshev.h:84-153, 245-294); nodes enumerated in lattice
+//    order (last dimension fastest, src/LatticeIterator.h:269-281);
+//  * the dual-tree traversal of FastMultipoleMethod::matrix_vector_multiply
+//    (src/FastMultipoleMethod.h:111-548) with theta_condition
+//    (src/detail/FastMultipoleMethod.h:1249-1279): near iff
+//    max_diam^2 > dist^2;
+//  * calculate_P2P direct sums (:936-1101).
+// The tree is the HyperOctree of orc_octree_build (leaves of <= n_leaf).
+namespace {
+struct FNode {
+  int level, tag, begin, end, kind, first_child;
+  double lo[3], hi[3];
+};
+
+struct Fmm {
+  int D, n, ncheb, nchild;
+  std::vector<FNode> nodes;
+  std::vector<std::vector<double>> W, g;
+  std::vector<std::array<int, 3>> midx;  // multi-index of each Chebyshev node
+  const double *pos;                      // tag-sorted positions
+  KDesc k;
+  double K(const double *a, const double *b) const {
+    double dx[3];
+    for (int d = 0; d < D; ++d) dx[d] = b[d] - a[d];
+    return kernel_eval(k, dx, D, 0, 0);
+  }
+  double node_pos(int j, int d, const double *lo, const double *hi) const {
+    const double c = std::cos((2.0 * midx[j][d] + 1.0) * M_PI / (2.0 * n));
+    return 0.5 * (c + 1) * (hi[d] - lo[d]) + lo[d];
+  }
+  // S_m(x) for m = 0..n-1 per dimension, x in box coordinates
+  void sn(const double *p, const double *lo, const double *hi, std::vector<double> &S) const {
+    S.assign(n * D, 0.0);
+    for (int d = 0; d < D; ++d) {
+      const double span = hi[d] - lo[d];
+      const double x = span > 0.0 ? (2 * p[d] - lo[d] - hi[d]) / span : 0.0;
+      const double invn = 1.0 / n;
+      for (int m = 0; m < n; ++m) {
+        double b1 = 0.0, b2 = 0.0;
+        for (int kk = n - 1; kk >= 1; --kk) {
+          const double bk = 2 * invn * std::cos(kk * (2.0 * m + 1.0) * (M_PI / 2) * invn) +
+                            2.0 * x * b1 - b2;
+          b2 = b1;
+          b1 = bk;
+        }
+        S[m * D + d] = invn + x * b1 - b2;
+      }
+    }
+  }
+  double R(const std::vector<double> &S, int j) const {
+    double r = 1.0;
+    for (int d = 0; d < D; ++d) r *= S[midx[j][d] * D + d];
+    return r;
+  }
+  void upward(int nd, const double *b) {
+    FNode &N = nodes[nd];
+    std::vector<double> &Wn = W[nd];
+    Wn.assign(ncheb, 0.0);
+    std::vector<double> S;
+    if (N.kind == 1) {
+      for (int i = N.begin; i < N.end; ++i) {
+        sn(pos + (size_t)i * D, N.lo, N.hi, S);
+        for (int j = 0; j < ncheb; ++j) Wn[j] += R(S, j) * b[i];
+      }
+    } else {
+      for (int c = 0; c < nchild; ++c) {
+        const int ch = N.first_child + c;
+        if (nodes[ch].kind == 0) continue;
+        upward(ch, b);
+        const FNode &C = nodes[ch];
+        for (int j = 0; j < ncheb; ++j) {
+          double pj[3];
+          for (int d = 0; d < D; ++d) pj[d] = node_pos(j, d, C.lo, C.hi);
+          sn(pj, N.lo, N.hi, S);
+          for (int i = 0; i < ncheb; ++i) Wn[i] += R(S, i) * W[ch][j];
+        }
+      }
+    }
+  }
+  bool near(const FNode &t, const FNode &s) const {
+    double maxd = std::numeric_limits<double>::min();
+    for (int d = 0; d < D; ++d) maxd = std::max(maxd, t.hi[d] - t.lo[d]);
+    double dist2 = 0.0;
+    for (int d = 0; d < D; ++d) {
+      double dd = 0.0;
+      if (t.hi[d] < s.lo[d]) dd = s.lo[d] - t.hi[d];
+      else if (s.hi[d] < t.lo[d]) dd = t.lo[d] - s.hi[d];
+      if (s.hi[d] - s.lo[d] > maxd) maxd = s.hi[d] - s.lo[d];
+      dist2 += dd * dd;
+    }
+    return maxd * maxd > dist2;
+  }
+  void m2l(int t, int s) {
+    const FNode &T = nodes[t], &Sx = nodes[s];
+    for (int i = 0; i < ncheb; ++i) {
+      double pi[3];
+      for (int d = 0; d < D; ++d) pi[d] = node_pos(i, d, T.lo, T.hi);
+      double acc = 0.0;
+      for (int j = 0; j < ncheb; ++j) {
+        double pj[3];
+        for (int d = 0; d < D; ++d) pj[d] = node_pos(j, d, Sx.lo, Sx.hi);
+        acc += K(pi, pj) * W[s][j];
+      }
+      g[t][i] += acc;
+    }
+  }
+  void p2p(int t, int s, const double *b, double *c) const {
+    const FNode &T = nodes[t], &Sx = nodes[s];
+    for (int i = T.begin; i < T.end; ++i)
+      for (int j = Sx.begin; j < Sx.end; ++j) c[i] += K(pos + (size_t)i * D, pos + (size_t)j * D) * b[j];
+  }
+  void leaves_of(int nd, std::vector<int> &out) const {
+    if (nodes[nd].kind == 1) { out.push_back(nd); return; }
+    if (nodes[nd].kind == 0) return;
+    for (int c = 0; c < nchild; ++c) leaves_of(nodes[nd].first_child + c, out);
+  }
+  void downward(int t, const std::vector<int> &conn_parent, int parent, const double *b, double *c) {
+    const FNode &T = nodes[t];
+    g[t].assign(ncheb, 0.0);
+    std::vector<int> conn;
+    std::vector<double> S;
+    if (parent < 0) {
+      for (int cc = 0; cc < nchild; ++cc) {
+        const int s = nodes[0].first_child + cc;
+        if (nodes[s].kind == 0) continue;
+        if (near(T, nodes[s])) conn.push_back(s); else m2l(t, s);
+      }
+    } else {
+      const FNode &P = nodes[parent];
+      for (int i = 0; i < ncheb; ++i) {  // L2L from the parent
+        double pi[3];
+        for (int d = 0; d < D; ++d) pi[d] = node_pos(i, d, T.lo, T.hi);
+        sn(pi, P.lo, P.hi, S);
+        double acc = 0.0;
+        for (int j = 0; j < ncheb; ++j) acc += R(S, j) * g[parent][j];
+        g[t][i] += acc;
+      }
+      for (int s : conn_parent) {
+        if (nodes[s].kind == 1) { conn.push_back(s); continue; }
+        for (int cc = 0; cc < nchild; ++cc) {
+          const int ch = nodes[s].first_child + cc;
+          if (nodes[ch].kind == 0) continue;
+          if (near(T, nodes[ch])) conn.push_back(ch); else m2l(t, ch);
+        }
+      }
+    }
+    if (T.kind == 2) {
+      for (int cc = 0; cc < nchild; ++cc) {
+        const int ch = T.first_child + cc;
+        if (nodes[ch].kind == 0) continue;
+        downward(ch, conn, t, b, c);
+      }
+    } else {
+      for (int i = T.begin; i < T.end; ++i) {  // L2P
+        sn(pos + (size_t)i * D, T.lo, T.hi, S);
+        double acc = 0.0;
+        for (int j = 0; j < ncheb; ++j) acc += R(S, j) * g[t][j];
+        c[i] += acc;
+      }
+      for (int s : conn) {
+        std::vector<int> lv;
+        leaves_of(s, lv);
+        for (int l : lv) p2p(t, l, b, c);
+      }
+    }
+  }
+};
+}  // namespace
+
+extern "C" {
+
+// Black-box FMM matvec c = K b for positions pos (n*D, any order; output in
+// the same order), order n_cheb nodes per dimension, octree leaves <= n_leaf.
+void orc_fmm(int D, int n_cheb, int64_t npts, const double *pos_in, const double *lo,
+             const double *hi, double n_leaf, int kind, const double *params, const double *b_in,
+             double *c_out) {
+  Fmm F;
+  F.D = D;
+  F.n = n_cheb;
+  F.nchild = 1 << D;
+  F.ncheb = 1;
+  for (int d = 0; d < D; ++d) F.ncheb *= n_cheb;
+  F.midx.resize(F.ncheb);
+  for (int j = 0; j < F.ncheb; ++j) {  // last dimension fastest
+    int r = j;
+    std::array<int, 3> m{0, 0, 0};
+    for (int d = D - 1; d >= 0; --d) {
+      m[d] = r % n_cheb;
+      r /= n_cheb;
+    }
+    F.midx[j] = m;
+  }
+  F.k = KDesc{kind, {params[0], params[1], params[2], params[3]}, nullptr, nullptr};
+  const int max_level = 32 / D - 2;
+  std::vector<std::pair<int, int64_t>> kv(npts);
+  for (int64_t i = 0; i < npts; ++i) kv[i] = {point_to_tag(pos_in + i * D, lo, hi, D, max_level), i};
+  std::stable_sort(kv.begin(), kv.end(), [](const std::pair<int, int64_t> &a,
+                                            const std::pair<int, int64_t> &b) { return a.first < b.first; });
+  std::vector<double> pos(npts * D), b(npts), c(npts, 0.0);
+  std::vector<int> tags(npts);
+  for (int64_t i = 0; i < npts; ++i) {
+    tags[i] = kv[i].first;
+    for (int d = 0; d < D; ++d) pos[i * D + d] = pos_in[kv[i].second * D + d];
+    b[i] = b_in[kv[i].second];
+  }
+  F.pos = pos.data();
+  // nodes level by level (root = 0), as HyperOctree::build_tree
+  FNode root{0, 0, 0, (int)npts, 2, -1, {lo[0], lo[1], lo[2]}, {hi[0], hi[1], hi[2]}};
+  if (D < 3) for (int d = D; d < 3; ++d) { root.lo[d] = 0; root.hi[d] = 1; }
+  F.nodes.push_back(root);
+  std::vector<int> active(1, 0);
+  for (int level = 1; !active.empty(); ++level) {
+    const int shift = (max_level - level) * D;
+    const int length = (1 << shift) - 1;
+    std::vector<int> next;
+    for (int a : active) {
+      F.nodes[a].first_child = (int)F.nodes.size();
+      for (int ch = 0; ch < F.nchild; ++ch) {
+        const int mask = F.nodes[a].tag | (ch << shift);
+        const int lb = (int)(std::lower_bound(tags.begin(), tags.end(), mask) - tags.begin());
+        const int ub = (int)(std::upper_bound(tags.begin(), tags.end(), mask + length) - tags.begin());
+        FNode N{level, mask, lb, ub, 0, -1, {0, 0, 0}, {0, 0, 0}};
+        if (ub > lb) N.kind = (level == max_level || (ub - lb) <= n_leaf) ? 1 : 2;
+        for (int d = 0; d < 3; ++d) {
+          N.lo[d] = F.nodes[a].lo[d];
+          N.hi[d] = F.nodes[a].hi[d];
+        }
+        for (int d = 0; d < D; ++d) {
+          const int bit = (ch >> (D - 1 - d)) & 1;
+          const double mid = 0.5 * (N.lo[d] + N.hi[d]);
+          if (bit) N.lo[d] = mid; else N.hi[d] = mid;
+        }
+        F.nodes.push_back(N);
+        if (N.kind == 2) next.push_back((int)F.nodes.size() - 1);
+      }
+    }
+    active.swap(next);
+  }
+  F.W.resize(F.nodes.size());
+  F.g.resize(F.nodes.size());
+  // upward pass from the root's children, then the downward pass
+  for (int ch = 0; ch < F.nchild; ++ch) {
+    const int s = F.nodes[0].first_child + ch;
+    if (F.nodes[s].kind != 0) F.upward(s, b.data());
+  }
+  std::vector<int> none;
+  for (int ch = 0; ch < F.nchild; ++ch) {
+    const int t = F.nodes[0].first_child + ch;
+    if (F.nodes[t].kind != 0) F.downward(t, none, -1, b.data(), c.data());
+  }
+  for (int64_t i = 0; i < npts; ++i) c_out[kv[i].second] = c[i];
+}
+
+// Direct sum c_i = sum_j K(x_i, x_j) b_j for the targets listed in `targets`.
+void orc_direct_sum(int D, int64_t npts, const double *pos, int kind, const double *params,
+                    const double *b, int64_t ntargets, const int64_t *targets, double *c) {
+  KDesc k{kind, {params[0], params[1], params[2], params[3]}, nullptr, nullptr};
+#pragma omp parallel for schedule(static)
+  for (int64_t t = 0; t < ntargets; ++t) {
+    const int64_t i = targets[t];
+    double acc = 0.0;
+    for (int64_t j = 0; j < npts; ++j) {
+      double dx[3];
+      for (int d = 0; d < D; ++d) dx[d] = pos[j * D + d] - pos[i * D + d];
+      acc += kernel_eval(k, dx, D, 0, 0) * b[j];
+    }
+    c[t] = acc;
   }
 }
 

@@ -39,6 +39,7 @@ def lib():
         _lib.orc_octree_build.restype = C.c_int64
         _lib.orc_num_threads.restype = C.c_int
         for name in ("orc_radius_count", "orc_radius_lists", "orc_sparse_matvec", "orc_schwarz_apply",
+                     "orc_fmm", "orc_direct_sum",
                      "orc_dense_matvec", "orc_brute_counts", "orc_set_num_threads",
                      "orc_reassemble"):
             getattr(_lib, name).restype = None
@@ -267,3 +268,31 @@ def schwarz_apply(pos, lo, hi, periodic, tree: Octree, radius, kind, params, b):
                             _p(tree.leaf_tag), _p(tree.leaf_begin), _p(tree.leaf_end),
                             C.c_double(radius), C.c_int(kind), _p(prm), _p(b), _p(x))
     return x
+
+
+def fmm(pos, lo, hi, n_leaf, order, kind, params, b):
+    """Black-box Chebyshev FMM restatement; output in input order."""
+    pos = np.ascontiguousarray(pos, np.float64)
+    npts, dim = pos.shape
+    lo = np.ascontiguousarray(lo, np.float64)
+    hi = np.ascontiguousarray(hi, np.float64)
+    prm = np.zeros(4)
+    prm[:len(params)] = params
+    b = np.ascontiguousarray(b, np.float64)
+    c = np.zeros(npts)
+    lib().orc_fmm(C.c_int(dim), C.c_int(order), C.c_int64(npts), _p(pos), _p(lo), _p(hi),
+                  C.c_double(n_leaf), C.c_int(kind), _p(prm), _p(b), _p(c))
+    return c
+
+
+def direct_sum(pos, kind, params, b, targets):
+    pos = np.ascontiguousarray(pos, np.float64)
+    npts, dim = pos.shape
+    prm = np.zeros(4)
+    prm[:len(params)] = params
+    targets = np.ascontiguousarray(targets, np.int64)
+    c = np.zeros(len(targets))
+    lib().orc_direct_sum(C.c_int(dim), C.c_int64(npts), _p(pos), C.c_int(kind), _p(prm),
+                         _p(np.ascontiguousarray(b, np.float64)), C.c_int64(len(targets)),
+                         _p(targets), _p(c))
+    return c

@@ -148,3 +148,20 @@ def test_mlp_oracle_gradient_matches_finite_differences():
         lp, _ = mlp_oracle.loss_and_grad(p + e, dims, x, y, sc, sh)
         lm, _ = mlp_oracle.loss_and_grad(p - e, dims, x, y, sc, sh)
         assert abs((lp - lm) / 2e-6 - g[i]) < 1e-6 * max(1.0, abs(g[i]))
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_fmm_oracle_reference_kat(dim):
+    """tests/fmm.h:167-253: N=1000 uniform, n_leaf 10, kernel sqrt(|dx|^2 + 0.01),
+    source prod cos(2 pi x)/N; order 3 must give L2^2/scale < 1e-2."""
+    N = 1000
+    pos = workloads.uniform(N, dim, seed=110 + dim)
+    b = np.prod(np.cos(2 * np.pi * pos), axis=1) / N
+    direct = oracle.direct_sum(pos, 5, [0.01], b, np.arange(N))
+    scale = np.sum(direct ** 2)
+    for order in (3, 5):
+        c = oracle.fmm(pos, [0.0] * dim, [1.0] * dim, 10, order, 5, [0.01], b)
+        l2 = np.sum((c - direct) ** 2)
+        if order == 3:
+            assert l2 / scale < 1e-2
+    assert l2 / scale < 1e-6  # order 5 is far more accurate on this smooth kernel
