@@ -503,8 +503,58 @@ __device__ __forceinline__ int find_seg(const WarpSeg &ws, int nseg, int t) {
 
 struct WarpTile32 {
   float4 p[32];
+  // the same candidates as pairs for the packed FP32x2 loop:
+  // pp[2h] = (x_a, x_b, y_a, y_b), pp[2h+1] = (z_a, z_b, b_a, b_b), a = 2h, b = 2h+1
+  float4 pp[32];
   int2 meta[32];  // column kernel index, segment index
 };
+
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// Wendland C2 of two pairs with the cut-off folded into the clamp
+// t = max(1 - q, 0): exactly zero for q >= 1.
+__device__ __forceinline__ float2 kern32x2_wendland_clamped(float2 dd, const KParams &P) {
+  const float2 r = make_float2(sqrt_approx(dd.x), sqrt_approx(dd.y));
+  const float2 q = __fmul2_rn(r, make_float2(P.p0f, P.p0f));
+  float2 t = __ffma2_rn(q, make_float2(-1.f, -1.f), make_float2(1.f, 1.f));
+  t.x = fmaxf(t.x, 0.f);
+  t.y = fmaxf(t.y, 0.f);
+  const float2 t2 = __fmul2_rn(t, t);
+  const float2 t4 = __fmul2_rn(t2, t2);
+  const float2 pw = __ffma2_rn(q, make_float2(4.f, 4.f), make_float2(1.f, 1.f));
+  return __fmul2_rn(t4, pw);
+}
+
+// Kernel values of two pairs at once on the packed FP32x2 pipe.
+template <int KIND> __device__ __forceinline__ float2 kern32x2(float2 dd, const KParams &P) {
+  if (KIND == ABX_K_CONST) return make_float2(P.p0f, P.p0f);
+  if (KIND == ABX_K_GAUSSIAN || KIND == ABX_K_COMPACT_GAUSSIAN) {
+    const float2 e = __fmul2_rn(dd, make_float2(P.c_exp2, P.c_exp2));
+    return make_float2(exp2f(e.x), exp2f(e.y));
+  }
+  const float2 r = make_float2(sqrt_approx(dd.x), sqrt_approx(dd.y));
+  if (KIND == ABX_K_WENDLAND_C2) {
+    const float2 q = __fmul2_rn(r, make_float2(P.p0f, P.p0f));
+    const float2 t = __ffma2_rn(q, make_float2(-1.f, -1.f), make_float2(1.f, 1.f));
+    const float2 t2 = __fmul2_rn(t, t);
+    const float2 t4 = __fmul2_rn(t2, t2);
+    const float2 pw = __ffma2_rn(q, make_float2(4.f, 4.f), make_float2(1.f, 1.f));
+    return __fmul2_rn(t4, pw);
+  }
+  if (KIND == ABX_K_LAPLACE) {
+    const float2 a = __fadd2_rn(r, make_float2(P.p0f, P.p0f));
+    return make_float2(__fdividef(1.f, a.x), __fdividef(1.f, a.y));
+  }
+  if (KIND == ABX_K_MULTIQUADRIC) {
+    const float2 a = __fadd2_rn(dd, make_float2(P.p0f, P.p0f));
+    return make_float2(sqrt_approx(a.x), sqrt_approx(a.y));
+  }
+  return make_float2(0.f, 0.f);
+}
 
 __device__ __forceinline__ float warp_min(float v) {
 #pragma unroll
@@ -590,6 +640,11 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 8)
     const float r2lo = __double2float_rd(fmax(P.r2 - band, 0.0));
     const float r2hi = __double2float_ru(P.r2 + band);
     const float r2box = __double2float_ru((P.r2 + band) * (1.0 + 1e-6) + 1e-300);
+    // band as |d2 - r2mid| <= r2half, widened by a few ulps so that the FP32
+    // subtraction never shrinks it below (r2lo, r2hi]
+    const float r2mid = (float)(0.5 * ((double)r2lo + (double)r2hi));
+    const float r2half =
+        __double2float_ru(0.5 * ((double)r2hi - (double)r2lo) + 8.0 * 5.960464477539063e-08 * P.r2);
     D4 xq;
     bool have_xq = false;
     double acc64 = 0.0;
@@ -601,13 +656,15 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 8)
       const int nseg = build_segments(P, lo, hi, a0, a1, R1, nrows, row0, ws, lane);
       if (nseg == 0) continue;
       const int total = ws.off[nseg];
+      int cur = 0;  // this lane's segment; its candidate index only grows
       for (int t0 = 0; t0 < total; t0 += 32) {
         const int t = t0 + lane;
         bool keep = false;
         float4 st;
         int k = 0, sidx = 0;
         if (t < total) {
-          sidx = find_seg(ws, nseg, t);
+          while (cur + 1 < nseg && ws.off[cur + 1] <= t) ++cur;
+          sidx = cur;
           const int4 sg = ws.seg[sidx];
           k = sg.x + (t - ws.off[sidx]);
           int img[3], du0, du1;
@@ -623,17 +680,66 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 8)
           if (keep) st.w = (POL == POL_MATVEC) ? P.b32[k] : 0.f;
         }
         const unsigned km = __ballot_sync(0xffffffffu, keep);
+        const int nt = __popc(km);
         if (keep) {
           const int slot = __popc(km & lt);
           sm.p[slot] = st;
           sm.meta[slot] = make_int2(k, sidx);
+          if (POL == POL_MATVEC) {
+            float *pf = reinterpret_cast<float *>(&sm.pp[2 * (slot >> 1)]);
+            const int o = slot & 1;
+            pf[o] = st.x;
+            pf[2 + o] = st.y;
+            pf[4 + o] = st.z;
+            pf[6 + o] = st.w;
+          }
+        }
+        if (POL == POL_MATVEC && lane == 0 && (nt & 1)) {
+          // pad an odd tile with a far-away candidate of weight 0 (finite, so
+          // that every kernel formula stays finite and the clamp/select zeroes it)
+          float *pf = reinterpret_cast<float *>(&sm.pp[2 * (nt >> 1)]);
+          pf[1] = pf[3] = pf[5] = 1e4f;
+          pf[7] = 0.f;
         }
         __syncwarp();
-        const int nt = __popc(km);
         float acc32 = 0.f;
         bool need = false;
+        if (POL == POL_MATVEC) {
+          // one query against two candidates per packed FP32x2 instruction
+          const float2 nqx = make_float2(-pq0, -pq0), nqy = make_float2(-pq1, -pq1),
+                       nqz = make_float2(-pq2, -pq2);
+          float2 acc2 = make_float2(0.f, 0.f);
+          const int npair = (nt + 1) >> 1;
+#pragma unroll 2
+          for (int h = 0; h < npair; ++h) {
+            const float4 A = sm.pp[2 * h], B = sm.pp[2 * h + 1];
+            const float2 dx = __fadd2_rn(make_float2(A.x, A.y), nqx);
+            const float2 dy = __fadd2_rn(make_float2(A.z, A.w), nqy);
+            const float2 dz = __fadd2_rn(make_float2(B.x, B.y), nqz);
+            float2 dd = __fmul2_rn(dx, dx);
+            dd = __ffma2_rn(dy, dy, dd);
+            dd = __ffma2_rn(dz, dz, dd);
+            float2 w;
+            if (KIND == ABX_K_WENDLAND_C2) {
+              // the kernel vanishes for q >= 1: the clamp is the cut-off for
+              // every pair outside the rounding band (d2 > r2hi means q > 1),
+              // and band pairs are flagged for the exact test below
+              const float2 bd = __fadd2_rn(dd, make_float2(-r2mid, -r2mid));
+              need |= (fabsf(bd.x) <= r2half) | (fabsf(bd.y) <= r2half);
+              w = kern32x2_wendland_clamped(dd, P);
+            } else {
+              const bool ia = dd.x <= r2lo, ib = dd.y <= r2lo;
+              need |= ((dd.x > r2lo) & (dd.x <= r2hi)) | ((dd.y > r2lo) & (dd.y <= r2hi));
+              w = kern32x2<KIND>(dd, P);
+              w.x = ia ? w.x : 0.f;
+              w.y = ib ? w.y : 0.f;
+            }
+            acc2 = __ffma2_rn(w, make_float2(B.z, B.w), acc2);
+          }
+          acc32 = acc2.x + acc2.y;
+        }
 #pragma unroll 4
-        for (int j = 0; j < nt; ++j) {
+        for (int j = 0; j < nt && POL != POL_MATVEC; ++j) {
           const float4 c = sm.p[j];
           const float d0 = c.x - pq0, d1 = c.y - pq1, d2v = c.z - pq2;
           const float dd = fmaf(d2v, d2v, fmaf(d1, d1, d0 * d0));
@@ -657,11 +763,19 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 8)
               const float4 c = sm.p[j];
               const float d0 = c.x - pq0, d1 = c.y - pq1, d2v = c.z - pq2;
               const float dd = fmaf(d2v, d2v, fmaf(d1, d1, d0 * d0));
-              if (dd > r2lo && dd <= r2hi) {
+              const bool wend = POL == POL_MATVEC && KIND == ABX_K_WENDLAND_C2;
+              const bool flagged = wend ? fabsf(__fadd_rn(dd, -r2mid)) <= r2half
+                                        : (dd > r2lo && dd <= r2hi);
+              if (flagged) {
                 const int2 mt = sm.meta[j];
                 int img[3], du0, du1;
                 unpack_seg(ws.seg[mt.y].z, img, du0, du1);
-                if (!(exact_d2(xq, P.cpos[mt.x], img, fg) > P.r2)) {
+                const bool inside = !(exact_d2(xq, P.cpos[mt.x], img, fg) > P.r2);
+                if (wend) {
+                  // the packed loop added the clamped value: take it back out
+                  // for pairs the FP64 test rejects
+                  if (!inside) acc32 -= kern32x2_wendland_clamped(make_float2(dd, dd), P).x * c.w;
+                } else if (inside) {
                   if (POL == POL_MATVEC) acc32 = fmaf(kern32<KIND>(dd, P), c.w, acc32);
                   if (POL == POL_COUNT) ++count;
                   if (POL == POL_LIST && active) P.cols_out[out_off++] = (int32_t)P.cperm[mt.x];
