@@ -501,12 +501,14 @@ __device__ __forceinline__ int find_seg(const WarpSeg &ws, int nseg, int t) {
   return lo;
 }
 
+constexpr int STAGE = 64;  // candidates staged per round (two per lane)
+
 struct WarpTile32 {
-  float4 p[32];
+  float4 p[STAGE];
   // the same candidates as pairs for the packed FP32x2 loop:
   // pp[2h] = (x_a, x_b, y_a, y_b), pp[2h+1] = (z_a, z_b, b_a, b_b), a = 2h, b = 2h+1
-  float4 pp[32];
-  int2 meta[32];  // column kernel index, segment index
+  float4 pp[STAGE + 2];
+  int2 meta[STAGE];  // column kernel index, segment index
 };
 
 __device__ __forceinline__ float sqrt_approx(float x) {
@@ -657,43 +659,48 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 8)
       if (nseg == 0) continue;
       const int total = ws.off[nseg];
       int cur = 0;  // this lane's segment; its candidate index only grows
-      for (int t0 = 0; t0 < total; t0 += 32) {
-        const int t = t0 + lane;
-        bool keep = false;
-        float4 st;
-        int k = 0, sidx = 0;
-        if (t < total) {
-          while (cur + 1 < nseg && ws.off[cur + 1] <= t) ++cur;
-          sidx = cur;
-          const int4 sg = ws.seg[sidx];
-          k = sg.x + (t - ws.off[sidx]);
-          int img[3], du0, du1;
-          unpack_seg(sg.z, img, du0, du1);
-          const float4 cl = P.cloc[k];
-          st.x = fmaf((float)du0, fg.hf[0], cl.x);
-          st.y = fmaf((float)du1, fg.hf[1], cl.y);
-          st.z = fmaf((float)(__float_as_int(cl.w) + sg.w), fg.hf[2], cl.z);
-          const float e0 = fmaxf(fmaxf(bl0 - st.x, st.x - bh0), 0.f);
-          const float e1 = fmaxf(fmaxf(bl1 - st.y, st.y - bh1), 0.f);
-          const float e2 = fmaxf(fmaxf(bl2 - st.z, st.z - bh2), 0.f);
-          keep = fmaf(e2, e2, fmaf(e1, e1, e0 * e0)) <= r2box;
-          if (keep) st.w = (POL == POL_MATVEC) ? P.b32[k] : 0.f;
-        }
-        const unsigned km = __ballot_sync(0xffffffffu, keep);
-        const int nt = __popc(km);
-        if (keep) {
-          const int slot = __popc(km & lt);
-          sm.p[slot] = st;
-          sm.meta[slot] = make_int2(k, sidx);
-          if (POL == POL_MATVEC) {
-            float *pf = reinterpret_cast<float *>(&sm.pp[2 * (slot >> 1)]);
-            const int o = slot & 1;
-            pf[o] = st.x;
-            pf[2 + o] = st.y;
-            pf[4 + o] = st.z;
-            pf[6 + o] = st.w;
+      for (int t0 = 0; t0 < total; t0 += STAGE) {
+        int nt = 0;
+#pragma unroll
+        for (int sub = 0; sub < STAGE / 32; ++sub) {
+          const int t = t0 + sub * 32 + lane;
+          bool keep = false;
+          float4 st;
+          int k = 0, sidx = 0;
+          if (t < total) {
+            while (cur + 1 < nseg && ws.off[cur + 1] <= t) ++cur;
+            sidx = cur;
+            const int4 sg = ws.seg[sidx];
+            k = sg.x + (t - ws.off[sidx]);
+            int img[3], du0, du1;
+            unpack_seg(sg.z, img, du0, du1);
+            const float4 cl = P.cloc[k];
+            st.x = fmaf((float)du0, fg.hf[0], cl.x);
+            st.y = fmaf((float)du1, fg.hf[1], cl.y);
+            st.z = fmaf((float)(__float_as_int(cl.w) + sg.w), fg.hf[2], cl.z);
+            const float e0 = fmaxf(fmaxf(bl0 - st.x, st.x - bh0), 0.f);
+            const float e1 = fmaxf(fmaxf(bl1 - st.y, st.y - bh1), 0.f);
+            const float e2 = fmaxf(fmaxf(bl2 - st.z, st.z - bh2), 0.f);
+            keep = fmaf(e2, e2, fmaf(e1, e1, e0 * e0)) <= r2box;
+            if (keep) st.w = (POL == POL_MATVEC) ? P.b32[k] : 0.f;
           }
+          const unsigned km = __ballot_sync(0xffffffffu, keep);
+          if (keep) {
+            const int slot = nt + __popc(km & lt);
+            sm.p[slot] = st;
+            sm.meta[slot] = make_int2(k, sidx);
+            if (POL == POL_MATVEC) {
+              float *pf = reinterpret_cast<float *>(&sm.pp[2 * (slot >> 1)]);
+              const int o = slot & 1;
+              pf[o] = st.x;
+              pf[2 + o] = st.y;
+              pf[4 + o] = st.z;
+              pf[6 + o] = st.w;
+            }
+          }
+          nt += __popc(km);
         }
+        __syncwarp();
         if (POL == POL_MATVEC && lane == 0 && (nt & 1)) {
           // pad an odd tile with a far-away candidate of weight 0 (finite, so
           // that every kernel formula stays finite and the clamp/select zeroes it)
