@@ -24,6 +24,7 @@ from ._lib import ABXError, closing, lib, load_library  # noqa: F401
 __all__ = [
     "ABXError", "Context", "Particles", "Kernel", "Operator", "create_sparse_operator",
     "create_dense_operator", "radius_count", "radius_query_csr", "PREC_FP64", "PREC_MIXED",
+    "LOSS_MSE", "LOSS_SPAI_RESIDUAL",
     "K_CONST", "K_GAUSSIAN", "K_WENDLAND_C2", "K_COMPACT_GAUSSIAN", "K_LAPLACE",
     "K_MULTIQUADRIC", "K_SCALAR_SUM", "default_context", "Preconditioner",
     "schwarz_preconditioner", "spai_preconditioner", "gmres", "knn", "spai_exact_rows", "MLP",
@@ -31,6 +32,7 @@ __all__ = [
 ]
 
 PREC_FP64, PREC_MIXED = 0, 1
+LOSS_MSE, LOSS_SPAI_RESIDUAL = 0, 1
 (K_CONST, K_GAUSSIAN, K_WENDLAND_C2, K_COMPACT_GAUSSIAN, K_LAPLACE, K_MULTIQUADRIC,
  K_SCALAR_SUM) = range(7)
 
@@ -461,9 +463,17 @@ class MLP:
         p = np.ascontiguousarray(p, dtype=np.float32)
         _check(lib().abx_mlp_set_params(self._h, _ptr(p)), "abx_mlp_set_params")
 
-    def gradients(self, x, y):
+    def set_loss(self, kind, dim=0, kernel=None, cutoff=0.0):
+        """LOSS_MSE (targets) or LOSS_SPAI_RESIDUAL (mean |A_i m_i - e_0|^2 with
+        A_i built from each row's features by ``kernel`` inside ``cutoff``)."""
+        _check(lib().abx_mlp_set_loss(self._h, int(kind), int(dim),
+                                      C.byref(kernel) if kernel is not None else None,
+                                      float(cutoff)), "abx_mlp_set_loss")
+
+    def gradients(self, x, y=None):
         x = np.ascontiguousarray(x, dtype=np.float32)
-        y = np.ascontiguousarray(y, dtype=np.float32)
+        if y is not None:
+            y = np.ascontiguousarray(y, dtype=np.float32)
         g = np.empty(self.num_params, dtype=np.float32)
         loss = C.c_float()
         _check(lib().abx_mlp_gradients(self._h, _ptr(x), _ptr(y), x.shape[0], _ptr(g),
@@ -474,7 +484,8 @@ class MLP:
         loss = C.c_float()
         if isinstance(x, np.ndarray):
             x = np.ascontiguousarray(x, dtype=np.float32)
-            y = np.ascontiguousarray(y, dtype=np.float32)
+            if y is not None:
+                y = np.ascontiguousarray(y, dtype=np.float32)
         _check(lib().abx_mlp_train_step(self._h, _ptr(x), _ptr(y), int(x.shape[0]), float(lr),
                                         C.byref(loss)), "abx_mlp_train_step")
         return loss.value

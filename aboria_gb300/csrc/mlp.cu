@@ -34,6 +34,10 @@ struct abx_mlp {
   float in_scale = 1.0f;
   int out_transform = 0;  // 0: y; 1: out_c * sinh(y) (targets trained as asinh(w / out_c))
   float out_c = 1.0f;
+  int loss_kind = ABX_LOSS_MSE;
+  int loss_dim = 0;         // ABX_LOSS_SPAI_RESIDUAL: coordinates per support point
+  abx_kernel loss_kern{};   //   kernel and cut-off in feature units
+  float loss_cut2 = 0.f;
   int64_t step = 0;
   // activations for the last batch (training)
   abx::DevBuf<float> act, pre;  // sum over layers of B*dims
@@ -163,6 +167,66 @@ __global__ void k_mse(int64_t n, int N, const float *__restrict__ out,
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
   if ((threadIdx.x & 31) == 0 && l != 0.f) atomicAdd(loss, l);
+}
+
+__device__ __forceinline__ float kern_feature(const abx_kernel &k, float d2) {
+  switch (k.kind) {
+  case ABX_K_CONST: return (float)k.p[0];
+  case ABX_K_GAUSSIAN:
+  case ABX_K_COMPACT_GAUSSIAN: return __expf(-d2 * (float)k.p[0]);
+  case ABX_K_WENDLAND_C2: {
+    const float q = sqrtf(d2) * (float)k.p[0];
+    const float t = fmaxf(1.f - q, 0.f), t2 = t * t;
+    return t2 * t2 * (4.f * q + 1.f);
+  }
+  case ABX_K_LAPLACE: return 1.f / (sqrtf(d2) + (float)k.p[0]);
+  case ABX_K_MULTIQUADRIC: return sqrtf(d2 + (float)k.p[0]);
+  default: return 0.f;
+  }
+}
+
+// Approximate-inverse residual loss, one warp per row (k <= 32 support
+// points, lane a holds point a): m = out * scale + shift, r = A m - e_0,
+// loss += |r|^2 / B, d = scale * 2 A r / B (A symmetric).
+__global__ void k_spai_residual(int64_t B, int k, int dim, abx_kernel kern, float cut2,
+                                const float *__restrict__ feats, const float *__restrict__ out,
+                                const float *__restrict__ scale, const float *__restrict__ shift,
+                                float *__restrict__ d, float *__restrict__ loss) {
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int a = threadIdx.x & 31;
+  if (row >= B) return;  // whole warps exit together
+  const bool act = a < k;
+  float f[3] = {0.f, 0.f, 0.f};
+  for (int e = 0; e < dim; ++e) f[e] = act ? feats[(row * k + a) * dim + e] : 0.f;
+  const float m = act ? out[row * k + a] * scale[a] + shift[a] : 0.f;
+  float am = 0.f;
+  for (int b = 0; b < k; ++b) {
+    float d2 = 0.f;
+    for (int e = 0; e < dim; ++e) {
+      const float v = __shfl_sync(0xffffffffu, f[e], b) - f[e];
+      d2 = fmaf(v, v, d2);
+    }
+    const float mb = __shfl_sync(0xffffffffu, m, b);
+    const float A = (cut2 <= 0.f || d2 < cut2) ? kern_feature(kern, d2) : 0.f;
+    am = fmaf(A, mb, am);
+  }
+  const float r = act ? am - (a == 0 ? 1.f : 0.f) : 0.f;
+  float ar = 0.f;
+  for (int b = 0; b < k; ++b) {
+    float d2 = 0.f;
+    for (int e = 0; e < dim; ++e) {
+      const float v = __shfl_sync(0xffffffffu, f[e], b) - f[e];
+      d2 = fmaf(v, v, d2);
+    }
+    const float rb = __shfl_sync(0xffffffffu, r, b);
+    const float A = (cut2 <= 0.f || d2 < cut2) ? kern_feature(kern, d2) : 0.f;
+    ar = fmaf(A, rb, ar);
+  }
+  if (act) d[row * k + a] = scale[a] * 2.f * ar / (float)B;
+  float l = r * r / (float)B;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+  if (a == 0) atomicAdd(loss, l);
 }
 
 __global__ void k_adam(int64_t n, float *__restrict__ p, const float *__restrict__ g,
@@ -376,9 +440,15 @@ int mlp_backward(abx_mlp *M, const float *x, const float *target, int64_t B, flo
   const int nout = M->dims[L];
   float *d = M->dbuf0.ptr, *dn = M->dbuf1.ptr;
   ABX_CHECK_CUDA(cudaMemsetAsync(M->lossbuf.ptr, 0, sizeof(float), s));
-  k_mse<<<ceil_div((size_t)B * nout, 256), 256, 0, s>>>((size_t)B * nout, nout, M->act.ptr + aoff[L],
-                                                        target, M->out_scale.ptr,
-                                                        M->out_shift.ptr, d, M->lossbuf.ptr);
+  if (M->loss_kind == ABX_LOSS_SPAI_RESIDUAL)
+    k_spai_residual<<<ceil_div((size_t)B * 32, 256), 256, 0, s>>>(
+        B, nout, M->loss_dim, M->loss_kern, M->loss_cut2, x, M->act.ptr + aoff[L],
+        M->out_scale.ptr, M->out_shift.ptr, d, M->lossbuf.ptr);
+  else
+    k_mse<<<ceil_div((size_t)B * nout, 256), 256, 0, s>>>((size_t)B * nout, nout,
+                                                          M->act.ptr + aoff[L], target,
+                                                          M->out_scale.ptr, M->out_shift.ptr, d,
+                                                          M->lossbuf.ptr);
   for (int l = L - 1; l >= 0; --l) {
     const int in = M->dims[l], out = M->dims[l + 1];
     if (l < L - 1)
@@ -557,6 +627,25 @@ int abx_mlp_set_output_transform(abx_mlp *M, int kind, float c) {
   return ABX_OK;
 }
 
+int abx_mlp_set_loss(abx_mlp *M, int kind, int dim, const abx_kernel *k, double cutoff) {
+  ABX_REQUIRE(M, ABX_ERR_INVALID, "null mlp");
+  if (kind == ABX_LOSS_MSE) {
+    M->loss_kind = kind;
+    return ABX_OK;
+  }
+  ABX_REQUIRE(kind == ABX_LOSS_SPAI_RESIDUAL && k, ABX_ERR_INVALID, "unknown loss %d", kind);
+  const int nout = M->dims.back();
+  ABX_REQUIRE(dim >= 1 && dim <= 3 && nout <= 32 && M->dims[0] == nout * dim, ABX_ERR_INVALID,
+              "residual loss needs out_dim <= 32 and in_dim = out_dim * dim (%d, %d, %d)",
+              M->dims[0], nout, dim);
+  ABX_REQUIRE(M->out_transform == 0, ABX_ERR_INVALID, "residual loss needs output transform 0");
+  M->loss_kind = kind;
+  M->loss_dim = dim;
+  M->loss_kern = *k;
+  M->loss_cut2 = cutoff > 0 ? (float)(cutoff * cutoff) : 0.f;
+  return ABX_OK;
+}
+
 int abx_mlp_get_params(abx_mlp *M, float *out) {
   ABX_REQUIRE(M && out, ABX_ERR_INVALID, "null argument");
   ABX_TRY(ctx_activate(M->ctx));
@@ -574,12 +663,13 @@ int abx_mlp_set_params(abx_mlp *M, const float *in) {
 
 int abx_mlp_gradients(abx_mlp *M, const float *x, const float *y, int64_t batch, float *grads,
                       float *loss) {
-  ABX_REQUIRE(M && x && y && batch > 0, ABX_ERR_INVALID, "invalid argument");
+  ABX_REQUIRE(M && x && (y || M->loss_kind == ABX_LOSS_SPAI_RESIDUAL) && batch > 0,
+              ABX_ERR_INVALID, "invalid argument");
   ABX_TRY(ctx_activate(M->ctx));
-  const void *dx, *dy;
+  const void *dx, *dy = nullptr;
   HostStage a, b;
   ABX_TRY(a.in(M->ctx, x, (size_t)batch * M->dims[0] * 4, &dx));
-  ABX_TRY(b.in(M->ctx, y, (size_t)batch * M->dims.back() * 4, &dy));
+  if (y) ABX_TRY(b.in(M->ctx, y, (size_t)batch * M->dims.back() * 4, &dy));
   ABX_TRY(mlp_backward(M, (const float *)dx, (const float *)dy, batch, loss));
   if (grads) {
     ABX_CHECK_CUDA(cudaMemcpyAsync(grads, M->grads.ptr, M->nparams * 4, cudaMemcpyDefault,
@@ -591,11 +681,12 @@ int abx_mlp_gradients(abx_mlp *M, const float *x, const float *y, int64_t batch,
 
 int abx_mlp_train_step(abx_mlp *M, const float *x, const float *y, int64_t batch, float lr,
                        float *loss) {
-  ABX_REQUIRE(M && x && y && batch > 0, ABX_ERR_INVALID, "invalid argument");
+  ABX_REQUIRE(M && x && (y || M->loss_kind == ABX_LOSS_SPAI_RESIDUAL) && batch > 0,
+              ABX_ERR_INVALID, "invalid argument");
   ABX_TRY(ctx_activate(M->ctx));
-  const void *dx, *dy;
+  const void *dx, *dy = nullptr;
   ABX_TRY(M->sx.in(M->ctx, x, (size_t)batch * M->dims[0] * 4, &dx));
-  ABX_TRY(M->sy.in(M->ctx, y, (size_t)batch * M->dims.back() * 4, &dy));
+  if (y) ABX_TRY(M->sy.in(M->ctx, y, (size_t)batch * M->dims.back() * 4, &dy));
   ABX_TRY(mlp_backward(M, (const float *)dx, (const float *)dy, batch, loss));
   ++M->step;
   const float b1 = 0.9f, b2 = 0.999f;

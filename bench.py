@@ -111,15 +111,17 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
 
 
+PROFILE_SUMMARY = ROOT / "profiles" / "k_pairs_mixed_wendland_n4M.md"
+
+
 def profile_traffic():
-    """Per-launch DRAM bytes of the pair kernel from the committed ncu summary."""
-    p = ROOT / "profiles" / "pairs_matvec_traffic.json"
-    if p.exists():
-        try:
-            return json.loads(p.read_text())
-        except Exception:
-            return None
-    return None
+    """Per-launch DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of
+    the pair kernel, from the committed ncu summary of one capture."""
+    import re
+    if not PROFILE_SUMMARY.exists():
+        return None
+    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", PROFILE_SUMMARY.read_text())
+    return float(m.group(1)) if m else None
 
 
 def dist_setup(args):
@@ -256,7 +258,7 @@ def run_ours(args):
         "roofline": {
             "bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
             "frac": achieved_gbs / hbm_peak, "peak_source": peak_kind,
-            "traffic": (tr or {}).get("dram_bytes_per_launch"),
+            "traffic": tr,
             "note": "compulsory bytes N*(24+8+8)+ncells*8 per matvec; the pair kernel is "
                     "FP32-issue bound, see compute_roofline",
         },
@@ -270,6 +272,10 @@ def run_ours(args):
         "gpu_launches": 3 * args.steps,
         "clocks": clocks,
     }
+    if not args.matvec_only:
+        del K
+        out["rbf_solve"] = rbf_section(ctx, ROOT / "aboria_gb300" / "models" / "spai_mlp_2d.bin")
+        out["fmm"] = fmm_section(ctx)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(pos, b_by_id, budget_s=args.cpu_seconds)
     if rank == 0:
@@ -277,6 +283,135 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+RBF_N = 200_000
+RBF_EH = 2.5  # scaled shape parameter eps*h, h = N^-1/2
+
+
+def _timed(fn, ctx):
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    out = fn()
+    ctx.synchronize()
+    return out, time.perf_counter() - t0
+
+
+def rbf_section(ctx, model_path):
+    """RBF interpolation solve to 1e-8 FP64 relative residual: 2-D, N=200,000
+    uniform points, f = sin(4 pi x) cos(3 pi y) + 1e-3 noise, compactly
+    supported Gaussian exp(-(eps |dx|)^2) cut at eps |dx| = 4, GMRES(100).
+
+    * plain   : restricted additive Schwarz on octree leaves of 256 points,
+                blocks factorised by FP64 LU, FP64 operator throughout.
+    * learned : the trained MLP's sparse approximate inverse (32 k-NN columns
+                per row, BF16 tensor-core inference), FP32 operator with FP64
+                residual refinement; Schwarz taken as fallback when the learned
+                preconditioner has not converged after 30 iterations.
+    * local_inverse : the exact FP64 local-inverse rows the network is trained
+                on, as the same sparse approximate inverse (the label method).
+    Every time includes the preconditioner's set-up; the residual reported is
+    |b - A x| / |b| with the FP64 operator."""
+    import aboria_gb300 as ab
+    import workloads
+    n = RBF_N
+    eps = RBF_EH * np.sqrt(n)
+    r = 4.0 / eps
+    pos = workloads.uniform(n, 2, seed=4040)
+    p = ab.Particles(2, ctx).set(pos)
+    p.init_octree([0.0, 0.0], [1.0, 1.0], [False, False], 256)
+    P = p.positions
+    f = np.sin(4 * np.pi * P[:, 0]) * np.cos(3 * np.pi * P[:, 1])
+    f += 1e-3 * np.random.default_rng(4041).standard_normal(n)
+    kern = ab.Kernel.make(ab.K_COMPACT_GAUSSIAN, eps * eps)
+    K64 = ab.create_sparse_operator(p, p, r, kern, ab.PREC_FP64)
+    K32 = ab.create_sparse_operator(p, p, r, kern, ab.PREC_MIXED)
+    out = {"workload": f"2-D N={n} uniform, compact Gaussian eps*h={RBF_EH} (eps={eps:.1f}), "
+                       f"cut-off r=4/eps={r:.3g}, f=sin(4 pi x)cos(3 pi y)+1e-3 noise, GMRES(100), "
+                       f"tol 1e-8 (FP64 residual)"}
+
+    def check(x):
+        return float(np.linalg.norm(f - K64 * x) / np.linalg.norm(f))
+
+    def plain():
+        M = ab.schwarz_preconditioner(K64)
+        x, it, res = ab.gmres(K64, f, M=M, restart=100, max_iters=2000, tol=1e-8)
+        return x, it, M.stats()
+    (x, it, st), t = _timed(plain, ctx)
+    out["plain_schwarz_fp64"] = {"seconds": t, "iterations": it, "residual": check(x),
+                                 "schwarz_setup_s": st["setup_s"], "domains": st["domains"]}
+
+    if model_path.exists():
+        mlp = ab.MLP.load(model_path)
+
+        def learned():
+            M = ab.learned_preconditioner(K32, mlp, eps)
+            return ab.gmres_with_fallback(K32, f, M, K64, restart=100, learned_max_iters=30,
+                                          max_iters=2000, tol=1e-8, A_check=K64)
+        (x, it, res, fb), t = _timed(learned, ctx)
+        out["learned_mixed"] = {"seconds": t, "iterations": it, "residual": check(x),
+                                "fallback_taken": bool(fb)}
+
+    def local_inverse():
+        cols, vals = ab.spai_local_inverse_rows(K64, 32)
+        M = ab.spai_preconditioner(ctx, cols, vals)
+        x, it, res = ab.gmres(K32, f, M=M, restart=100, max_iters=2000, tol=1e-8, A_check=K64)
+        return x, it
+    (x, it), t = _timed(local_inverse, ctx)
+    out["local_inverse_mixed"] = {"seconds": t, "iterations": it, "residual": check(x)}
+    if "learned_mixed" in out:
+        out["speedup_learned_vs_plain"] = (out["plain_schwarz_fp64"]["seconds"]
+                                           / out["learned_mixed"]["seconds"])
+    return out
+
+
+def fmm_section(ctx, n=1 << 20, orders=(3, 5, 7), n_targets=10000, steps=3):
+    """Chebyshev black-box FMM, Laplace 1/(|dx| + 1e-12), N uniform points in
+    the unit cube, octree leaves of 64, weights U[-1,1].  Per order: plan +
+    M2L set-up time, matvec time (CUDA events, mean of ``steps``) in FP64 and
+    mixed mode (3xTF32 tensor-core M2L, FP32 P2P), and the relative L2 error
+    of each against an FP64 direct sum (dense operator) on 10,000 seeded
+    targets, with the self term K(0) b_i = 1e12 b_i removed from both."""
+    import torch
+    import aboria_gb300 as ab
+    import workloads
+    pos = workloads.uniform(n, 3, seed=5050)
+    p = ab.Particles(3, ctx).set(pos)
+    p.init_octree([0.0] * 3, [1.0] * 3, [False] * 3, 64)
+    P = p.positions
+    b = np.random.default_rng(5051).uniform(-1, 1, n)
+    tgt = np.sort(np.random.default_rng(5052).choice(n, n_targets, replace=False))
+    kern = ab.Kernel.make(ab.K_LAPLACE, 1e-12)
+    tp = ab.Particles(3, ctx).set(P[tgt])
+    D = ab.create_dense_operator(tp, p, kern, ab.PREC_FP64)
+    direct = (D * b) - 1e12 * b[tgt]
+    del D
+    b_dev = torch.from_numpy(b).cuda()
+    c_dev = torch.empty_like(b_dev)
+    stream = torch.cuda.current_stream()
+    res = {"workload": f"3-D N={n} uniform, Laplace 1/(|dx|+1e-12), leaf 64, "
+                       f"error vs FP64 direct sum on {n_targets} targets"}
+    for order in orders:
+        K, t_setup = _timed(lambda: ab.create_fmm_operator(p, kern, order), ctx)
+        st = ab.fmm_stats(K)
+        row = {"setup_s": t_setup, "m2l_pairs": st["m2l_pairs"], "leaves": st["leaves"]}
+        for prec, name in ((ab.PREC_FP64, "fp64"), (ab.PREC_MIXED, "mixed")):
+            K.set_precision(prec)
+            K.matvec(b_dev, out=c_dev)
+            ts = []
+            for _ in range(steps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                K.matvec(b_dev, out=c_dev, sync=False)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            c = c_dev.cpu().numpy()[tgt] - 1e12 * b[tgt]
+            row[f"{name}_ms"] = float(np.mean(ts))
+            row[f"{name}_rel_l2"] = float(np.linalg.norm(c - direct) / np.linalg.norm(direct))
+        res[f"order{order}"] = row
+        del K
+    return res
 
 
 def cpu_baseline(pos, b_by_id, budget_s=15.0):
@@ -357,11 +492,13 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--matvec-only", action="store_true",
+                    help="skip the RBF-solve and FMM sections (profiling runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

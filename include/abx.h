@@ -267,8 +267,22 @@ ABX_API int abx_mlp_set_normalization(abx_mlp *mlp, float in_scale, const float 
 ABX_API int abx_mlp_set_output_transform(abx_mlp *mlp, int kind, float c);
 ABX_API int abx_mlp_get_params(abx_mlp *mlp, float *params);
 ABX_API int abx_mlp_set_params(abx_mlp *mlp, const float *params);
-/* Loss (mean squared error on normalised targets) and its gradient w.r.t.
- * the flat parameters for one batch, without updating. */
+/* Training loss of abx_mlp_gradients / abx_mlp_train_step.
+ *   ABX_LOSS_MSE (default): mean squared error on normalised targets y.
+ *   ABX_LOSS_SPAI_RESIDUAL: the approximate-inverse residual of each row,
+ *     mean_i |A_i m_i - e_0|^2, with m_i the denormalised output (k = out_dim
+ *     weights, output transform 0) and A_i the k x k kernel matrix of the
+ *     row's support read from its features x_i = (f_0 .. f_{k-1}), f_a in
+ *     R^dim (in_dim = k*dim, f_0 the row's own point): A_ab = kern(f_b - f_a)
+ *     when |f_b - f_a| < cutoff, else 0.  e_0 selects the row's own point.
+ *     Targets are not used (y may be NULL).  Errors in directions the
+ *     operator barely sees cost little, which a weight MSE cannot express.
+ * No counterpart in the reference. */
+#define ABX_LOSS_MSE 0
+#define ABX_LOSS_SPAI_RESIDUAL 1
+ABX_API int abx_mlp_set_loss(abx_mlp *mlp, int kind, int dim, const abx_kernel *k, double cutoff);
+/* Loss and its gradient w.r.t. the flat parameters for one batch, without
+ * updating. */
 ABX_API int abx_mlp_gradients(abx_mlp *mlp, const float *x, const float *y, int64_t batch,
                               float *grads, float *loss);
 /* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on one batch. */

@@ -34,6 +34,33 @@ def test_gradients_match_oracle():
     assert np.linalg.norm(g - go) / np.linalg.norm(go) < 1e-4
 
 
+def test_residual_loss_gradients_match_oracle():
+    """ABX_LOSS_SPAI_RESIDUAL: mean |A_i m_i - e_0|^2 with A_i the compact
+    Gaussian exp(-|f_a - f_b|^2) (cut at 4) of each row's 32 support points."""
+    m = ab.MLP.create(64, 128, 3, 32, seed=96)
+    sc = np.full(32, 0.1, np.float32)
+    sh = np.zeros(32, np.float32)
+    sh[0] = 1.0
+    m.set_normalization(1.0, sc, sh)
+    kern = ab.Kernel.make(ab.K_COMPACT_GAUSSIAN, 1.0)
+    m.set_loss(ab.LOSS_SPAI_RESIDUAL, 2, kern, 4.0)
+    rng = np.random.default_rng(97)
+    x = (rng.standard_normal((256, 32, 2)) * 1.5).astype(np.float32)
+    x[:, 0, :] = 0.0
+    x = x.reshape(256, 64)
+    loss, g = m.gradients(x)
+    dims = [64, 128, 128, 128, 32]
+    lo, go = mlp_oracle.residual_loss_and_grad(m.params.astype(np.float64), dims, x, 2,
+                                               lambda d2: np.exp(-d2), 4.0, sc, sh)
+    assert abs(loss - lo) / lo < 1e-4
+    assert np.linalg.norm(g - go) / np.linalg.norm(go) < 1e-4
+    # training on the residual lowers it
+    l0 = m.train_step(x, None, 1e-3)
+    for _ in range(30):
+        l1 = m.train_step(x, None, 1e-3)
+    assert l1 < 0.8 * l0
+
+
 def test_bf16_inference_matches_fp32():
     m, sc, sh = small_model(93)
     x = np.random.default_rng(94).standard_normal((1000, 64)).astype(np.float32)

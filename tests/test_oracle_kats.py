@@ -150,6 +150,26 @@ def test_mlp_oracle_gradient_matches_finite_differences():
         assert abs((lp - lm) / 2e-6 - g[i]) < 1e-6 * max(1.0, abs(g[i]))
 
 
+def test_mlp_oracle_residual_gradient_matches_finite_differences():
+    """The approximate-inverse residual loss: k = 4 support points in 2-D."""
+    import mlp_oracle
+    rng = np.random.default_rng(95)
+    dims = [8, 6, 4]
+    n = sum(dims[i] * dims[i + 1] + dims[i + 1] for i in range(2))
+    p = rng.standard_normal(n) * 0.5
+    x = rng.standard_normal((5, 8))
+    x[:, :2] = 0.0  # f_0 is the row's own point
+    sc, sh = np.full(4, 0.3), np.array([1.0, 0.0, 0.0, 0.0])
+    kern = lambda d2: np.exp(-d2)
+    loss, g = mlp_oracle.residual_loss_and_grad(p, dims, x, 2, kern, 2.5, sc, sh)
+    for i in rng.choice(n, 12, replace=False):
+        e = np.zeros(n)
+        e[i] = 1e-6
+        lp, _ = mlp_oracle.residual_loss_and_grad(p + e, dims, x, 2, kern, 2.5, sc, sh)
+        lm, _ = mlp_oracle.residual_loss_and_grad(p - e, dims, x, 2, kern, 2.5, sc, sh)
+        assert abs((lp - lm) / 2e-6 - g[i]) < 1e-6 * max(1.0, abs(g[i]))
+
+
 @pytest.mark.parametrize("dim", [2, 3])
 def test_fmm_oracle_reference_kat(dim):
     """tests/fmm.h:167-253: N=1000 uniform, n_leaf 10, kernel sqrt(|dx|^2 + 0.01),
