@@ -503,6 +503,17 @@ __device__ __forceinline__ int find_seg(const WarpSeg &ws, int nseg, int t) {
 
 constexpr int STAGE = 64;  // candidates staged per round (two per lane)
 
+// Internal kernel tag: Wendland C2 in a mixed-precision matvec whose kernel
+// support 1/p0 is no larger than the search radius (p0 * r >= 1 - 1e-9).  The kernel
+// then vanishes at and beyond the cut-off to fourth order, so the clamp
+// max(1 - q, 0) is the whole cut-off test: a pair whose FP32 and FP64
+// classifications differ has |q - 1| <= delta with delta ~ 1e-5 (the FP32
+// rounding band of d^2 relative to r^2), and contributes at most
+// 5 delta^4 |b_j| < 1e-19 |b_j| either way -- far below the FP32 term
+// precision -- so no pair needs the exact FP64 re-test.  Coordinates are
+// staged pre-scaled by p0, making d^2 = q^2 directly.
+constexpr int K_WEND_CUT = 100 + ABX_K_WENDLAND_C2;
+
 struct WarpTile32 {
   float4 p[STAGE];
   // the same candidates as pairs for the packed FP32x2 loop:
@@ -610,6 +621,8 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 8)
   WarpTile32 &sm = tile_all[wid];
   const FineGrid &fg = P.fg;
   const unsigned lt = (1u << lane) - 1u;
+  constexpr bool WCUT = KIND == K_WEND_CUT;
+  const float sc = WCUT ? P.p0f : 1.f;  // staging scale (d^2 = q^2 for WCUT)
   for (;;) {
     int unit = 0;
     if (lane == 0) unit = atomicAdd(P.counter, 1);
@@ -685,7 +698,11 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 8)
             if (keep) st.w = (POL == POL_MATVEC) ? P.b32[k] : 0.f;
           }
           const unsigned km = __ballot_sync(0xffffffffu, keep);
-          if (keep) {
+          if (WCUT) {
+            // natural order, one 16-byte store per lane (no bank conflicts);
+            // repacked into candidate pairs below
+            if (keep) sm.p[nt + __popc(km & lt)] = make_float4(st.x * sc, st.y * sc, st.z * sc, st.w);
+          } else if (keep) {
             const int slot = nt + __popc(km & lt);
             sm.p[slot] = st;
             sm.meta[slot] = make_int2(k, sidx);
@@ -701,7 +718,18 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 8)
           nt += __popc(km);
         }
         __syncwarp();
-        if (POL == POL_MATVEC && lane == 0 && (nt & 1)) {
+        if (WCUT) {
+          // pairs for the packed loop; an odd tail is paired with a far-away
+          // candidate of weight 0 (the clamp zeroes it)
+          const int h = lane;
+          if (2 * h < nt) {
+            const float4 c0 = sm.p[2 * h];
+            const float4 c1 = 2 * h + 1 < nt ? sm.p[2 * h + 1] : make_float4(1e4f, 1e4f, 1e4f, 0.f);
+            sm.pp[2 * h] = make_float4(c0.x, c1.x, c0.y, c1.y);
+            sm.pp[2 * h + 1] = make_float4(c0.z, c1.z, c0.w, c1.w);
+          }
+        }
+        if (!WCUT && POL == POL_MATVEC && lane == 0 && (nt & 1)) {
           // pad an odd tile with a far-away candidate of weight 0 (finite, so
           // that every kernel formula stays finite and the clamp/select zeroes it)
           float *pf = reinterpret_cast<float *>(&sm.pp[2 * (nt >> 1)]);
@@ -711,7 +739,33 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 8)
         __syncwarp();
         float acc32 = 0.f;
         bool need = false;
-        if (POL == POL_MATVEC) {
+        if (WCUT) {
+          // one query against two candidates per packed FP32x2 instruction;
+          // coordinates in units of the kernel support, so q = |dx|
+          const float2 nqx = make_float2(-pq0 * sc, -pq0 * sc), nqy = make_float2(-pq1 * sc, -pq1 * sc),
+                       nqz = make_float2(-pq2 * sc, -pq2 * sc);
+          float2 acc2 = make_float2(0.f, 0.f);
+          const int npair = (nt + 1) >> 1;
+#pragma unroll 2
+          for (int h = 0; h < npair; ++h) {
+            const float4 A = sm.pp[2 * h], B = sm.pp[2 * h + 1];
+            const float2 dx = __fadd2_rn(make_float2(A.x, A.y), nqx);
+            const float2 dy = __fadd2_rn(make_float2(A.z, A.w), nqy);
+            const float2 dz = __fadd2_rn(make_float2(B.x, B.y), nqz);
+            float2 dd = __fmul2_rn(dx, dx);
+            dd = __ffma2_rn(dy, dy, dd);
+            dd = __ffma2_rn(dz, dz, dd);
+            const float2 q = make_float2(sqrt_approx(dd.x), sqrt_approx(dd.y));
+            float2 t = __ffma2_rn(q, make_float2(-1.f, -1.f), make_float2(1.f, 1.f));
+            t.x = fmaxf(t.x, 0.f);
+            t.y = fmaxf(t.y, 0.f);
+            const float2 t2 = __fmul2_rn(t, t);
+            const float2 pw = __ffma2_rn(q, make_float2(4.f, 4.f), make_float2(1.f, 1.f));
+            const float2 t4 = __fmul2_rn(t2, t2);
+            acc2 = __ffma2_rn(__fmul2_rn(t4, pw), make_float2(B.z, B.w), acc2);
+          }
+          acc32 = acc2.x + acc2.y;
+        } else if (POL == POL_MATVEC) {
           // one query against two candidates per packed FP32x2 instruction
           const float2 nqx = make_float2(-pq0, -pq0), nqy = make_float2(-pq1, -pq1),
                        nqz = make_float2(-pq2, -pq2);
@@ -759,7 +813,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 8)
           if (POL == POL_COUNT) count += in ? 1 : 0;
           if (POL == POL_LIST && in && active) P.cols_out[out_off++] = (int32_t)P.cperm[sm.meta[j].x];
         }
-        if (__any_sync(0xffffffffu, need)) {
+        if (!WCUT && __any_sync(0xffffffffu, need)) {
           // rare: decide the band pairs with the reference's FP64 test
           if (need) {
             if (!have_xq) {
@@ -980,11 +1034,23 @@ template <int POL, int KIND> int launch_pairs(abx_context *ctx, const KParams &P
   return ABX_OK;
 }
 
+int launch_wend_cut(abx_context *ctx, const KParams &P) {
+  const int blocks = grid_blocks(ctx, P.nunits);
+  ABX_CHECK_CUDA(cudaMemsetAsync(P.counter, 0, sizeof(int), ctx->stream));
+  k_pairs_mixed<POL_MATVEC, K_WEND_CUT><<<blocks, WARPS_PER_CTA * 32, 0, ctx->stream>>>(P);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  return ABX_OK;
+}
+
 template <int POL> int launch_pairs_kind(abx_context *ctx, const KParams &P, bool mixed) {
   switch (P.kind) {
   case ABX_K_CONST: return launch_pairs<POL, ABX_K_CONST>(ctx, P, mixed);
   case ABX_K_GAUSSIAN: return launch_pairs<POL, ABX_K_GAUSSIAN>(ctx, P, mixed);
-  case ABX_K_WENDLAND_C2: return launch_pairs<POL, ABX_K_WENDLAND_C2>(ctx, P, mixed);
+  case ABX_K_WENDLAND_C2:
+    // support 1/p0 <= r up to rounding of p0 = 1/r (a support wider by a
+    // relative 1e-9 adds pairs of weight <= 5e-36)
+    if (POL == POL_MATVEC && mixed && P.p0 * P.r >= 1.0 - 1e-9) return launch_wend_cut(ctx, P);
+    return launch_pairs<POL, ABX_K_WENDLAND_C2>(ctx, P, mixed);
   case ABX_K_COMPACT_GAUSSIAN: return launch_pairs<POL, ABX_K_COMPACT_GAUSSIAN>(ctx, P, mixed);
   case ABX_K_LAPLACE: return launch_pairs<POL, ABX_K_LAPLACE>(ctx, P, mixed);
   case ABX_K_MULTIQUADRIC: return launch_pairs<POL, ABX_K_MULTIQUADRIC>(ctx, P, mixed);
