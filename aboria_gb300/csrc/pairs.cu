@@ -173,7 +173,8 @@ __global__ void k_fine_keys(const double *__restrict__ src, int64_t n, int64_t s
 // Anchor cell of a point: the clamped cell for column particles (their range
 // membership), the unclamped cell for query points (which may lie outside
 // the domain and must keep their true periodic image).  loc holds the FP32
-// offset from the anchor cell's corner and, in .w, the anchor's e2 index.
+// offset from the anchor cell's corner and, in .w, the anchor's e2 index as
+// an (exact) float.
 __global__ void k_fill_layout(const double *__restrict__ src, int64_t stride, FineGrid fg,
                               const uint32_t *__restrict__ perm, int64_t n, int clamp_anchor,
                               int4 *__restrict__ cell, float4 *__restrict__ loc,
@@ -200,7 +201,7 @@ __global__ void k_fill_layout(const double *__restrict__ src, int64_t stride, Fi
     f[e] = (float)(x[e] - corner);
   }
   cell[k] = make_int4(c[0], c[1], c[2], 0);
-  loc[k] = make_float4(f[0], f[1], f[2], __int_as_float(c[2]));
+  loc[k] = make_float4(f[0], f[1], f[2], (float)c[2]);  // exact: c[2] < 2^24
   posk[k] = D4{x[0], x[1], x[2], 0.0};
 }
 
@@ -403,6 +404,7 @@ __device__ __forceinline__ void unpack_seg(int z, int img[3], int &du0, int &du1
 // prefix, and one staged tile of candidates.
 struct WarpSeg {
   int4 seg[SEG_CAP];      // start, end, packed(img, du0, du1), c2shift
+  float4 segf[SEG_CAP];   // du0, du1, c2shift as exact floats (staging offsets)
   int off[SEG_CAP + 1];   // exclusive prefix of segment lengths
 };
 
@@ -416,8 +418,11 @@ __device__ __forceinline__ int build_segments(const KParams &P, const int lo[3],
   int4 mine[3];
   bool has[3] = {false, false, false};
   const int t = row0 + lane;
+  int u0s = 0, u1s = 0;
   if (t < nrows) {
     const int u0 = a0 + t / R1, u1 = a1 + t % R1;
+    u0s = u0;
+    u1s = u1;
     const int g0c = max(max(lo[0] - u0, u0 - hi[0]) - 1, 0);
     const int g1c = max(max(lo[1] - u1, u1 - hi[1]) - 1, 0);
     int ext;
@@ -461,7 +466,11 @@ __device__ __forceinline__ int build_segments(const KParams &P, const int lo[3],
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const unsigned m = __ballot_sync(0xffffffffu, has[k]);
-    if (has[k]) ws.seg[base + __popc(m & lt)] = mine[k];
+    if (has[k]) {
+      const int slot = base + __popc(m & lt);
+      ws.seg[slot] = mine[k];
+      ws.segf[slot] = make_float4((float)(u0s - lo[0]), (float)(u1s - lo[1]), (float)mine[k].w, 0.f);
+    }
     base += __popc(m);
   }
   __syncwarp();
@@ -521,6 +530,14 @@ struct WarpTile32 {
   float4 pp[STAGE + 2];
   int2 meta[STAGE];  // column kernel index, segment index
 };
+
+// Hardware reciprocal square root (MUFU, ~2 ulp), flush-to-zero: callers
+// keep x >= 1e-30 so that no denormal or zero reaches it.
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
 
 __device__ __forceinline__ float sqrt_approx(float x) {
   float r;
@@ -612,7 +629,7 @@ __device__ __forceinline__ void unit_box(const KParams &P, const int4 qc, bool a
 //   pairs in the rounding band (r2lo, r2hi] are re-decided afterwards with the
 //   exact FP64 test, which is rare enough to run divergently.
 template <int POL, int KIND>
-__global__ void __launch_bounds__(WARPS_PER_CTA * 32, 8)
+__global__ void __launch_bounds__(WARPS_PER_CTA * 32, 6)
     k_pairs_mixed(KParams P) {
   __shared__ WarpSeg seg_all[WARPS_PER_CTA];
   __shared__ WarpTile32 tile_all[WARPS_PER_CTA];
@@ -642,6 +659,11 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 8)
     const float bl0 = warp_min(pq0), bh0 = warp_max(pq0);
     const float bl1 = warp_min(pq1), bh1 = warp_max(pq1);
     const float bl2 = warp_min(pq2), bh2 = warp_max(pq2);
+    // the box as centre and half-width, the half-width rounded outwards (a
+    // wider box only keeps more candidates; none within r is dropped)
+    const float bc0 = 0.5f * (bl0 + bh0), bw0 = __fadd_ru(0.5f * (bh0 - bl0), 1e-6f * (fabsf(bl0) + fabsf(bh0)));
+    const float bc1 = 0.5f * (bl1 + bh1), bw1 = __fadd_ru(0.5f * (bh1 - bl1), 1e-6f * (fabsf(bl1) + fabsf(bh1)));
+    const float bc2 = 0.5f * (bl2 + bh2), bw2 = __fadd_ru(0.5f * (bh2 - bl2), 1e-6f * (fabsf(bl2) + fabsf(bh2)));
     // rounding band: every staged coordinate lies within `span` cells of the
     // reference corner, so an FP32 offset carries < (3*span+2)*h*2^-24 error
     // and a difference of two < edx = (span+2)*h*2^-20; |d2_f32 - d2| <= band.
@@ -674,28 +696,54 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 8)
       int cur = 0;  // this lane's segment; its candidate index only grows
       for (int t0 = 0; t0 < total; t0 += STAGE) {
         int nt = 0;
+        // staging in three phases so that the global loads of every
+        // sub-round are in flight together: (1) candidate indices from the
+        // segment list, (2) positions and weights, (3) bounding-box test and
+        // compaction into shared memory
+        constexpr int NS = STAGE / 32;
+        int kk[NS], sx[NS];
+        float4 so[NS];
 #pragma unroll
-        for (int sub = 0; sub < STAGE / 32; ++sub) {
+        for (int sub = 0; sub < NS; ++sub) {
           const int t = t0 + sub * 32 + lane;
-          bool keep = false;
-          float4 st;
-          int k = 0, sidx = 0;
+          kk[sub] = -1;
+          sx[sub] = 0;
+          so[sub] = make_float4(0.f, 0.f, 0.f, 0.f);
           if (t < total) {
             while (cur + 1 < nseg && ws.off[cur + 1] <= t) ++cur;
-            sidx = cur;
-            const int4 sg = ws.seg[sidx];
-            k = sg.x + (t - ws.off[sidx]);
-            int img[3], du0, du1;
-            unpack_seg(sg.z, img, du0, du1);
-            const float4 cl = P.cloc[k];
-            st.x = fmaf((float)du0, fg.hf[0], cl.x);
-            st.y = fmaf((float)du1, fg.hf[1], cl.y);
-            st.z = fmaf((float)(__float_as_int(cl.w) + sg.w), fg.hf[2], cl.z);
-            const float e0 = fmaxf(fmaxf(bl0 - st.x, st.x - bh0), 0.f);
-            const float e1 = fmaxf(fmaxf(bl1 - st.y, st.y - bh1), 0.f);
-            const float e2 = fmaxf(fmaxf(bl2 - st.z, st.z - bh2), 0.f);
+            sx[sub] = cur;
+            kk[sub] = ws.seg[cur].x + (t - ws.off[cur]);
+            so[sub] = ws.segf[cur];
+          }
+        }
+        float4 cls[NS];
+        float bws[NS];
+#pragma unroll
+        for (int sub = 0; sub < NS; ++sub) {
+          cls[sub] = make_float4(0.f, 0.f, 0.f, 0.f);
+          bws[sub] = 0.f;
+          if (kk[sub] >= 0) {
+            cls[sub] = __ldg(&P.cloc[kk[sub]]);
+            if (POL == POL_MATVEC) bws[sub] = __ldg(&P.b32[kk[sub]]);
+          }
+        }
+#pragma unroll
+        for (int sub = 0; sub < NS; ++sub) {
+          bool keep = false;
+          float4 st;
+          const int k = kk[sub], sidx = sx[sub];
+          if (k >= 0) {
+            const float4 cl = cls[sub];
+            // offsets from the unit's reference corner: whole cells (exact
+            // small integers) times the cell size plus the in-cell offset
+            st.x = fmaf(so[sub].x, fg.hf[0], cl.x);
+            st.y = fmaf(so[sub].y, fg.hf[1], cl.y);
+            st.z = fmaf(cl.w + so[sub].z, fg.hf[2], cl.z);
+            const float e0 = fmaxf(fabsf(st.x - bc0) - bw0, 0.f);
+            const float e1 = fmaxf(fabsf(st.y - bc1) - bw1, 0.f);
+            const float e2 = fmaxf(fabsf(st.z - bc2) - bw2, 0.f);
             keep = fmaf(e2, e2, fmaf(e1, e1, e0 * e0)) <= r2box;
-            if (keep) st.w = (POL == POL_MATVEC) ? P.b32[k] : 0.f;
+            st.w = bws[sub];
           }
           const unsigned km = __ballot_sync(0xffffffffu, keep);
           if (WCUT) {
@@ -721,8 +769,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 8)
         if (WCUT) {
           // pairs for the packed loop; an odd tail is paired with a far-away
           // candidate of weight 0 (the clamp zeroes it)
-          const int h = lane;
-          if (2 * h < nt) {
+          for (int h = lane; 2 * h < nt; h += 32) {
             const float4 c0 = sm.p[2 * h];
             const float4 c1 = 2 * h + 1 < nt ? sm.p[2 * h + 1] : make_float4(1e4f, 1e4f, 1e4f, 0.f);
             sm.pp[2 * h] = make_float4(c0.x, c1.x, c0.y, c1.y);
@@ -746,21 +793,23 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 8)
                        nqz = make_float2(-pq2 * sc, -pq2 * sc);
           float2 acc2 = make_float2(0.f, 0.f);
           const int npair = (nt + 1) >> 1;
-#pragma unroll 2
+#pragma unroll 8
           for (int h = 0; h < npair; ++h) {
             const float4 A = sm.pp[2 * h], B = sm.pp[2 * h + 1];
             const float2 dx = __fadd2_rn(make_float2(A.x, A.y), nqx);
             const float2 dy = __fadd2_rn(make_float2(A.z, A.w), nqy);
             const float2 dz = __fadd2_rn(make_float2(B.x, B.y), nqz);
-            float2 dd = __fmul2_rn(dx, dx);
+            // d^2 (+1e-30, so that rsqrt stays finite for the self pair)
+            float2 dd = __ffma2_rn(dx, dx, make_float2(1e-30f, 1e-30f));
             dd = __ffma2_rn(dy, dy, dd);
             dd = __ffma2_rn(dz, dz, dd);
-            const float2 q = make_float2(sqrt_approx(dd.x), sqrt_approx(dd.y));
-            float2 t = __ffma2_rn(q, make_float2(-1.f, -1.f), make_float2(1.f, 1.f));
-            t.x = fmaxf(t.x, 0.f);
-            t.y = fmaxf(t.y, 0.f);
+            const float2 rs = make_float2(rsqrt_approx(dd.x), rsqrt_approx(dd.y));
+            // t = max(1 - q, 0), q = d^2 / d, as saturating FMAs (q >= 0, so
+            // [0,1] is the clamp); then 4q + 1 = 5 - 4t wherever t > 0
+            const float2 t = make_float2(__saturatef(fmaf(-dd.x, rs.x, 1.f)),
+                                         __saturatef(fmaf(-dd.y, rs.y, 1.f)));
             const float2 t2 = __fmul2_rn(t, t);
-            const float2 pw = __ffma2_rn(q, make_float2(4.f, 4.f), make_float2(1.f, 1.f));
+            const float2 pw = __ffma2_rn(t, make_float2(-4.f, -4.f), make_float2(5.f, 5.f));
             const float2 t4 = __fmul2_rn(t2, t2);
             acc2 = __ffma2_rn(__fmul2_rn(t4, pw), make_float2(B.z, B.w), acc2);
           }
