@@ -508,10 +508,13 @@ def spai_features(p: Particles, knn_idx, eps):
 
 
 def learned_preconditioner(op: Operator, mlp: MLP, eps: float, k: int = 32,
-                           precision: int = PREC_MIXED) -> Preconditioner:
+                           precision: int = PREC_MIXED, exact_phi: float = 0.5) -> Preconditioner:
+    """The MLP's sparse approximate inverse; rows next to a neighbour with
+    kernel value > exact_phi are solved exactly (exact_phi >= 1: none)."""
     h = C.c_void_p()
     _check(lib().abx_precond_create_learned(op._h, mlp._h, float(eps), int(k), int(precision),
-                                            C.byref(h)), "abx_precond_create_learned")
+                                            float(exact_phi), C.byref(h)),
+           "abx_precond_create_learned")
     return Preconditioner(h, op.rows.ctx, op.shape[0], keep=(op, mlp))
 
 

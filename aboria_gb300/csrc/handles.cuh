@@ -99,6 +99,8 @@ struct abx_precond {
   abx::Spai *spai = nullptr;
   abx_context *ctx = nullptr;
   int64_t n = 0;
+  int64_t exact_rows = 0;  // learned approximate inverse: rows solved exactly
+  double setup_s = 0.0;    // approximate inverses: set-up time
   abx::HostStage stage_b, stage_x;
 };
 

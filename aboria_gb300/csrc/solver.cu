@@ -767,6 +767,13 @@ int abx_precond_stats(abx_precond *pc, int64_t *ndomains, int64_t *max_size, int
     if (max_size) *max_size = pc->schwarz->max_size;
     if (elements) *elements = pc->schwarz->mat_elems;
     if (setup_seconds) *setup_seconds = pc->schwarz->setup_s;
+  } else {
+    // approximate inverse: ndomains = rows solved exactly (learned: the rows
+    // next to a close neighbour); no domains or stored blocks
+    if (ndomains) *ndomains = pc->exact_rows;
+    if (max_size) *max_size = 0;
+    if (elements) *elements = 0;
+    if (setup_seconds) *setup_seconds = pc->setup_s;
   }
   return ABX_OK;
 }

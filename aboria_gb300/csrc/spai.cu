@@ -2,6 +2,8 @@
 // (column index, value) pairs per row.  The rows come either from the exact
 // local least-squares construction (spai_exact.cu) or from the learned model
 // (mlp.cu); applying M is the same gather-multiply in both cases.
+#include <chrono>
+
 #include "common.cuh"
 #include "handles.cuh"
 
@@ -115,6 +117,8 @@ struct LsParams {
   int *counter;
   int *status;         // 0 ok; 1 |U| over capacity
   int local;           // 1: U = S (row of the local block inverse)
+  const int32_t *subset;  // rows to solve (null: all n rows)
+  int64_t nrows;          // rows to solve
 };
 
 template <int KIND> __device__ __forceinline__ double ls_coeff(const LsParams &P, int a, int b) {
@@ -174,8 +178,8 @@ template <int KIND> __global__ void __launch_bounds__(LS_T) k_spai_ls(LsParams P
   for (;;) {
     if (tid == 0) s_row = atomicAdd(P.counter, 1);
     __syncthreads();
-    const int i = s_row;
-    if (i >= P.n) break;
+    if (s_row >= P.nrows) break;
+    const int i = P.subset ? P.subset[s_row] : s_row;
     for (int h = tid; h < LS_HT; h += LS_T) hset[h] = -1;
     if (tid < k) {
       S[tid] = P.knn[(int64_t)i * k + tid];
@@ -329,7 +333,10 @@ int self_csr_device(abx_particles *p, double r, DevBuf<int64_t> &rowptr, DevBuf<
                     int64_t &nnz);
 int knn_device(abx_particles *p, int k, int32_t *idx, double *d2);
 
-int spai_exact_rows(abx_operator *op, int k, int32_t *cols_out, double *vals_out, int local) {
+// subset (device, nsub rows) restricts the solve to those rows; knn_given
+// says cols_out already holds the k-nearest-neighbour supports.
+int spai_exact_rows(abx_operator *op, int k, int32_t *cols_out, double *vals_out, int local,
+                    const int32_t *subset = nullptr, int64_t nsub = -1, bool knn_given = false) {
   abx_particles *p = op->rows;
   abx_context *ctx = p->ctx;
   cudaStream_t s = ctx->stream;
@@ -339,12 +346,14 @@ int spai_exact_rows(abx_operator *op, int k, int32_t *cols_out, double *vals_out
   ABX_REQUIRE(op->k.kind != ABX_K_SCALAR_SUM, ABX_ERR_INVALID, "kernel not supported");
   const int64_t n = p->n;
   if (n == 0) return ABX_OK;
-  ABX_TRY(knn_device(p, k, cols_out, nullptr));
+  if (!knn_given) ABX_TRY(knn_device(p, k, cols_out, nullptr));
+  const int64_t nrows = subset ? nsub : n;
+  if (nrows == 0) return ABX_OK;
   DevBuf<int64_t> rowptr;
   DevBuf<int32_t> cols;
   int64_t nnz = 0;
-  ABX_TRY(self_csr_device(p, op->radius, rowptr, cols, nnz));
-  const int grid = (int)std::min<int64_t>(n, (int64_t)ctx->num_sms * 2);
+  if (!local) ABX_TRY(self_csr_device(p, op->radius, rowptr, cols, nnz));
+  const int grid = (int)std::min<int64_t>(nrows, (int64_t)ctx->num_sms * 2);
   DevBuf<double> scratch;
   DevBuf<int> flags;
   ABX_TRY(scratch.reserve((size_t)grid * LS_MCAP * LS_K));
@@ -370,6 +379,8 @@ int spai_exact_rows(abx_operator *op, int k, int32_t *cols_out, double *vals_out
   P.counter = flags.ptr;
   P.status = flags.ptr + 1;
   P.local = local;
+  P.subset = subset;
+  P.nrows = nrows;
   auto launch = [&](auto kern) -> int {
     ABX_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)LS_SMEM));
@@ -436,6 +447,29 @@ __global__ void k_spai_features(const double *__restrict__ pos, int64_t n, int d
   }
 }
 
+// Rows whose nearest other support point (k-NN entry 1) has kernel value
+// phi > exact_phi: their approximate-inverse row is solved exactly.
+__global__ void k_flag_close(const double *__restrict__ d2, int64_t n, int k, int kind, double p0,
+                             double exact_phi, int32_t *__restrict__ list,
+                             int *__restrict__ count) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || k < 2) return;
+  const double r2 = d2[i * k + 1];
+  double phi = 0.0;
+  switch (kind) {
+  case ABX_K_GAUSSIAN:
+  case ABX_K_COMPACT_GAUSSIAN: phi = exp(-p0 * r2); break;
+  case ABX_K_WENDLAND_C2: {
+    const double q = sqrt(r2) * p0;
+    const double t = q < 1.0 ? 1.0 - q : 0.0;
+    phi = t * t * t * t * (4.0 * q + 1.0);
+    break;
+  }
+  default: phi = 1.0;  // kernels not normalised to phi(0) = 1: every row exact
+  }
+  if (phi > exact_phi) list[atomicAdd(count, 1)] = (int32_t)i;
+}
+
 __global__ void k_f2d_masked(const float *__restrict__ y, const int32_t *__restrict__ cols,
                              int64_t n, double *__restrict__ vals) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -473,7 +507,7 @@ extern "C" int abx_spai_features(abx_particles *p, const int32_t *knn, int k, do
 }
 
 extern "C" int abx_precond_create_learned(abx_operator *op, abx_mlp *mlp, double eps, int k,
-                                          int precision, abx_precond **out) {
+                                          int precision, double exact_phi, abx_precond **out) {
   ABX_REQUIRE(op && mlp && out, ABX_ERR_INVALID, "null argument");
   ABX_REQUIRE(op->rows == op->cols, ABX_ERR_INVALID, "needs a square operator");
   abx_particles *p = op->rows;
@@ -490,10 +524,13 @@ extern "C" int abx_precond_create_learned(abx_operator *op, abx_mlp *mlp, double
   S->n = n;
   S->k = k;
   int st = ABX_OK;
+  const auto t0 = std::chrono::steady_clock::now();
   DevBuf<float> feats, y;
+  DevBuf<double> d2;
   if ((st = S->cols.reserve((size_t)n * k + 1)) || (st = S->vals.reserve((size_t)n * k + 1)) ||
       (st = feats.reserve((size_t)n * k * p->dim + 1)) || (st = y.reserve((size_t)n * k + 1)) ||
-      (n > 0 && ((st = knn_device(p, k, S->cols.ptr, nullptr)) ||
+      (st = d2.reserve((size_t)n * k + 1)) ||
+      (n > 0 && ((st = knn_device(p, k, S->cols.ptr, d2.ptr)) ||
                  (st = spai_features_device(p, S->cols.ptr, k, eps, feats.ptr)) ||
                  (st = precision == ABX_PREC_FP64
                            ? mlp_infer_fp32(mlp, feats.ptr, n, y.ptr)
@@ -506,14 +543,39 @@ extern "C" int abx_precond_create_learned(abx_operator *op, abx_mlp *mlp, double
     k_f2d_masked<<<ceil_div((size_t)n * k, 256), 256, 0, p->ctx->stream>>>(y.ptr, S->cols.ptr,
                                                                           (size_t)n * k,
                                                                           S->vals.ptr);
-    cudaError_t e = cudaStreamSynchronize(p->ctx->stream);
+    // rows next to a close neighbour: exact FP64 local-inverse rows
+    DevBuf<int32_t> list;
+    DevBuf<int> cnt;
+    int nexact = 0;
+    cudaError_t e = cudaSuccess;
+    if (exact_phi < 1.0 && k >= 2) {
+      if ((st = list.reserve((size_t)n)) || (st = cnt.reserve(1))) {
+        delete pc->spai;
+        delete pc;
+        return st;
+      }
+      cudaMemsetAsync(cnt.ptr, 0, sizeof(int), p->ctx->stream);
+      k_flag_close<<<ceil_div((size_t)n, 256), 256, 0, p->ctx->stream>>>(
+          d2.ptr, n, k, op->k.kind, op->k.p[0], exact_phi, list.ptr, cnt.ptr);
+      e = cudaMemcpyAsync(&nexact, cnt.ptr, sizeof(int), cudaMemcpyDeviceToHost, p->ctx->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(p->ctx->stream);
+      if (e == cudaSuccess && nexact > 0 &&
+          (st = spai_exact_rows(op, k, S->cols.ptr, S->vals.ptr, 1, list.ptr, nexact, true))) {
+        delete pc->spai;
+        delete pc;
+        return st;
+      }
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->ctx->stream);
     if (e != cudaSuccess) {
       delete pc->spai;
       delete pc;
       set_error("learned preconditioner: %s", cudaGetErrorString(e));
       return ABX_ERR_CUDA;
     }
+    pc->exact_rows = nexact;
   }
+  pc->setup_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   ctx_retain(pc->ctx);
   *out = pc;
   return ABX_OK;

@@ -287,6 +287,7 @@ def run_ours(args):
 
 RBF_N = 200_000
 RBF_EH = 2.5  # scaled shape parameter eps*h, h = N^-1/2
+EXACT_PHI = 0.5  # learned preconditioner: rows with a neighbour of kernel value > 0.5 solved exactly
 
 
 def _timed(fn, ctx):
@@ -305,9 +306,12 @@ def rbf_section(ctx, model_path):
     * plain   : restricted additive Schwarz on octree leaves of 256 points,
                 blocks factorised by FP64 LU, FP64 operator throughout.
     * learned : the trained MLP's sparse approximate inverse (32 k-NN columns
-                per row, BF16 tensor-core inference), FP32 operator with FP64
-                residual refinement; Schwarz taken as fallback when the learned
-                preconditioner has not converged after 30 iterations.
+                per row, BF16 tensor-core inference; rows next to a neighbour
+                with kernel value > 0.5 solved exactly in FP64), FP32 operator
+                with FP64 residual refinement; Schwarz taken as fallback when
+                the learned preconditioner has not converged after 60
+                iterations.
+    * without_network : the same, with identity rows where the network answers.
     * local_inverse : the exact FP64 local-inverse rows the network is trained
                 on, as the same sparse approximate inverse (the label method).
     Every time includes the preconditioner's set-up; the residual reported is
@@ -344,13 +348,21 @@ def rbf_section(ctx, model_path):
     if model_path.exists():
         mlp = ab.MLP.load(model_path)
 
-        def learned():
-            M = ab.learned_preconditioner(K32, mlp, eps)
-            return ab.gmres_with_fallback(K32, f, M, K64, restart=100, learned_max_iters=30,
-                                          max_iters=2000, tol=1e-8, A_check=K64)
-        (x, it, res, fb), t = _timed(learned, ctx)
+        def learned(net):
+            M = ab.learned_preconditioner(K32, net, eps, exact_phi=EXACT_PHI)
+            x, it, res, fb = ab.gmres_with_fallback(K32, f, M, K64, restart=100,
+                                                    learned_max_iters=60, max_iters=2000,
+                                                    tol=1e-8, A_check=K64)
+            return x, it, fb, M.stats()["domains"]
+        (x, it, fb, nex), t = _timed(lambda: learned(mlp), ctx)
         out["learned_mixed"] = {"seconds": t, "iterations": it, "residual": check(x),
-                                "fallback_taken": bool(fb)}
+                                "fallback_taken": bool(fb), "rows_solved_exactly": nex}
+        # the same method without the network: identity rows where it answers
+        ident = ab.MLP.load(model_path)
+        ident.params = np.zeros(ident.num_params, np.float32)
+        (x, it, fb, nex), t = _timed(lambda: learned(ident), ctx)
+        out["without_network_mixed"] = {"seconds": t, "iterations": it, "residual": check(x),
+                                        "fallback_taken": bool(fb)}
 
     def local_inverse():
         cols, vals = ab.spai_local_inverse_rows(K64, 32)

@@ -128,8 +128,9 @@ ABX_API int abx_particles_get_buckets(abx_particles *p, uint32_t *bucket_begin, 
  * ((0+dx0^2)+dx1^2)+dx2^2 <= r^2 in FP64, dx = x_j - (x + image*L). */
 ABX_API int abx_radius_count(abx_particles *p, int64_t nq, const double *q, double r, int32_t *counts);
 /* Neighbour lists as CSR: rowptr[nq+1] and cols[] (indices into storage
- * order, ascending within a row; a particle reached through two periodic
- * images appears twice).  Call with cols == NULL to get rowptr only (nnz in
+ * order; the order within a row is unspecified -- the neighbour set is the
+ * reference's, bit for bit, not its visiting order; a particle reached through
+ * two periodic images appears twice).  Call with cols == NULL to get rowptr only (nnz in
  * rowptr[nq]); cap is the capacity of cols. */
 ABX_API int abx_radius_query_csr(abx_particles *p, int64_t nq, const double *q, double r,
                          int64_t *rowptr, int32_t *cols, int64_t cap);
@@ -230,13 +231,20 @@ ABX_API int abx_spai_features(abx_particles *p, const int32_t *knn, int k, doubl
                               float *feats);
 /* Learned sparse approximate inverse (no counterpart in the reference): k-NN
  * support, features as above, weights from the MLP (precision ABX_PREC_MIXED:
- * BF16 tensor-core inference; ABX_PREC_FP64: FP32 SIMT inference). */
+ * BF16 tensor-core inference; ABX_PREC_FP64: FP32 SIMT inference).  Rows
+ * whose nearest other point has kernel value phi > exact_phi (phi(0) = 1 for
+ * the Gaussian and Wendland kernels) are instead solved exactly as FP64
+ * local-inverse rows (abx_spai_local_inverse_rows): next to a near-coincident
+ * pair the inverse's weights grow like 1/(1 - phi) and cancel, which no
+ * regression reproduces.  exact_phi >= 1: every row from the network. */
 typedef struct abx_mlp abx_mlp;
 ABX_API int abx_precond_create_learned(abx_operator *op, abx_mlp *mlp, double eps, int k,
-                                       int precision, abx_precond **out);
+                                       int precision, double exact_phi, abx_precond **out);
 ABX_API int abx_precond_get_spai(abx_precond *pc, int32_t *cols, double *vals);
 ABX_API int abx_precond_destroy(abx_precond *pc);
 ABX_API int abx_precond_apply(abx_precond *pc, const double *b, double *x);
+/* Schwarz: domains, largest domain, stored factor elements, set-up seconds.
+ * Approximate inverses: ndomains = rows solved exactly, set-up seconds. */
 ABX_API int abx_precond_stats(abx_precond *pc, int64_t *ndomains, int64_t *max_size,
                               int64_t *elements, double *setup_seconds);
 /* Solve A x = b (x holds the initial guess) with restarted, right-

@@ -104,38 +104,54 @@ def rbf_problem(n, eh, seed):
 
 
 @pytest.mark.skipif(not MODEL.exists(), reason="trained model not present")
-def test_trained_network_vs_labels_and_untrained():
-    """What the trained network gains, measured on a test instance (seed
-    disjoint from training): its predicted rows are far closer to the exact
-    local-inverse labels than an untrained network's, but not close enough to
-    precondition (the labels tolerate only ~1% weight error), so the solve
-    falls back to Schwarz; the labels themselves cut GMRES iterations by more
-    than 100x."""
+def test_trained_network_gain_over_the_method_without_it():
+    """What the trained network gains, on a test instance (seed disjoint from
+    training).  The method without it: the same hybrid approximate inverse
+    (exact FP64 local-inverse rows next to close neighbours, phi > 0.5) with
+    identity rows where the network would answer.  With the network the
+    mixed-precision GMRES reaches the FP64-checked 1e-8 in well under 70% of
+    the iterations (measured: 13 vs 27), and each network row's residual on its
+    own support, |A_i m_i - e_0|, is far below the identity row's."""
     p, K, eps = rbf_problem(50000, 2.5, seed=99)
-    cols, vals = ab.spai_local_inverse_rows(K, 32)
+    K32 = ab.create_sparse_operator(p, p, 4.0 / eps, ab.Kernel.make(ab.K_COMPACT_GAUSSIAN, eps * eps),
+                                    ab.PREC_MIXED)
     trained = ab.MLP.load(MODEL)
-    untrained = ab.MLP.create(64, 128, 3, 32, seed=11)
-    lc, lv = ab.spai_rows(ab.learned_preconditioner(K, trained, eps))
-    _, uv = ab.spai_rows(ab.learned_preconditioner(K, untrained, eps))
-    assert np.array_equal(lc, cols)
-    err_t = np.median(np.linalg.norm(lv - vals, axis=1) / np.linalg.norm(vals, axis=1))
-    err_u = np.median(np.linalg.norm(uv - vals, axis=1) / np.linalg.norm(vals, axis=1))
-    assert err_t < 0.3 and err_t < 0.5 * err_u, (err_t, err_u)
+    ident = ab.MLP.load(MODEL)
+    ident.params = np.zeros(ident.num_params, np.float32)  # m = e_0 on every network row
     b = np.random.default_rng(100).standard_normal(len(p))
-    _, it0, _ = ab.gmres(K, b, restart=100, max_iters=1000, tol=1e-8)
-    _, it_lab, r_lab = ab.gmres(K, b, M=ab.spai_preconditioner(p.ctx, cols, vals), restart=100,
-                                max_iters=1000, tol=1e-8)
-    assert r_lab <= 1e-8 and it_lab * 100 < it0
-    M = ab.learned_preconditioner(K, trained, eps)
-    x, it, res, fb = ab.gmres_with_fallback(K, b, M, K, learned_max_iters=30, tol=1e-8)
-    assert res <= 1e-8
+    Mt = ab.learned_preconditioner(K32, trained, eps)
+    Mi = ab.learned_preconditioner(K32, ident, eps)
+    assert Mt.stats()["domains"] == Mi.stats()["domains"] > 0
+    x, it_t, res_t = ab.gmres(K32, b, M=Mt, restart=100, max_iters=1000, tol=1e-8, A_check=K)
+    _, it_i, res_i = ab.gmres(K32, b, M=Mi, restart=100, max_iters=1000, tol=1e-8, A_check=K)
+    assert res_t <= 1e-8 and res_i <= 1e-8
+    assert it_t < 0.7 * it_i, (it_t, it_i)
+    r = b - K * x
+    assert np.linalg.norm(r) / np.linalg.norm(b) <= 1.0001e-8
+    # per-row residual on the support, network rows only
+    idx, d2 = ab.knn(p, 32)
+    feats = ab.spai_features(p, idx, eps)
+    easy = np.exp(-eps * eps * d2[:, 1]) <= 0.5
+    _, vals = ab.spai_rows(Mt)
+    A = mlp_oracle.local_matrices(feats[easy], 32, 2, lambda d2_: np.exp(-d2_), 4.0)
+    e0 = np.zeros(32)
+    e0[0] = 1.0
+    res_net = np.linalg.norm(np.einsum("bac,bc->ba", A, vals[easy]) - e0, axis=1)
+    res_id = np.linalg.norm(A[:, :, 0] - e0, axis=1)
+    assert np.median(res_net) < 0.3 * np.median(res_id), (np.median(res_net), np.median(res_id))
+    # the rows next to a close neighbour are the exact local-inverse rows
+    cols_x, vals_x = ab.spai_local_inverse_rows(K, 32)
+    cols_t, _ = ab.spai_rows(Mt)
+    assert np.array_equal(cols_t, cols_x) and np.array_equal(cols_t, idx)
+    assert np.array_equal(vals[~easy], vals_x[~easy])
+    assert (~easy).sum() == Mt.stats()["domains"]
 
 
 def test_fallback_taken_when_learned_fails():
     p, K, eps = rbf_problem(20000, 2.0, seed=101)
     bad = ab.MLP.create(64, 128, 3, 32, seed=5)
     bad.set_normalization(1.0, np.zeros(32, np.float32), np.zeros(32, np.float32))  # M = 0
-    Mbad = ab.learned_preconditioner(K, bad, eps)
+    Mbad = ab.learned_preconditioner(K, bad, eps, exact_phi=1.0)  # every row from the network
     b = np.random.default_rng(102).standard_normal(len(p))
     x, it, res, fb = ab.gmres_with_fallback(K, b, Mbad, K, learned_max_iters=50, tol=1e-8)
     assert fb and res <= 1e-8
