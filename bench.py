@@ -511,7 +511,20 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--matvec-only", action="store_true",
                     help="skip the RBF-solve and FMM sections (profiling runs)")
+    ap.add_argument("--only", choices=["fmm", "rbf"],
+                    help="run one secondary section alone and print it (profiling runs)")
     args = ap.parse_args()
+    if args.only:
+        import torch
+        import aboria_gb300 as ab
+        torch.cuda.set_device(0)
+        stream = torch.cuda.Stream()
+        torch.cuda.set_stream(stream)  # events and library calls on one stream
+        ctx = ab.Context(0, stream=stream.cuda_stream)
+        sec = (fmm_section(ctx) if args.only == "fmm"
+               else rbf_section(ctx, ROOT / "aboria_gb300" / "models" / "spai_mlp_2d.bin"))
+        print(json.dumps({"section": args.only, **sec}))
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
