@@ -69,6 +69,8 @@ struct FmmPlan {
   double build_s = 0.0;
   double chebsetup_s = 0.0;
   DevBuf<float> W32, G32;
+  DevBuf<float4> posf;  // mixed near field: FP32 position relative to the leaf centre
+  DevBuf<float> b32;    // mixed near field: FP32 weights of the current matvec
   DevBuf<int> mi_d;                 // ncheb x 3 multi-indices
   DevBuf<int> tile_mat, tile_first; // tensor-core M2L tiles
   int ntiles = 0;
@@ -407,6 +409,129 @@ __global__ void __launch_bounds__(FT) k_l2p_p2p(int D, int n, int ncheb, const i
   }
 }
 
+// FP32 position of every particle relative to the centre of its leaf: the
+// mixed-precision near field works on these small offsets (and on the
+// leaf-to-leaf centre offsets), never on absolute FP32 coordinates.
+__global__ void k_leaf_rel(int D, const int *__restrict__ leaves, const int *__restrict__ nb,
+                           const int *__restrict__ ne, const double *__restrict__ box,
+                           const double *__restrict__ pos, int64_t npos,
+                           float4 *__restrict__ posf) {
+  const int leaf = leaves[blockIdx.x];
+  const double *bx = box + (size_t)leaf * 6;
+  for (int i = nb[leaf] + threadIdx.x; i < ne[leaf]; i += blockDim.x) {
+    float v[3] = {0.f, 0.f, 0.f};
+    for (int d = 0; d < D; ++d)
+      v[d] = (float)(pos[(int64_t)d * npos + i] - 0.5 * (bx[d] + bx[3 + d]));
+    posf[i] = make_float4(v[0], v[1], v[2], 0.f);
+  }
+}
+
+__device__ __forceinline__ float rsqrt_approx_f(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float rcp_approx_f(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// FP32 kernel value of the mixed near field.  Laplace 1/(|dx| + p0) from the
+// hardware reciprocal square root and reciprocal (~2 ulp each): |dx| =
+// d2 * rsqrt(d2 + 1e-30), which is 0 at d2 = 0.
+template <int KIND> __device__ __forceinline__ float p2p_k32(float d2, float p0) {
+  if (KIND == ABX_K_LAPLACE) return rcp_approx_f(fmaf(d2, rsqrt_approx_f(d2 + 1e-30f), p0));
+  return fmm_k32<KIND>(d2, p0);
+}
+
+constexpr int PT = 64;  // threads per target leaf in the mixed near field
+
+// Mixed-precision L2P + P2P: one CTA per target leaf, one thread per target.
+// L2P in FP64 as in the FP64 kernel; each source leaf of the near field is
+// staged in shared memory as FP32 offsets from the target leaf's centre
+// (leaf-relative FP32 position + FP32 centre offset), the pair terms are FP32
+// with a staged chunk (<= 64 terms) summed in FP32 and chunks summed in
+// FP64.  The self pair (a regularised singular kernel is huge there) is
+// masked out of the FP32 sum and added in FP64.
+template <int KIND>
+__global__ void __launch_bounds__(PT) k_l2p_p2p32(
+    int D, int n, int ncheb, const int *__restrict__ leaves, const int *__restrict__ nb,
+    const int *__restrict__ ne, const double *__restrict__ box, const double *__restrict__ pos,
+    int64_t npos, const float4 *__restrict__ posf, const float *__restrict__ b32,
+    const double *__restrict__ b, const int *__restrict__ mi, const double *__restrict__ G,
+    const int *__restrict__ rp, const int *__restrict__ src, double p0, double *__restrict__ c) {
+  __shared__ double sg[MAXC];
+  __shared__ float4 ss[PT];
+  const int tid = threadIdx.x;
+  const int li = blockIdx.x;
+  const int leaf = leaves[li];
+  const double *bx = box + (size_t)leaf * 6;
+  double ct[3] = {0.0, 0.0, 0.0};
+  for (int d = 0; d < D; ++d) ct[d] = 0.5 * (bx[d] + bx[3 + d]);
+  for (int j = tid; j < ncheb; j += PT) sg[j] = G[(size_t)leaf * ncheb + j];
+  __syncthreads();
+  const float p0f = (float)p0;
+  for (int i0 = nb[leaf]; i0 < ne[leaf]; i0 += PT) {
+    const int i = i0 + tid;
+    const bool act = i < ne[leaf];
+    double acc = 0.0;
+    float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (act) {
+      double xi[3] = {0, 0, 0};
+      for (int d = 0; d < D; ++d) xi[d] = pos[(int64_t)d * npos + i];
+      double S[3][MAXN];
+      for (int d = 0; d < D; ++d) cheb_sn(shift_coord(xi[d], bx[d], bx[3 + d]), n, S[d]);
+      for (int j = 0; j < ncheb; ++j) {
+        double r = sg[j];
+        for (int d = 0; d < D; ++d) r *= S[d][mi[j * 3 + d]];
+        acc += r;
+      }
+      t = posf[i];
+    }
+    for (int e = rp[li]; e < rp[li + 1]; ++e) {
+      const int sl = src[e];
+      const double *sbx = box + (size_t)sl * 6;
+      float off[3] = {0.f, 0.f, 0.f};
+      for (int d = 0; d < D; ++d) off[d] = (float)(0.5 * (sbx[d] + sbx[3 + d]) - ct[d]);
+      const bool own = sl == leaf;
+      for (int j0 = nb[sl]; j0 < ne[sl]; j0 += PT) {
+        __syncthreads();
+        const int j = j0 + tid;
+        if (j < ne[sl]) {
+          const float4 q = posf[j];
+          ss[tid] = make_float4(q.x + off[0], q.y + off[1], q.z + off[2], b32[j]);
+        }
+        __syncthreads();
+        const int cnt = min(PT, ne[sl] - j0);
+        if (act) {
+          float a = 0.f;
+          if (own) {
+            for (int q = 0; q < cnt; ++q) {
+              const float4 sq = ss[q];
+              const float dx = sq.x - t.x, dy = sq.y - t.y, dz = sq.z - t.z;
+              const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+              const float w = j0 + q == i ? 0.f : p2p_k32<KIND>(d2, p0f);
+              a = fmaf(w, sq.w, a);
+            }
+            if (i >= j0 && i < j0 + cnt) acc += fmm_k64<KIND>(0.0, p0) * b[i];
+          } else {
+#pragma unroll 4
+            for (int q = 0; q < cnt; ++q) {
+              const float4 sq = ss[q];
+              const float dx = sq.x - t.x, dy = sq.y - t.y, dz = sq.z - t.z;
+              const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+              a = fmaf(p2p_k32<KIND>(d2, p0f), sq.w, a);
+            }
+          }
+          acc += (double)a;
+        }
+      }
+    }
+    if (act) c[i] = acc;
+  }
+}
+
 // M2L matrices: for each (level box size, offset) K[i][j] = kernel(x_i^t, x_j^s)
 template <int KIND>
 __global__ void k_m2l_mats(int D, int n, int ncheb, const double *__restrict__ mat_desc,
@@ -672,6 +797,11 @@ int fmm_plan_build(abx_operator *op, int order, FmmPlan *&out) {
       return fail(ABX_ERR_INVALID);
     }
   }
+  if (P->nleaves > 0) {
+    if ((st = P->posf.reserve((size_t)std::max<int64_t>(op->rows->n, 1)))) return fail(st);
+    k_leaf_rel<<<P->nleaves, FT, 0, s>>>(D, P->leaf_ids.ptr, P->node_begin.ptr, P->node_end.ptr,
+                                          P->box.ptr, op->rows->pos.ptr, op->rows->n, P->posf.ptr);
+  }
   if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
     set_error("FMM plan upload failed");
     return fail(ABX_ERR_CUDA);
@@ -686,11 +816,14 @@ namespace {
 template <int KIND>
 int launch_l2p_p2p(FmmPlan *P, cudaStream_t s, const double *pos, int64_t npos, const double *b,
                    double *c, bool mixed) {
-  if (mixed)
-    k_l2p_p2p<KIND, true><<<P->nleaves, FT, 0, s>>>(
+  if (mixed) {
+    ABX_TRY(P->b32.reserve((size_t)npos));
+    k_f64_to_f32<<<ceil_div((size_t)npos, 256), 256, 0, s>>>(b, npos, P->b32.ptr);
+    k_l2p_p2p32<KIND><<<P->nleaves, PT, 0, s>>>(
         P->D, P->n, P->ncheb, P->leaf_ids.ptr, P->node_begin.ptr, P->node_end.ptr, P->box.ptr, pos,
-        npos, b, P->mi_d.ptr, P->G.ptr, P->p2p_rowptr.ptr, P->p2p_src.ptr, P->p0, c);
-  else
+        npos, P->posf.ptr, P->b32.ptr, b, P->mi_d.ptr, P->G.ptr, P->p2p_rowptr.ptr,
+        P->p2p_src.ptr, P->p0, c);
+  } else
     k_l2p_p2p<KIND, false><<<P->nleaves, FT, 0, s>>>(
         P->D, P->n, P->ncheb, P->leaf_ids.ptr, P->node_begin.ptr, P->node_end.ptr, P->box.ptr, pos,
         npos, b, P->mi_d.ptr, P->G.ptr, P->p2p_rowptr.ptr, P->p2p_src.ptr, P->p0, c);
