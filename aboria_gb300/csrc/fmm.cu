@@ -35,6 +35,13 @@
 
 namespace abx {
 
+constexpr int MAXN_TAB = 8;  // max Chebyshev order of the coefficient table
+
+// Clenshaw coefficients of S_m: c[m][k] = (2/n) cos(k (2m+1) pi / (2n)).
+struct ChebTab {
+  double c[MAXN_TAB][MAXN_TAB];
+};
+
 struct FmmPlan {
   int D = 3, n = 3, ncheb = 27, nchild = 8;
   int nnodes = 0;
@@ -69,6 +76,7 @@ struct FmmPlan {
   double build_s = 0.0;
   double chebsetup_s = 0.0;
   DevBuf<float> W32, G32;
+  ChebTab tab{};        // Clenshaw coefficients of the order
   DevBuf<float4> posf;  // mixed near field: FP32 position relative to the leaf centre
   DevBuf<float> b32;    // mixed near field: FP32 weights of the current matvec
   DevBuf<int> mi_d;                 // ncheb x 3 multi-indices
@@ -97,6 +105,32 @@ __host__ __device__ inline void cheb_sn(double x, int n, double *S) {
 }
 
 __host__ __device__ inline double cheb_node(int m, int n) { return cos((2.0 * m + 1.0) * PI / (2.0 * n)); }
+
+// The Clenshaw coefficients of S_m (ChebTab, declared with the plan),
+// computed once on the host (the same std::cos values as the host-side
+// recurrence above) and passed by value, so that no kernel evaluates cos.
+inline ChebTab cheb_table(int n) {
+  ChebTab t{};
+  const double invn = 1.0 / n;
+  for (int m = 0; m < n; ++m)
+    for (int k = 1; k < n; ++k) t.c[m][k] = 2 * invn * cos(k * (2.0 * m + 1.0) * (PI / 2) * invn);
+  return t;
+}
+
+// S_m(x), m = 0..n-1, with the tabulated coefficients: the same recurrence
+// as cheb_sn.
+__device__ __forceinline__ void cheb_sn_tab(double x, int n, const ChebTab &t, double *S) {
+  const double invn = 1.0 / n;
+  for (int m = 0; m < n; ++m) {
+    double b1 = 0.0, b2 = 0.0;
+    for (int k = n - 1; k >= 1; --k) {
+      const double bk = t.c[m][k] + 2.0 * x * b1 - b2;
+      b2 = b1;
+      b1 = bk;
+    }
+    S[m] = invn + x * b1 - b2;
+  }
+}
 
 __host__ __device__ inline double shift_coord(double p, double lo, double hi) {
   const double span = hi - lo;
@@ -129,7 +163,7 @@ __global__ void __launch_bounds__(FT) k_p2m(int D, int n, int ncheb, const int *
                                             const double *__restrict__ box,
                                             const double *__restrict__ pos, int64_t npos,
                                             const double *__restrict__ b, const int *__restrict__ mi,
-                                            double *__restrict__ W) {
+                                            const ChebTab tab, double *__restrict__ W) {
   __shared__ double S[FT][MAXN * 3];
   __shared__ double sb[FT];
   const int leaf = leaves[blockIdx.x];
@@ -141,7 +175,7 @@ __global__ void __launch_bounds__(FT) k_p2m(int D, int n, int ncheb, const int *
     if (i < ne[leaf]) {
       for (int d = 0; d < D; ++d) {
         const double x = shift_coord(pos[(int64_t)d * npos + i], bx[d], bx[3 + d]);
-        cheb_sn(x, n, &S[threadIdx.x][d * MAXN]);
+        cheb_sn_tab(x, n, tab, &S[threadIdx.x][d * MAXN]);
       }
       sb[threadIdx.x] = b[i];
     }
@@ -339,7 +373,7 @@ __global__ void __launch_bounds__(FT) k_l2p_p2p(int D, int n, int ncheb, const i
                                                 const double *__restrict__ G,
                                                 const int *__restrict__ rp,
                                                 const int *__restrict__ src, double p0,
-                                                double *__restrict__ c) {
+                                                const ChebTab tab, double *__restrict__ c) {
   __shared__ double sg[MAXC];
   __shared__ double sx[FT], sy[FT], sz[FT], sbv[FT];
   __shared__ int sid[FT];
@@ -356,7 +390,7 @@ __global__ void __launch_bounds__(FT) k_l2p_p2p(int D, int n, int ncheb, const i
     if (act) {
       for (int d = 0; d < D; ++d) xi[d] = pos[(int64_t)d * npos + i];
       double S[3][MAXN];
-      for (int d = 0; d < D; ++d) cheb_sn(shift_coord(xi[d], bx[d], bx[3 + d]), n, S[d]);
+      for (int d = 0; d < D; ++d) cheb_sn_tab(shift_coord(xi[d], bx[d], bx[3 + d]), n, tab, S[d]);
       for (int j = 0; j < ncheb; ++j) {
         double r = sg[j];
         for (int d = 0; d < D; ++d) r *= S[d][mi[j * 3 + d]];
@@ -460,7 +494,8 @@ __global__ void __launch_bounds__(PT) k_l2p_p2p32(
     const int *__restrict__ ne, const double *__restrict__ box, const double *__restrict__ pos,
     int64_t npos, const float4 *__restrict__ posf, const float *__restrict__ b32,
     const double *__restrict__ b, const int *__restrict__ mi, const double *__restrict__ G,
-    const int *__restrict__ rp, const int *__restrict__ src, double p0, double *__restrict__ c) {
+    const int *__restrict__ rp, const int *__restrict__ src, double p0, const ChebTab tab,
+    double *__restrict__ c) {
   __shared__ double sg[MAXC];
   __shared__ float4 ss[PT];
   const int tid = threadIdx.x;
@@ -481,7 +516,7 @@ __global__ void __launch_bounds__(PT) k_l2p_p2p32(
       double xi[3] = {0, 0, 0};
       for (int d = 0; d < D; ++d) xi[d] = pos[(int64_t)d * npos + i];
       double S[3][MAXN];
-      for (int d = 0; d < D; ++d) cheb_sn(shift_coord(xi[d], bx[d], bx[3 + d]), n, S[d]);
+      for (int d = 0; d < D; ++d) cheb_sn_tab(shift_coord(xi[d], bx[d], bx[3 + d]), n, tab, S[d]);
       for (int j = 0; j < ncheb; ++j) {
         double r = sg[j];
         for (int d = 0; d < D; ++d) r *= S[d][mi[j * 3 + d]];
@@ -569,6 +604,7 @@ int fmm_plan_build(abx_operator *op, int order, FmmPlan *&out) {
   const int D = p->dim;
   P->D = D;
   P->n = order;
+  P->tab = cheb_table(order);
   P->nchild = 1 << D;
   P->ncheb = 1;
   for (int d = 0; d < D; ++d) P->ncheb *= order;
@@ -822,11 +858,11 @@ int launch_l2p_p2p(FmmPlan *P, cudaStream_t s, const double *pos, int64_t npos, 
     k_l2p_p2p32<KIND><<<P->nleaves, PT, 0, s>>>(
         P->D, P->n, P->ncheb, P->leaf_ids.ptr, P->node_begin.ptr, P->node_end.ptr, P->box.ptr, pos,
         npos, P->posf.ptr, P->b32.ptr, b, P->mi_d.ptr, P->G.ptr, P->p2p_rowptr.ptr,
-        P->p2p_src.ptr, P->p0, c);
+        P->p2p_src.ptr, P->p0, P->tab, c);
   } else
     k_l2p_p2p<KIND, false><<<P->nleaves, FT, 0, s>>>(
         P->D, P->n, P->ncheb, P->leaf_ids.ptr, P->node_begin.ptr, P->node_end.ptr, P->box.ptr, pos,
-        npos, b, P->mi_d.ptr, P->G.ptr, P->p2p_rowptr.ptr, P->p2p_src.ptr, P->p0, c);
+        npos, b, P->mi_d.ptr, P->G.ptr, P->p2p_rowptr.ptr, P->p2p_src.ptr, P->p0, P->tab, c);
   ABX_CHECK_CUDA(cudaGetLastError());
   return ABX_OK;
 }
@@ -846,7 +882,7 @@ int fmm_matvec_device(abx_operator *op, const double *b, double *c) {
   if (P->nleaves > 0)
     k_p2m<<<P->nleaves, FT, 0, s>>>(P->D, P->n, nc, P->leaf_ids.ptr, P->node_begin.ptr,
                                     P->node_end.ptr, P->box.ptr, p->pos.ptr, npos, b, P->mi_d.ptr,
-                                    P->W.ptr);
+                                    P->tab, P->W.ptr);
   const int maxlev = P->max_level.empty() ? 0 : P->max_level[0];
   for (int lev = maxlev; lev >= 1; --lev)
     if (P->link_cnt[lev] > 0)
