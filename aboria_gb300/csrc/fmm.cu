@@ -63,7 +63,7 @@ struct FmmPlan {
   DevBuf<int> m2l;
   int n_m2l = 0;
   DevBuf<double> Km;      // nmat x ncheb x ncheb
-  DevBuf<float> Km32;     // FP32 copy (mixed precision)
+  DevBuf<float> Kmh, Kml; // split-TF32 hi/lo parts of the FP32 copy (tensor-core M2L)
   int nmat = 0;
   // M2L grouped by matrix (for the tensor-core GEMM): per matrix a list of
   // (target, source)
@@ -277,88 +277,152 @@ __device__ __forceinline__ void mma_tf32(float c[4], const uint32_t a[4], const 
 }
 
 constexpr int TC_PAIRS = 64;  // pairs per CTA
-constexpr int TC_KP = 8;      // k step
 
-__global__ void __launch_bounds__(128) k_m2l_tc(int ncheb, int kpad, const float *__restrict__ Km32,
-                                                const int2 *__restrict__ pairs,
-                                                const int *__restrict__ mat_off,
-                                                const int *__restrict__ tile_mat,
-                                                const int *__restrict__ tile_first,
-                                                const float *__restrict__ W32,
-                                                float *__restrict__ G32) {
-  // one CTA = one (matrix, 64-pair tile); 4 warps each own 16 of the 64 pairs
-  // (n dimension) and loop over 16-row blocks of K
-  extern __shared__ float sm[];
-  float *sW = sm;  // [kpad][TC_PAIRS + 4]  gathered source expansions (hi part)
-  const int tile = blockIdx.x;
-  const int m = tile_mat[tile];
-  const int p0 = tile_first[tile];
-  const int pend = mat_off[m + 1];
-  const int np = min(TC_PAIRS, pend - p0);
-  const int ldw = TC_PAIRS + 4;
+// Split-TF32 parts of the FP32 M2L matrices: hi = tf32(K), lo = tf32(K - hi),
+// so that K ~= hi + lo to ~2^-22 and K W ~= hi Wh + hi Wl + lo Wh.
+__global__ void k_split_tf32(const double *__restrict__ K, int64_t n, float *__restrict__ hi,
+                             float *__restrict__ lo) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float f = (float)K[i];
+  const uint32_t h = f2tf32(f);
+  hi[i] = __uint_as_float(h);
+  lo[i] = __uint_as_float(f2tf32(f - __uint_as_float(h)));
+}
+
+// Tensor-core M2L, one CTA per (M2L matrix, 64-pair tile, MT-row block):
+// G[tgt_q][rows] += K[rows][:] W[src_q][:] for the tile's pairs q, as an
+// MT x 64 x ncheb GEMM in 3xTF32 (mma.sync m16n8k8, FP32 accumulation).
+// WM x 2 warps (rows x pairs), 32 x 32 per warp, MT = 32 WM chosen from the
+// number of Chebyshev nodes; K and W are staged 32 columns at a time in
+// padded shared memory (conflict-free fragment loads); the accumulators
+// leave through shared memory as 16-byte vector reductions into G (row
+// stride ldg, a multiple of 4).
+constexpr int M2_NT = 64, M2_KB = 32, M2_LD = M2_KB + 4;
+template <int WM> struct M2Cfg {
+  static constexpr int MT = 32 * WM, LDC = MT + 4, THREADS = 64 * WM;
+  static constexpr size_t SMEM =
+      (size_t)(2 * MT * M2_LD + 2 * M2_NT * M2_LD) * sizeof(float) + 2 * M2_NT * sizeof(int);
+  static_assert((size_t)M2_NT * LDC <= (size_t)(2 * MT * M2_LD + 2 * M2_NT * M2_LD),
+                "the epilogue tile reuses the staging area");
+};
+
+template <int WM>
+__global__ void __launch_bounds__(64 * WM) k_m2l_tc2(int ncheb, int ldg, const float *__restrict__ Kh,
+                                                 const float *__restrict__ Kl,
+                                                 const int2 *__restrict__ pairs,
+                                                 const int *__restrict__ mat_off,
+                                                 const int *__restrict__ tile_mat,
+                                                 const int *__restrict__ tile_first,
+                                                 const float *__restrict__ W32,
+                                                 float *__restrict__ G32) {
+  constexpr int M2_MT = M2Cfg<WM>::MT, M2_LDC = M2Cfg<WM>::LDC, NTH = M2Cfg<WM>::THREADS;
+  extern __shared__ __align__(16) float m2s[];
+  float *sAh = m2s, *sAl = sAh + M2_MT * M2_LD;
+  float *sBh = sAl + M2_MT * M2_LD, *sBl = sBh + M2_NT * M2_LD;
+  int *sSrc = (int *)(sBl + M2_NT * M2_LD), *sTgt = sSrc + M2_NT;
+  float *sC = m2s;  // epilogue, after the main loop
+  const int tile = blockIdx.x, i0 = blockIdx.y * M2_MT;
+  const int m = tile_mat[tile], p0 = tile_first[tile];
+  const int np = min(M2_NT, mat_off[m + 1] - p0);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int e = tid; e < kpad * TC_PAIRS; e += 128) {
-    const int k = e / TC_PAIRS, q = e % TC_PAIRS;
-    float v = 0.f;
-    if (q < np && k < ncheb) v = W32[(size_t)pairs[p0 + q].y * ncheb + k];
-    sW[k * ldw + q] = v;
+  const int g = lane >> 2, t4 = lane & 3;
+  const int wm = warp % WM, wn = warp / WM;
+  if (tid < M2_NT) {
+    const int2 pr = tid < np ? pairs[p0 + tid] : make_int2(-1, -1);
+    sTgt[tid] = pr.x;
+    sSrc[tid] = pr.y;
+  }
+  const float *Ah = Kh + (size_t)m * ncheb * ncheb, *Al = Kl + (size_t)m * ncheb * ncheb;
+  float c[2][4][4] = {};
+  for (int k0 = 0; k0 < ncheb; k0 += M2_KB) {
+    __syncthreads();
+    for (int e = tid; e < M2_MT * M2_KB; e += NTH) {
+      const int r = e / M2_KB, cc = e % M2_KB, i = i0 + r, k = k0 + cc;
+      const bool in = i < ncheb && k < ncheb;
+      sAh[r * M2_LD + cc] = in ? Ah[(size_t)i * ncheb + k] : 0.f;
+      sAl[r * M2_LD + cc] = in ? Al[(size_t)i * ncheb + k] : 0.f;
+    }
+    for (int e = tid; e < M2_NT * M2_KB; e += NTH) {
+      const int q = e / M2_KB, cc = e % M2_KB, k = k0 + cc;
+      const int sidx = sSrc[q];
+      const float v = (sidx >= 0 && k < ncheb) ? W32[(size_t)sidx * ncheb + k] : 0.f;
+      const uint32_t h = f2tf32(v);
+      sBh[q * M2_LD + cc] = __uint_as_float(h);
+      sBl[q * M2_LD + cc] = __uint_as_float(f2tf32(v - __uint_as_float(h)));
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < M2_KB; kk += 8) {
+      uint32_t ah[2][4], al[2][4], bh[4][2], bl[4][2];
+#pragma unroll
+      for (int mf = 0; mf < 2; ++mf) {
+        const int r = wm * 32 + mf * 16 + g;
+        ah[mf][0] = __float_as_uint(sAh[r * M2_LD + kk + t4]);
+        ah[mf][1] = __float_as_uint(sAh[(r + 8) * M2_LD + kk + t4]);
+        ah[mf][2] = __float_as_uint(sAh[r * M2_LD + kk + t4 + 4]);
+        ah[mf][3] = __float_as_uint(sAh[(r + 8) * M2_LD + kk + t4 + 4]);
+        al[mf][0] = __float_as_uint(sAl[r * M2_LD + kk + t4]);
+        al[mf][1] = __float_as_uint(sAl[(r + 8) * M2_LD + kk + t4]);
+        al[mf][2] = __float_as_uint(sAl[r * M2_LD + kk + t4 + 4]);
+        al[mf][3] = __float_as_uint(sAl[(r + 8) * M2_LD + kk + t4 + 4]);
+      }
+#pragma unroll
+      for (int nf = 0; nf < 4; ++nf) {
+        const int q = wn * 32 + nf * 8 + g;
+        bh[nf][0] = __float_as_uint(sBh[q * M2_LD + kk + t4]);
+        bh[nf][1] = __float_as_uint(sBh[q * M2_LD + kk + t4 + 4]);
+        bl[nf][0] = __float_as_uint(sBl[q * M2_LD + kk + t4]);
+        bl[nf][1] = __float_as_uint(sBl[q * M2_LD + kk + t4 + 4]);
+      }
+#pragma unroll
+      for (int mf = 0; mf < 2; ++mf)
+#pragma unroll
+        for (int nf = 0; nf < 4; ++nf) {
+          mma_tf32(c[mf][nf], al[mf], bh[nf]);
+          mma_tf32(c[mf][nf], ah[mf], bl[nf]);
+          mma_tf32(c[mf][nf], ah[mf], bh[nf]);
+        }
+    }
   }
   __syncthreads();
-  const float *K = Km32 + (size_t)m * ncheb * ncheb;
-  const int g = lane >> 2, t4 = lane & 3;
-  const int nbase = warp * 16;  // 16 pairs per warp = 2 n-tiles of 8
-  for (int i0 = 0; i0 < ncheb; i0 += 16) {
-    float c[2][4] = {};
-    for (int k0 = 0; k0 < kpad; k0 += TC_KP) {
-      // A fragment (16x8 row-major): rows i0+g, i0+g+8; cols k0+t4, k0+t4+4
-      float af[4];
-      const int r0 = i0 + g, r1 = i0 + g + 8, ca = k0 + t4, cb = k0 + t4 + 4;
-      af[0] = (r0 < ncheb && ca < ncheb) ? K[(size_t)r0 * ncheb + ca] : 0.f;
-      af[1] = (r1 < ncheb && ca < ncheb) ? K[(size_t)r1 * ncheb + ca] : 0.f;
-      af[2] = (r0 < ncheb && cb < ncheb) ? K[(size_t)r0 * ncheb + cb] : 0.f;
-      af[3] = (r1 < ncheb && cb < ncheb) ? K[(size_t)r1 * ncheb + cb] : 0.f;
-      uint32_t ah[4], al[4];
+  // C fragments -> sC[pair][row]
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        ah[q] = f2tf32(af[q]);
-        al[q] = f2tf32(af[q] - __uint_as_float(ah[q]));
-      }
+  for (int mf = 0; mf < 2; ++mf)
 #pragma unroll
-      for (int nt = 0; nt < 2; ++nt) {
-        // B fragment (8x8 col): rows k0+t4, k0+t4+4; col n = nbase + nt*8 + g
-        const int col = nbase + nt * 8 + g;
-        const float b0 = sW[(k0 + t4) * ldw + col], b1 = sW[(k0 + t4 + 4) * ldw + col];
-        uint32_t bh[2] = {f2tf32(b0), f2tf32(b1)};
-        uint32_t bl[2] = {f2tf32(b0 - __uint_as_float(bh[0])), f2tf32(b1 - __uint_as_float(bh[1]))};
-        mma_tf32(c[nt], al, bh);
-        mma_tf32(c[nt], ah, bl);
-        mma_tf32(c[nt], ah, bh);
-      }
+    for (int nf = 0; nf < 4; ++nf) {
+      const int r = wm * 32 + mf * 16 + g, q = wn * 32 + nf * 8 + 2 * t4;
+      sC[q * M2_LDC + r] = c[mf][nf][0];
+      sC[(q + 1) * M2_LDC + r] = c[mf][nf][1];
+      sC[q * M2_LDC + r + 8] = c[mf][nf][2];
+      sC[(q + 1) * M2_LDC + r + 8] = c[mf][nf][3];
     }
-    // C fragment: rows i0+g (c0,c1), i0+g+8 (c2,c3); cols 2*t4, 2*t4+1
-#pragma unroll
-    for (int nt = 0; nt < 2; ++nt) {
-      const int cbase = nbase + nt * 8 + 2 * t4;
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int q = cbase + h;
-        if (q >= np) continue;
-        const int tgt = pairs[p0 + q].x;
-        const int ra = i0 + g, rb = i0 + g + 8;
-        if (ra < ncheb) atomicAdd(&G32[(size_t)tgt * ncheb + ra], c[nt][h]);
-        if (rb < ncheb) atomicAdd(&G32[(size_t)tgt * ncheb + rb], c[nt][2 + h]);
-      }
-    }
+  __syncthreads();
+  for (int e = tid; e < M2_NT * (M2_MT / 4); e += NTH) {
+    const int q = e / (M2_MT / 4), r4 = (e % (M2_MT / 4)) * 4;
+    const int tgt = sTgt[q];
+    if (tgt < 0 || i0 + r4 >= ncheb) continue;
+    const float4 v = *reinterpret_cast<const float4 *>(&sC[q * M2_LDC + r4]);
+    float *dst = G32 + (size_t)tgt * ldg + i0 + r4;  // 16-byte aligned: ldg, i0 + r4 multiples of 4
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst), "f"(v.x), "f"(v.y),
+                 "f"(v.z), "f"(v.w)
+                 : "memory");
   }
+}
+
+// G[node][i] += G32[node][i] for the padded FP32 accumulator (row stride ldg).
+__global__ void k_add_g32(const float *__restrict__ G32, int64_t nnodes, int ncheb, int ldg,
+                          double *__restrict__ G) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nnodes * ncheb) return;
+  const int64_t node = e / ncheb;
+  const int i = (int)(e % ncheb);
+  G[e] += (double)G32[node * ldg + i];
 }
 
 __global__ void k_f64_to_f32(const double *__restrict__ a, int64_t n, float *__restrict__ b) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) b[i] = (float)a[i];
-}
-__global__ void k_add_f32_to_f64(const float *__restrict__ a, int64_t n, double *__restrict__ b) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) b[i] += (double)a[i];
 }
 
 // ----------------------------------------------------------- L2P + P2P ---
@@ -892,23 +956,33 @@ int fmm_matvec_device(abx_operator *op, const double *b, double *c) {
   if (P->n_m2l > 0) {
     if (mixed) {
       const size_t tot = (size_t)P->nnodes * nc;
+      const int ldg = (nc + 3) / 4 * 4;
       ABX_TRY(P->W32.reserve(tot));
-      ABX_TRY(P->G32.reserve(tot));
-      if (!P->Km32.ptr) {
-        ABX_TRY(P->Km32.reserve((size_t)P->nmat * nc * nc));
-        k_f64_to_f32<<<ceil_div((size_t)P->nmat * nc * nc, 256), 256, 0, s>>>(
-            P->Km.ptr, (size_t)P->nmat * nc * nc, P->Km32.ptr);
+      ABX_TRY(P->G32.reserve((size_t)P->nnodes * ldg));
+      if (!P->Kmh.ptr) {
+        const size_t nk = (size_t)P->nmat * nc * nc;
+        ABX_TRY(P->Kmh.reserve(nk));
+        ABX_TRY(P->Kml.reserve(nk));
+        k_split_tf32<<<ceil_div(nk, 256), 256, 0, s>>>(P->Km.ptr, nk, P->Kmh.ptr, P->Kml.ptr);
       }
       k_f64_to_f32<<<ceil_div(tot, 256), 256, 0, s>>>(P->W.ptr, tot, P->W32.ptr);
-      ABX_CHECK_CUDA(cudaMemsetAsync(P->G32.ptr, 0, tot * 4, s));
-      const int kpad = (nc + TC_KP - 1) / TC_KP * TC_KP;
-      const size_t smem = (size_t)kpad * (TC_PAIRS + 4) * sizeof(float);
-      ABX_CHECK_CUDA(cudaFuncSetAttribute(k_m2l_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem));
-      k_m2l_tc<<<P->ntiles, 128, smem, s>>>(nc, kpad, P->Km32.ptr, P->m2l_by_mat.ptr,
-                                             P->mat_off_d.ptr, P->tile_mat.ptr, P->tile_first.ptr,
-                                             P->W32.ptr, P->G32.ptr);
-      k_add_f32_to_f64<<<ceil_div(tot, 256), 256, 0, s>>>(P->G32.ptr, tot, P->G.ptr);
+      ABX_CHECK_CUDA(cudaMemsetAsync(P->G32.ptr, 0, (size_t)P->nnodes * ldg * 4, s));
+      auto launch_m2l = [&](auto kern, int mt, int threads, size_t smem) -> int {
+        ABX_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)smem));
+        const dim3 grid(P->ntiles, (nc + mt - 1) / mt);
+        kern<<<grid, threads, smem, s>>>(nc, ldg, P->Kmh.ptr, P->Kml.ptr, P->m2l_by_mat.ptr,
+                                         P->mat_off_d.ptr, P->tile_mat.ptr, P->tile_first.ptr,
+                                         P->W32.ptr, P->G32.ptr);
+        return ABX_OK;
+      };
+      if (nc <= 32)
+        ABX_TRY(launch_m2l(k_m2l_tc2<1>, M2Cfg<1>::MT, M2Cfg<1>::THREADS, M2Cfg<1>::SMEM));
+      else if (nc <= 64)
+        ABX_TRY(launch_m2l(k_m2l_tc2<2>, M2Cfg<2>::MT, M2Cfg<2>::THREADS, M2Cfg<2>::SMEM));
+      else
+        ABX_TRY(launch_m2l(k_m2l_tc2<4>, M2Cfg<4>::MT, M2Cfg<4>::THREADS, M2Cfg<4>::SMEM));
+      k_add_g32<<<ceil_div(tot, 256), 256, 0, s>>>(P->G32.ptr, P->nnodes, nc, ldg, P->G.ptr);
     } else {
       k_m2l64<<<P->n_m2l, FT, 0, s>>>(nc, P->m2l.ptr, P->n_m2l, P->Km.ptr, P->W.ptr, P->G.ptr);
     }
