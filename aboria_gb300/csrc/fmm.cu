@@ -64,6 +64,7 @@ struct FmmPlan {
   int n_m2l = 0;
   DevBuf<double> Km;      // nmat x ncheb x ncheb
   DevBuf<float> Kmh, Kml; // split-TF32 hi/lo parts of the FP32 copy (tensor-core M2L)
+  DevBuf<float> W32l;     // lo part of W (the tcgen05 M2L reads W32 as the hi part)
   int nmat = 0;
   // M2L grouped by matrix (for the tensor-core GEMM): per matrix a list of
   // (target, source)
@@ -280,14 +281,29 @@ constexpr int TC_PAIRS = 64;  // pairs per CTA
 
 // Split-TF32 parts of the FP32 M2L matrices: hi = tf32(K), lo = tf32(K - hi),
 // so that K ~= hi + lo to ~2^-22 and K W ~= hi Wh + hi Wl + lo Wh.
-__global__ void k_split_tf32(const double *__restrict__ K, int64_t n, float *__restrict__ hi,
-                             float *__restrict__ lo) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float f = (float)K[i];
+// Rows of ncheb entries are stored with stride ldk (a multiple of 32, zero
+// padded), so that the tensor-core kernels stage whole 16-byte-aligned
+// 32-column blocks.
+__global__ void k_split_tf32(const double *__restrict__ K, int64_t nrows, int ncheb, int ldk,
+                             float *__restrict__ hi, float *__restrict__ lo) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nrows * ldk) return;
+  const int64_t row = e / ldk;
+  const int k = (int)(e % ldk);
+  const float f = k < ncheb ? (float)K[row * ncheb + k] : 0.f;
   const uint32_t h = f2tf32(f);
-  hi[i] = __uint_as_float(h);
-  lo[i] = __uint_as_float(f2tf32(f - __uint_as_float(h)));
+  hi[e] = __uint_as_float(h);
+  lo[e] = __uint_as_float(f2tf32(f - __uint_as_float(h)));
+}
+
+// W32[node][k] = (float)W[node][k] with row stride ldk (zero padded).
+__global__ void k_to_f32_padded(const double *__restrict__ W, int64_t nrows, int ncheb, int ldk,
+                                float *__restrict__ W32) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nrows * ldk) return;
+  const int64_t row = e / ldk;
+  const int k = (int)(e % ldk);
+  W32[e] = k < ncheb ? (float)W[row * ncheb + k] : 0.f;
 }
 
 // Tensor-core M2L, one CTA per (M2L matrix, 64-pair tile, MT-row block):
@@ -308,7 +324,7 @@ template <int WM> struct M2Cfg {
 };
 
 template <int WM>
-__global__ void __launch_bounds__(64 * WM) k_m2l_tc2(int ncheb, int ldg, const float *__restrict__ Kh,
+__global__ void __launch_bounds__(64 * WM) k_m2l_tc2(int ncheb, int ldk, int ldg, const float *__restrict__ Kh,
                                                  const float *__restrict__ Kl,
                                                  const int2 *__restrict__ pairs,
                                                  const int *__restrict__ mat_off,
@@ -333,20 +349,20 @@ __global__ void __launch_bounds__(64 * WM) k_m2l_tc2(int ncheb, int ldg, const f
     sTgt[tid] = pr.x;
     sSrc[tid] = pr.y;
   }
-  const float *Ah = Kh + (size_t)m * ncheb * ncheb, *Al = Kl + (size_t)m * ncheb * ncheb;
+  const float *Ah = Kh + (size_t)m * ncheb * ldk, *Al = Kl + (size_t)m * ncheb * ldk;
   float c[2][4][4] = {};
   for (int k0 = 0; k0 < ncheb; k0 += M2_KB) {
     __syncthreads();
     for (int e = tid; e < M2_MT * M2_KB; e += NTH) {
       const int r = e / M2_KB, cc = e % M2_KB, i = i0 + r, k = k0 + cc;
       const bool in = i < ncheb && k < ncheb;
-      sAh[r * M2_LD + cc] = in ? Ah[(size_t)i * ncheb + k] : 0.f;
-      sAl[r * M2_LD + cc] = in ? Al[(size_t)i * ncheb + k] : 0.f;
+      sAh[r * M2_LD + cc] = in ? Ah[(size_t)i * ldk + k] : 0.f;
+      sAl[r * M2_LD + cc] = in ? Al[(size_t)i * ldk + k] : 0.f;
     }
     for (int e = tid; e < M2_NT * M2_KB; e += NTH) {
       const int q = e / M2_KB, cc = e % M2_KB, k = k0 + cc;
       const int sidx = sSrc[q];
-      const float v = (sidx >= 0 && k < ncheb) ? W32[(size_t)sidx * ncheb + k] : 0.f;
+      const float v = (sidx >= 0 && k < ncheb) ? W32[(size_t)sidx * ldk + k] : 0.f;
       const uint32_t h = f2tf32(v);
       sBh[q * M2_LD + cc] = __uint_as_float(h);
       sBl[q * M2_LD + cc] = __uint_as_float(f2tf32(v - __uint_as_float(h)));
@@ -408,6 +424,227 @@ __global__ void __launch_bounds__(64 * WM) k_m2l_tc2(int ncheb, int ldg, const f
                  "f"(v.z), "f"(v.w)
                  : "memory");
   }
+}
+
+// ------------------------------------------------- M2L on tcgen05 (TMEM) ---
+// The same tile GEMM on the 5th-generation tensor cores: one CTA (4 warps)
+// per (M2L matrix, T5_N-pair tile, 128-row block).  K (hi, lo: split once per
+// plan) and the gathered source expansions W (hi, lo: split once per matvec)
+// are copied T5_KB columns at a time by cp.async into a T5_S-stage ring in the
+// no-swizzle K-major core-matrix layout (8 rows x 16 bytes per core matrix;
+// the descriptor's leading byte offset is the core-matrix stride along K,
+// the stride byte offset along rows).  Thread 0 issues, per 8-column step,
+// the three split-TF32 products lo*hi, hi*lo, hi*hi as tcgen05.mma
+// kind::tf32 into one 128 x T5_N FP32 accumulator in TMEM and commits each
+// stage to its mbarrier; a stage is refilled only after that barrier
+// completes.  Every wait is bounded: on timeout the kernel sets *status,
+// skips the epilogue and still releases its TMEM.  Epilogue: each warp reads
+// its 32 accumulator lanes (rows) with tcgen05.ld and adds them into G with
+// reductions that are coalesced along the rows.
+constexpr int T5_M = 128, T5_N = 128, T5_KB = 8, T5_S = 3;
+static_assert(T5_N % 16 == 0 && T5_N <= 128, "one pair per thread when loading the tile");
+constexpr int T5_A = T5_M * T5_KB * 4, T5_B = T5_N * T5_KB * 4;  // bytes per operand part
+constexpr int T5_STAGE = 2 * T5_A + 2 * T5_B;                     // hi + lo of A and B
+constexpr size_t T5_SMEM = T5_S * (size_t)T5_STAGE + 1024 + 2048;  // + alignment, barriers, indices
+constexpr int T5_SPIN = 1 << 26;  // mbarrier polls before giving up (seconds at most)
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor: no swizzle, K-major.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+
+// Instruction descriptor, kind::tf32: D F32, A and B TF32, both K-major.
+__host__ __device__ constexpr uint32_t umma_idesc_tf32(int m, int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (int it = 0; it < T5_SPIN; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+// 16-byte asynchronous copy; nbytes = 0 writes zeros.
+__device__ __forceinline__ void cp16(uint32_t dst, const void *src, int nbytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(nbytes)
+               : "memory");
+}
+
+__global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int ldk, int ldg,
+                                                 const float *__restrict__ Kh,
+                                                 const float *__restrict__ Kl,
+                                                 const int2 *__restrict__ pairs,
+                                                 const int *__restrict__ mat_off,
+                                                 const int *__restrict__ tile_mat,
+                                                 const int *__restrict__ tile_first,
+                                                 const float *__restrict__ Wh,
+                                                 const float *__restrict__ Wl,
+                                                 float *__restrict__ G32, int *__restrict__ status) {
+  extern __shared__ __align__(128) unsigned char t5raw[];
+  unsigned char *sm = (unsigned char *)(((uintptr_t)t5raw + 1023) & ~(uintptr_t)1023);
+  uint64_t *mbar = (uint64_t *)(sm + T5_S * T5_STAGE);
+  uint32_t *tslot = (uint32_t *)(mbar + T5_S);
+  int *sSrc = (int *)(tslot + 4), *sTgt = sSrc + T5_N;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tile = blockIdx.x, i0 = blockIdx.y * T5_M;
+  const int m = tile_mat[tile], p0 = tile_first[tile];
+  const int np = min(T5_N, mat_off[m + 1] - p0);
+  if (tid < T5_N) {
+    const int2 pr = tid < np ? pairs[p0 + tid] : make_int2(-1, -1);
+    sTgt[tid] = pr.x;
+    sSrc[tid] = pr.y;
+  }
+  if (tid == 0) {
+    for (int q = 0; q < T5_S; ++q)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[q])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_addr(tslot)),
+                 "r"(T5_N));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+  const float *Ah = Kh + (size_t)m * ncheb * ldk, *Al = Kl + (size_t)m * ncheb * ldk;
+  const int nkb = ldk / T5_KB;
+  constexpr uint32_t idesc = umma_idesc_tf32(T5_M, T5_N);
+  const uint32_t smbase = smem_addr(sm);
+
+  // copies of k-block kb into stage kb % T5_S (one cp.async group)
+  auto load_block = [&](int kb) {
+    const int k0 = kb * T5_KB;
+    const uint32_t st = smbase + (uint32_t)((kb % T5_S) * T5_STAGE);
+    // A: element (r, k) at ((k/4) * 16 + r/8) * 128 + (r%8) * 16 + (k%4) * 4
+    for (int e = tid; e < T5_M * (T5_KB / 4); e += 128) {
+      const int rl = e & 7, kq = (e >> 3) % (T5_KB / 4), rh = (e >> 3) / (T5_KB / 4);
+      const int r = rh * 8 + rl, i = i0 + r;
+      const int ic = min(i, ncheb - 1);
+      const uint32_t off = (uint32_t)((kq * (T5_M / 8) + rh) * 128 + rl * 16);
+      const size_t g = (size_t)ic * ldk + k0 + kq * 4;
+      cp16(st + off, Ah + g, i < ncheb ? 16 : 0);
+      cp16(st + T5_A + off, Al + g, i < ncheb ? 16 : 0);
+    }
+    // B: the tile's source expansions
+    for (int e = tid; e < T5_N * (T5_KB / 4); e += 128) {
+      const int rl = e & 7, kq = (e >> 3) % (T5_KB / 4), rh = (e >> 3) / (T5_KB / 4);
+      const int q = rh * 8 + rl;
+      const int src = sSrc[q];
+      const uint32_t off = (uint32_t)((kq * (T5_N / 8) + rh) * 128 + rl * 16);
+      const size_t g = (size_t)(src >= 0 ? src : 0) * ldk + k0 + kq * 4;
+      cp16(st + 2 * T5_A + off, Wh + g, src >= 0 ? 16 : 0);
+      cp16(st + 2 * T5_A + T5_B + off, Wl + g, src >= 0 ? 16 : 0);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+
+  for (int kb = 0; kb < T5_S - 1; ++kb) {
+    if (kb < nkb) load_block(kb);
+    else asm volatile("cp.async.commit_group;" ::: "memory");
+  }
+  bool ok = true;
+  for (int kb = 0; kb < nkb; ++kb) {
+    const int st = kb % T5_S;
+    // this thread's copies of block kb have landed (at most T5_S - 2 newer groups pending)
+    asm volatile("cp.async.wait_group %0;" ::"n"(T5_S - 2) : "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t base = smbase + (uint32_t)(st * T5_STAGE);
+      const uint32_t a_ks = (T5_M / 8) * 128, b_ks = (T5_N / 8) * 128;
+#pragma unroll
+      for (int j = 0; j < T5_KB / 8; ++j) {
+        const uint64_t ah = umma_desc(base + 2 * j * a_ks, a_ks, 128);
+        const uint64_t al = umma_desc(base + T5_A + 2 * j * a_ks, a_ks, 128);
+        const uint64_t bh = umma_desc(base + 2 * T5_A + 2 * j * b_ks, b_ks, 128);
+        const uint64_t bl = umma_desc(base + 2 * T5_A + T5_B + 2 * j * b_ks, b_ks, 128);
+        const uint64_t ad[3] = {al, ah, ah}, bd[3] = {bh, bl, bh};
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+          const uint32_t acc = (kb > 0 || j > 0 || t > 0) ? 1u : 0u;
+          asm volatile(
+              "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+              "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+              "l"(ad[t]), "l"(bd[t]), "r"(idesc), "r"(acc));
+        }
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_addr(&mbar[st])));
+    }
+    // refill the stage that block kb - 1 used with block kb + T5_S - 1, once
+    // block kb - 1's MMAs have completed (the c-th commit on a stage's barrier
+    // completes its phase c)
+    const int nb = kb + T5_S - 1;
+    if (nb < nkb) {
+      if (kb >= 1) {
+        const int pst = (kb - 1) % T5_S;
+        if (!mbar_wait(smem_addr(&mbar[pst]), ((kb - 1) / T5_S) & 1)) ok = false;
+      }
+      if (!__syncthreads_and(ok)) {
+        ok = false;
+        break;
+      }
+      load_block(nb);
+    } else {
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+  }
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  // the last block's commit covers every MMA issued before it
+  const int lst = (nkb - 1) % T5_S;
+  const uint32_t lpar = ((nkb - 1) / T5_S) & 1;
+  if (ok && nkb > 0 && !mbar_wait(smem_addr(&mbar[lst]), lpar)) ok = false;
+  ok = __syncthreads_and(ok);
+  if (!ok) {
+    if (tid == 0) atomicExch(status, 1);
+    // let anything still in flight drain (bounded) before the TMEM is released
+    if (nkb > 0) mbar_wait(smem_addr(&mbar[lst]), lpar);
+  } else {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int r = 32 * warp + lane, i = i0 + r;
+#pragma unroll
+    for (int c0 = 0; c0 < T5_N; c0 += 16) {
+      uint32_t v[16];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+          "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+            "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+            "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+          : "r"(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (i < ncheb) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          const int tgt = sTgt[c0 + q];
+          if (tgt >= 0) atomicAdd(&G32[(size_t)tgt * ldg + i], __uint_as_float(v[q]));
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(T5_N));
 }
 
 // G[node][i] += G32[node][i] for the padded FP32 accumulator (row stride ldg).
@@ -858,8 +1095,11 @@ int fmm_plan_build(abx_operator *op, int order, FmmPlan *&out) {
   if ((st = P->mi_d.reserve(P->mi.size())) || (st = md_d.reserve(mdesc.size() + 1))) return fail(st);
   // tensor-core M2L tiles: 64 pairs of one matrix each
   std::vector<int> tmat, tfirst;
+  // tensor-core M2L tiles: 64 pairs for the mma.sync kernel (<= 64 nodes),
+  // T5_N pairs for the tcgen05 kernel
+  const int tile_pairs = nc <= 64 ? TC_PAIRS : T5_N;
   for (int m = 0; m < P->nmat; ++m)
-    for (int q = P->mat_off[m]; q < P->mat_off[m + 1]; q += TC_PAIRS) {
+    for (int q = P->mat_off[m]; q < P->mat_off[m + 1]; q += tile_pairs) {
       tmat.push_back(m);
       tfirst.push_back(q);
     }
@@ -957,31 +1197,52 @@ int fmm_matvec_device(abx_operator *op, const double *b, double *c) {
     if (mixed) {
       const size_t tot = (size_t)P->nnodes * nc;
       const int ldg = (nc + 3) / 4 * 4;
-      ABX_TRY(P->W32.reserve(tot));
+      const int ldk = (nc + 31) / 32 * 32;
+      ABX_TRY(P->W32.reserve((size_t)P->nnodes * ldk));
       ABX_TRY(P->G32.reserve((size_t)P->nnodes * ldg));
       if (!P->Kmh.ptr) {
-        const size_t nk = (size_t)P->nmat * nc * nc;
+        const size_t nk = (size_t)P->nmat * nc * ldk;
         ABX_TRY(P->Kmh.reserve(nk));
         ABX_TRY(P->Kml.reserve(nk));
-        k_split_tf32<<<ceil_div(nk, 256), 256, 0, s>>>(P->Km.ptr, nk, P->Kmh.ptr, P->Kml.ptr);
+        k_split_tf32<<<ceil_div(nk, 256), 256, 0, s>>>(P->Km.ptr, (int64_t)P->nmat * nc, nc, ldk,
+                                                       P->Kmh.ptr, P->Kml.ptr);
       }
-      k_f64_to_f32<<<ceil_div(tot, 256), 256, 0, s>>>(P->W.ptr, tot, P->W32.ptr);
+      k_to_f32_padded<<<ceil_div((size_t)P->nnodes * ldk, 256), 256, 0, s>>>(
+          P->W.ptr, P->nnodes, nc, ldk, P->W32.ptr);
       ABX_CHECK_CUDA(cudaMemsetAsync(P->G32.ptr, 0, (size_t)P->nnodes * ldg * 4, s));
       auto launch_m2l = [&](auto kern, int mt, int threads, size_t smem) -> int {
         ABX_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)smem));
         const dim3 grid(P->ntiles, (nc + mt - 1) / mt);
-        kern<<<grid, threads, smem, s>>>(nc, ldg, P->Kmh.ptr, P->Kml.ptr, P->m2l_by_mat.ptr,
+        kern<<<grid, threads, smem, s>>>(nc, ldk, ldg, P->Kmh.ptr, P->Kml.ptr, P->m2l_by_mat.ptr,
                                          P->mat_off_d.ptr, P->tile_mat.ptr, P->tile_first.ptr,
                                          P->W32.ptr, P->G32.ptr);
         return ABX_OK;
       };
-      if (nc <= 32)
+      if (nc <= 32) {
         ABX_TRY(launch_m2l(k_m2l_tc2<1>, M2Cfg<1>::MT, M2Cfg<1>::THREADS, M2Cfg<1>::SMEM));
-      else if (nc <= 64)
+      } else if (nc <= 64) {
         ABX_TRY(launch_m2l(k_m2l_tc2<2>, M2Cfg<2>::MT, M2Cfg<2>::THREADS, M2Cfg<2>::SMEM));
-      else
-        ABX_TRY(launch_m2l(k_m2l_tc2<4>, M2Cfg<4>::MT, M2Cfg<4>::THREADS, M2Cfg<4>::SMEM));
+      } else {
+        // 5th-generation tensor cores (tcgen05, TMEM accumulator)
+        ABX_TRY(P->W32l.reserve((size_t)P->nnodes * ldk));
+        k_split_tf32<<<ceil_div((size_t)P->nnodes * ldk, 256), 256, 0, s>>>(
+            P->W.ptr, P->nnodes, nc, ldk, P->W32.ptr, P->W32l.ptr);
+        int *status = p->ctx->dev_flag.ptr + 8;
+        ABX_CHECK_CUDA(cudaMemsetAsync(status, 0, sizeof(int), s));
+        ABX_CHECK_CUDA(cudaFuncSetAttribute(k_m2l_tc5, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)T5_SMEM));
+        const dim3 grid(P->ntiles, (nc + T5_M - 1) / T5_M);
+        k_m2l_tc5<<<grid, 128, T5_SMEM, s>>>(nc, ldk, ldg, P->Kmh.ptr, P->Kml.ptr,
+                                              P->m2l_by_mat.ptr, P->mat_off_d.ptr,
+                                              P->tile_mat.ptr, P->tile_first.ptr, P->W32.ptr,
+                                              P->W32l.ptr, P->G32.ptr, status);
+        ABX_CHECK_CUDA(cudaGetLastError());
+        int st = 0;
+        ABX_CHECK_CUDA(cudaMemcpyAsync(&st, status, sizeof(int), cudaMemcpyDeviceToHost, s));
+        ABX_CHECK_CUDA(cudaStreamSynchronize(s));
+        ABX_REQUIRE(st == 0, ABX_ERR_TIMEOUT, "FMM M2L: a tensor-core completion wait timed out");
+      }
       k_add_g32<<<ceil_div(tot, 256), 256, 0, s>>>(P->G32.ptr, P->nnodes, nc, ldg, P->G.ptr);
     } else {
       k_m2l64<<<P->n_m2l, FT, 0, s>>>(nc, P->m2l.ptr, P->n_m2l, P->Km.ptr, P->W.ptr, P->G.ptr);
