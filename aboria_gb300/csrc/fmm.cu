@@ -51,6 +51,7 @@ struct FmmPlan {
   // device
   DevBuf<double> W, G;            // nnodes x ncheb
   DevBuf<double> Tc;              // nchild x ncheb x ncheb (child->parent interpolation)
+  DevBuf<float> Tc32;             // FP32 copy (mixed-precision M2M / L2L)
   DevBuf<double> box;             // nnodes x 6 (lo[3], hi[3])
   DevBuf<int> leaf_ids;           // leaves (node ids)
   DevBuf<int> node_begin, node_end;
@@ -203,37 +204,41 @@ __global__ void __launch_bounds__(FT) k_p2m(int D, int n, int ncheb, const int *
 
 // ------------------------------------------------------------ M2M / L2L ---
 // links: (parent, child, octant); one CTA per link group of one parent.
-// M2M: W[p][i] += sum_j Tc[o][i][j] W[c][j]   (atomic over children)
+// M2M: W[p][i] += sum_j Tc[o][i][j] W[c][j]   (atomic over children).
+// T is the compute type: double in FP64 mode; float in mixed mode (FP32
+// copy of Tc, FP32 sums of ncheb terms, FP64 storage).
+template <typename T>
 __global__ void __launch_bounds__(FT) k_m2m(int ncheb, const int *__restrict__ links, int nlinks,
-                                            const double *__restrict__ Tc, double *__restrict__ W) {
+                                            const T *__restrict__ Tc, double *__restrict__ W) {
   const int l = blockIdx.x;
   if (l >= nlinks) return;
   const int p = links[3 * l], c = links[3 * l + 1], o = links[3 * l + 2];
-  __shared__ double wc[MAXC];
-  for (int j = threadIdx.x; j < ncheb; j += FT) wc[j] = W[(size_t)c * ncheb + j];
+  __shared__ T wc[MAXC];
+  for (int j = threadIdx.x; j < ncheb; j += FT) wc[j] = (T)W[(size_t)c * ncheb + j];
   __syncthreads();
-  const double *T = Tc + (size_t)o * ncheb * ncheb;
+  const T *Tm = Tc + (size_t)o * ncheb * ncheb;
   for (int i = threadIdx.x; i < ncheb; i += FT) {
-    double a = 0.0;
-    for (int j = 0; j < ncheb; ++j) a += T[(size_t)i * ncheb + j] * wc[j];
-    atomicAdd(&W[(size_t)p * ncheb + i], a);
+    T a = 0;
+    for (int j = 0; j < ncheb; ++j) a += Tm[(size_t)i * ncheb + j] * wc[j];
+    atomicAdd(&W[(size_t)p * ncheb + i], (double)a);
   }
 }
 
-// L2L: G[c][i] += sum_j Tc[o][j][i] G[p][j]
+// L2L: G[c][i] += sum_j Tc[o][j][i] G[p][j]   (compute type T as for M2M)
+template <typename T>
 __global__ void __launch_bounds__(FT) k_l2l(int ncheb, const int *__restrict__ links, int nlinks,
-                                            const double *__restrict__ Tc, double *__restrict__ G) {
+                                            const T *__restrict__ Tc, double *__restrict__ G) {
   const int l = blockIdx.x;
   if (l >= nlinks) return;
   const int p = links[3 * l], c = links[3 * l + 1], o = links[3 * l + 2];
-  __shared__ double gp[MAXC];
-  for (int j = threadIdx.x; j < ncheb; j += FT) gp[j] = G[(size_t)p * ncheb + j];
+  __shared__ T gp[MAXC];
+  for (int j = threadIdx.x; j < ncheb; j += FT) gp[j] = (T)G[(size_t)p * ncheb + j];
   __syncthreads();
-  const double *T = Tc + (size_t)o * ncheb * ncheb;
+  const T *Tm = Tc + (size_t)o * ncheb * ncheb;
   for (int i = threadIdx.x; i < ncheb; i += FT) {
-    double a = 0.0;
-    for (int j = 0; j < ncheb; ++j) a += T[(size_t)j * ncheb + i] * gp[j];
-    G[(size_t)c * ncheb + i] += a;
+    T a = 0;
+    for (int j = 0; j < ncheb; ++j) a += Tm[(size_t)j * ncheb + i] * gp[j];
+    G[(size_t)c * ncheb + i] += (double)a;
   }
 }
 
@@ -1187,11 +1192,20 @@ int fmm_matvec_device(abx_operator *op, const double *b, double *c) {
     k_p2m<<<P->nleaves, FT, 0, s>>>(P->D, P->n, nc, P->leaf_ids.ptr, P->node_begin.ptr,
                                     P->node_end.ptr, P->box.ptr, p->pos.ptr, npos, b, P->mi_d.ptr,
                                     P->tab, P->W.ptr);
+  if (mixed && !P->Tc32.ptr) {
+    const size_t nt = (size_t)P->nchild * nc * nc;
+    ABX_TRY(P->Tc32.reserve(nt));
+    k_f64_to_f32<<<ceil_div(nt, 256), 256, 0, s>>>(P->Tc.ptr, nt, P->Tc32.ptr);
+  }
   const int maxlev = P->max_level.empty() ? 0 : P->max_level[0];
   for (int lev = maxlev; lev >= 1; --lev)
     if (P->link_cnt[lev] > 0)
-      k_m2m<<<P->link_cnt[lev], FT, 0, s>>>(nc, P->links.ptr + 3 * P->link_off[lev],
-                                           P->link_cnt[lev], P->Tc.ptr, P->W.ptr);
+      if (mixed)
+        k_m2m<float><<<P->link_cnt[lev], FT, 0, s>>>(nc, P->links.ptr + 3 * P->link_off[lev],
+                                                     P->link_cnt[lev], P->Tc32.ptr, P->W.ptr);
+      else
+        k_m2m<double><<<P->link_cnt[lev], FT, 0, s>>>(nc, P->links.ptr + 3 * P->link_off[lev],
+                                                      P->link_cnt[lev], P->Tc.ptr, P->W.ptr);
   ABX_CHECK_CUDA(cudaGetLastError());
   if (P->n_m2l > 0) {
     if (mixed) {
@@ -1251,8 +1265,12 @@ int fmm_matvec_device(abx_operator *op, const double *b, double *c) {
   }
   for (int lev = 1; lev <= maxlev; ++lev)
     if (P->link_cnt[lev] > 0)
-      k_l2l<<<P->link_cnt[lev], FT, 0, s>>>(nc, P->links.ptr + 3 * P->link_off[lev],
-                                           P->link_cnt[lev], P->Tc.ptr, P->G.ptr);
+      if (mixed)
+        k_l2l<float><<<P->link_cnt[lev], FT, 0, s>>>(nc, P->links.ptr + 3 * P->link_off[lev],
+                                                     P->link_cnt[lev], P->Tc32.ptr, P->G.ptr);
+      else
+        k_l2l<double><<<P->link_cnt[lev], FT, 0, s>>>(nc, P->links.ptr + 3 * P->link_off[lev],
+                                                      P->link_cnt[lev], P->Tc.ptr, P->G.ptr);
   ABX_CHECK_CUDA(cudaGetLastError());
   if (P->nleaves == 0) return ABX_OK;
   switch (P->kind) {
