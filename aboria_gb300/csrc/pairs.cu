@@ -87,7 +87,7 @@ namespace {
 
 constexpr int TPB = 256;
 constexpr int WARPS_PER_CTA = 4;
-constexpr int GROUP_E2 = 16;  // a unit spans at most this many fine cells along e2
+constexpr int GROUP_E2 = 4;  // a unit spans at most this many fine cells along e2
 
 enum { POL_COUNT = 0, POL_LIST = 1, POL_MATVEC = 2 };
 
