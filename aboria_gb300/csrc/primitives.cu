@@ -102,16 +102,19 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(uint32_t *data, siz
 }
 
 // ---------------------------------------------------------------- radix ---
-constexpr int RADIX_BITS = 8;
-constexpr int RADIX = 1 << RADIX_BITS;
+// LSD radix sort of (key, value) pairs, stable; RB-bit digits (8, or 10 when
+// two 10-bit passes cover the key where 8-bit digits would need three).
 constexpr int RS_THREADS = 256;
 constexpr int RS_WARPS = RS_THREADS / 32;
 constexpr int RS_ITEMS = 16;
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;  // 4096
+constexpr int RADIX_MAX = 1 << 10;
 
+template <int RB>
 __global__ void __launch_bounds__(RS_THREADS) k_radix_hist(const uint32_t *keys, size_t n,
                                                            int shift, uint32_t mask,
                                                            uint32_t *hist, int ntiles) {
+  constexpr int RADIX = 1 << RB;
   __shared__ uint32_t h[RADIX];
   for (int i = threadIdx.x; i < RADIX; i += RS_THREADS) h[i] = 0;
   __syncthreads();
@@ -125,10 +128,12 @@ __global__ void __launch_bounds__(RS_THREADS) k_radix_hist(const uint32_t *keys,
     hist[(size_t)d * ntiles + blockIdx.x] = h[d];
 }
 
+template <int RB>
 __global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(
     const uint32_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
     uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, size_t n, int shift,
     uint32_t mask, const uint32_t *__restrict__ offsets, int ntiles) {
+  constexpr int RADIX = 1 << RB;
   __shared__ uint32_t wcount[RS_WARPS][RADIX + 1];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int i = tid; i < RS_WARPS * (RADIX + 1); i += RS_THREADS) (&wcount[0][0])[i] = 0;
@@ -215,25 +220,33 @@ int exclusive_scan_u32(uint32_t *data, size_t n, uint32_t *temp, cudaStream_t s)
 
 size_t radix_temp_u32(size_t n) {
   const size_t ntiles = (n + RS_TILE - 1) / RS_TILE;
-  const size_t hist = ntiles * RADIX;
+  const size_t hist = ntiles * RADIX_MAX;
   return hist + 64 + scan_temp_elems(hist);
 }
 
 int radix_sort_pairs(uint32_t *keys, uint32_t *vals, size_t n, int bits, uint32_t *keys_alt,
                      uint32_t *vals_alt, uint32_t *temp, cudaStream_t s) {
   if (n <= 1 || bits <= 0) return ABX_OK;
+  // digit width: 10 bits where that saves a pass (17..20-bit keys)
+  const int rb = (bits > 16 && bits <= 20) ? 10 : 8;
   const int ntiles = (int)((n + RS_TILE - 1) / RS_TILE);
-  const size_t hist_n = (size_t)ntiles * RADIX;
+  const size_t hist_n = (size_t)ntiles << rb;
   uint32_t *hist = temp;
   uint32_t *scan_tmp = temp + hist_n + 64;
   uint32_t *ki = keys, *vi = vals, *ko = keys_alt, *vo = vals_alt;
-  for (int shift = 0; shift < bits; shift += RADIX_BITS) {
-    const int nb = bits - shift < RADIX_BITS ? bits - shift : RADIX_BITS;
+  for (int shift = 0; shift < bits; shift += rb) {
+    const int nb = bits - shift < rb ? bits - shift : rb;
     const uint32_t mask = (1u << nb) - 1u;
-    k_radix_hist<<<ntiles, RS_THREADS, 0, s>>>(ki, n, shift, mask, hist, ntiles);
+    if (rb == 10)
+      k_radix_hist<10><<<ntiles, RS_THREADS, 0, s>>>(ki, n, shift, mask, hist, ntiles);
+    else
+      k_radix_hist<8><<<ntiles, RS_THREADS, 0, s>>>(ki, n, shift, mask, hist, ntiles);
     ABX_CHECK_CUDA(cudaGetLastError());
     ABX_TRY(exclusive_scan_u32(hist, hist_n, scan_tmp, s));
-    k_radix_scatter<<<ntiles, RS_THREADS, 0, s>>>(ki, vi, ko, vo, n, shift, mask, hist, ntiles);
+    if (rb == 10)
+      k_radix_scatter<10><<<ntiles, RS_THREADS, 0, s>>>(ki, vi, ko, vo, n, shift, mask, hist, ntiles);
+    else
+      k_radix_scatter<8><<<ntiles, RS_THREADS, 0, s>>>(ki, vi, ko, vo, n, shift, mask, hist, ntiles);
     ABX_CHECK_CUDA(cudaGetLastError());
     uint32_t *t;
     t = ki; ki = ko; ko = t;
