@@ -785,33 +785,37 @@ template <int KIND> __device__ __forceinline__ float p2p_k32(float d2, float p0)
   return fmm_k32<KIND>(d2, p0);
 }
 
-constexpr int PT = 64;  // threads per target leaf in the mixed near field
+constexpr int PT = 32;  // threads per target leaf (one warp) in the mixed near field
+constexpr int PW = 4;   // target leaves (warps) per CTA
 
-// Mixed-precision L2P + P2P: one CTA per target leaf, one thread per target.
+// Mixed-precision L2P + P2P: one warp per target leaf, one lane per target.
 // L2P in FP64 as in the FP64 kernel; each source leaf of the near field is
 // staged in shared memory as FP32 offsets from the target leaf's centre
 // (leaf-relative FP32 position + FP32 centre offset), the pair terms are FP32
-// with a staged chunk (<= 64 terms) summed in FP32 and chunks summed in
+// with a staged chunk (<= 32 terms) summed in FP32 and chunks summed in
 // FP64.  The self pair (a regularised singular kernel is huge there) is
 // masked out of the FP32 sum and added in FP64.
 template <int KIND>
-__global__ void __launch_bounds__(PT) k_l2p_p2p32(
-    int D, int n, int ncheb, const int *__restrict__ leaves, const int *__restrict__ nb,
+__global__ void __launch_bounds__(PT * PW) k_l2p_p2p32(
+    int D, int n, int ncheb, int nleaves, const int *__restrict__ leaves, const int *__restrict__ nb,
     const int *__restrict__ ne, const double *__restrict__ box, const double *__restrict__ pos,
     int64_t npos, const float4 *__restrict__ posf, const float *__restrict__ b32,
     const double *__restrict__ b, const int *__restrict__ mi, const double *__restrict__ G,
     const int *__restrict__ rp, const int *__restrict__ src, double p0, const ChebTab tab,
     double *__restrict__ c) {
-  __shared__ double sg[MAXC];
-  __shared__ float4 ss[PT];
-  const int tid = threadIdx.x;
-  const int li = blockIdx.x;
+  __shared__ double sg_all[PW][MAXC];
+  __shared__ float4 ss_all[PW][PT];
+  const int tid = threadIdx.x & 31, wl = threadIdx.x >> 5;
+  const int li = blockIdx.x * PW + wl;
+  if (li >= nleaves) return;  // whole warps: only warp-level synchronisation below
+  double *sg = sg_all[wl];
+  float4 *ss = ss_all[wl];
   const int leaf = leaves[li];
   const double *bx = box + (size_t)leaf * 6;
   double ct[3] = {0.0, 0.0, 0.0};
   for (int d = 0; d < D; ++d) ct[d] = 0.5 * (bx[d] + bx[3 + d]);
   for (int j = tid; j < ncheb; j += PT) sg[j] = G[(size_t)leaf * ncheb + j];
-  __syncthreads();
+  __syncwarp();
   const float p0f = (float)p0;
   for (int i0 = nb[leaf]; i0 < ne[leaf]; i0 += PT) {
     const int i = i0 + tid;
@@ -837,13 +841,13 @@ __global__ void __launch_bounds__(PT) k_l2p_p2p32(
       for (int d = 0; d < D; ++d) off[d] = (float)(0.5 * (sbx[d] + sbx[3 + d]) - ct[d]);
       const bool own = sl == leaf;
       for (int j0 = nb[sl]; j0 < ne[sl]; j0 += PT) {
-        __syncthreads();
+        __syncwarp();
         const int j = j0 + tid;
         if (j < ne[sl]) {
           const float4 q = posf[j];
           ss[tid] = make_float4(q.x + off[0], q.y + off[1], q.z + off[2], b32[j]);
         }
-        __syncthreads();
+        __syncwarp();
         const int cnt = min(PT, ne[sl] - j0);
         if (act) {
           float a = 0.f;
@@ -1164,8 +1168,9 @@ int launch_l2p_p2p(FmmPlan *P, cudaStream_t s, const double *pos, int64_t npos, 
   if (mixed) {
     ABX_TRY(P->b32.reserve((size_t)npos));
     k_f64_to_f32<<<ceil_div((size_t)npos, 256), 256, 0, s>>>(b, npos, P->b32.ptr);
-    k_l2p_p2p32<KIND><<<P->nleaves, PT, 0, s>>>(
-        P->D, P->n, P->ncheb, P->leaf_ids.ptr, P->node_begin.ptr, P->node_end.ptr, P->box.ptr, pos,
+    k_l2p_p2p32<KIND><<<ceil_div((size_t)P->nleaves, PW), PT * PW, 0, s>>>(
+        P->D, P->n, P->ncheb, P->nleaves, P->leaf_ids.ptr, P->node_begin.ptr, P->node_end.ptr,
+        P->box.ptr, pos,
         npos, P->posf.ptr, P->b32.ptr, b, P->mi_d.ptr, P->G.ptr, P->p2p_rowptr.ptr,
         P->p2p_src.ptr, P->p0, P->tab, c);
   } else
