@@ -1,7 +1,7 @@
 """Train the learned sparse-approximate-inverse model on the GPU.
 
 Model: the 32 nearest neighbours' positions relative to the row's point,
-scaled by the shape parameter eps (64 features in 2-D), -> MLP (3 hidden
+scaled by the shape parameter eps (32 x dim features), -> MLP (3 hidden
 layers of 128, SiLU) -> the row's 32 weights as m = e_0 + 0.1 y, a correction
 to the identity row.
 
@@ -19,12 +19,14 @@ weights next to near-coincident points) and its rows failed to precondition.
 Rows: only rows whose nearest other point has phi = exp(-(eps d)^2) <= 0.5;
 the preconditioner solves the other rows exactly (exact_phi = 0.5).
 
-Instances: 2-D, uniform or an 8-component Gaussian mixture (sigma 0.05), the
-scaled shape parameter eps*h uniform on [2, 3] (h = N^-1/2), instance seeds
-from 1000 (disjoint from every test seed).  Below eps*h ~ 0.75 the truncated
-Gaussian matrix is numerically singular and no preconditioner reaches 1e-8.
+Instances: 2-D or 3-D (--dim), uniform or an 8-component Gaussian mixture
+(sigma 0.05), the scaled shape parameter eps*h uniform on [2, 3]
+(h = N^(-1/dim)), instance seeds from 1000 (disjoint from every test seed).
+Below eps*h ~ 0.75 the truncated Gaussian matrix is numerically singular and
+no preconditioner reaches 1e-8.
 
     python -m aboria_gb300.spai_train --out aboria_gb300/models/spai_mlp_2d.bin
+    python -m aboria_gb300.spai_train --dim 3 --out aboria_gb300/models/spai_mlp_3d.bin
 """
 from __future__ import annotations
 
@@ -48,7 +50,7 @@ def instance(seed, n, dim=2):
         pos = centres[rng.integers(0, 8, size=n)] + 0.05 * rng.standard_normal((n, dim))
         pos = np.clip(pos, 0.0, np.nextafter(1.0, 0.0))
     eh = rng.uniform(2.0, 3.0)
-    eps = eh * np.sqrt(n)
+    eps = eh * n ** (1.0 / dim)
     return pos, eps
 
 
@@ -75,6 +77,7 @@ def make_model(seed=7, dim=2):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
+    ap.add_argument("--dim", type=int, default=2)
     ap.add_argument("--instances", type=int, default=40)
     ap.add_argument("--n", type=int, default=50000)
     ap.add_argument("--epochs", type=int, default=30)
@@ -82,9 +85,9 @@ def main():
     ap.add_argument("--lr", type=float, default=1e-3)
     args = ap.parse_args()
     t0 = time.time()
-    X = np.concatenate([easy_rows(1000 + i, args.n) for i in range(args.instances)])
+    X = np.concatenate([easy_rows(1000 + i, args.n, args.dim) for i in range(args.instances)])
     print(f"rows {len(X)} in {time.time() - t0:.1f}s", flush=True)
-    m = make_model()
+    m = make_model(dim=args.dim)
     import torch
     Xd = torch.from_numpy(X).cuda()
     rng = np.random.default_rng(3)

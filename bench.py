@@ -298,7 +298,12 @@ def run_ours(args):
     }
     if not args.matvec_only:
         del K
-        out["rbf_solve"] = rbf_section(ctx, ROOT / "aboria_gb300" / "models" / "spai_mlp_2d.bin")
+        models = ROOT / "aboria_gb300" / "models"
+        out["rbf_solve"] = rbf_section(ctx, models / "spai_mlp_2d.bin")
+        out["rbf_solve_3d"] = rbf_section(ctx, models / "spai_mlp_3d.bin", dim=3, n=50000)
+        # plain Schwarz is not run at 2M: its FP64 block LU took 69 s at N=500,000 (3-D)
+        out["rbf_solve_3d_2M"] = rbf_section(ctx, models / "spai_mlp_3d.bin", dim=3, n=2_000_000,
+                                             run_schwarz=False)
         out["fmm"] = fmm_section(ctx)
         out["fmm_16M"] = fmm_section(ctx, n=1 << 24, orders=(5,), steps=1)
     if rank == 0 and not args.no_cpu_baseline:
@@ -323,10 +328,12 @@ def _timed(fn, ctx):
     return out, time.perf_counter() - t0
 
 
-def rbf_section(ctx, model_path):
-    """RBF interpolation solve to 1e-8 FP64 relative residual: 2-D, N=200,000
-    uniform points, f = sin(4 pi x) cos(3 pi y) + 1e-3 noise, compactly
-    supported Gaussian exp(-(eps |dx|)^2) cut at eps |dx| = 4, GMRES(100).
+def rbf_section(ctx, model_path, dim=2, n=None, run_schwarz=True, seed=4040):
+    """RBF interpolation solve to 1e-8 FP64 relative residual: N uniform points
+    in the unit square or cube (2-D N=200,000 with the 2-D model; 3-D N=50,000
+    and 2,000,000 with the 3-D model), eps*h = 2.5 (h = N^(-1/dim)),
+    f = sin(4 pi x) cos(3 pi y) + 1e-3 noise, compactly supported Gaussian
+    exp(-(eps |dx|)^2) cut at eps |dx| = 4, GMRES(100).
 
     * plain   : restricted additive Schwarz on octree leaves of 256 points,
                 blocks factorised by FP64 LU, FP64 operator throughout.
@@ -334,7 +341,7 @@ def rbf_section(ctx, model_path):
                 per row, BF16 tensor-core inference; rows next to a neighbour
                 with kernel value > 0.5 solved exactly in FP64), FP32 operator
                 with FP64 residual refinement; Schwarz taken as fallback when
-                the learned preconditioner has not converged after 60
+                the learned preconditioner has not converged after 100
                 iterations.
     * without_network : the same, with identity rows where the network answers.
     * local_inverse : the exact FP64 local-inverse rows the network is trained
@@ -343,19 +350,19 @@ def rbf_section(ctx, model_path):
     |b - A x| / |b| with the FP64 operator."""
     import aboria_gb300 as ab
     import workloads
-    n = RBF_N
-    eps = RBF_EH * np.sqrt(n)
+    n = n or RBF_N
+    eps = RBF_EH * n ** (1.0 / dim)
     r = 4.0 / eps
-    pos = workloads.uniform(n, 2, seed=4040)
-    p = ab.Particles(2, ctx).set(pos)
-    p.init_octree([0.0, 0.0], [1.0, 1.0], [False, False], 256)
+    pos = workloads.uniform(n, dim, seed=seed)
+    p = ab.Particles(dim, ctx).set(pos)
+    p.init_octree([0.0] * dim, [1.0] * dim, [False] * dim, 256)
     P = p.positions
     f = np.sin(4 * np.pi * P[:, 0]) * np.cos(3 * np.pi * P[:, 1])
-    f += 1e-3 * np.random.default_rng(4041).standard_normal(n)
+    f += 1e-3 * np.random.default_rng(seed + 1).standard_normal(n)
     kern = ab.Kernel.make(ab.K_COMPACT_GAUSSIAN, eps * eps)
     K64 = ab.create_sparse_operator(p, p, r, kern, ab.PREC_FP64)
     K32 = ab.create_sparse_operator(p, p, r, kern, ab.PREC_MIXED)
-    out = {"workload": f"2-D N={n} uniform, compact Gaussian eps*h={RBF_EH} (eps={eps:.1f}), "
+    out = {"workload": f"{dim}-D N={n} uniform, compact Gaussian eps*h={RBF_EH} (eps={eps:.1f}), "
                        f"cut-off r=4/eps={r:.3g}, f=sin(4 pi x)cos(3 pi y)+1e-3 noise, GMRES(100), "
                        f"tol 1e-8 (FP64 residual)"}
 
@@ -366,9 +373,10 @@ def rbf_section(ctx, model_path):
         M = ab.schwarz_preconditioner(K64)
         x, it, res = ab.gmres(K64, f, M=M, restart=100, max_iters=2000, tol=1e-8)
         return x, it, M.stats()
-    (x, it, st), t = _timed(plain, ctx)
-    out["plain_schwarz_fp64"] = {"seconds": t, "iterations": it, "residual": check(x),
-                                 "schwarz_setup_s": st["setup_s"], "domains": st["domains"]}
+    if run_schwarz:
+        (x, it, st), t = _timed(plain, ctx)
+        out["plain_schwarz_fp64"] = {"seconds": t, "iterations": it, "residual": check(x),
+                                     "schwarz_setup_s": st["setup_s"], "domains": st["domains"]}
 
     if model_path.exists():
         mlp = ab.MLP.load(model_path)
@@ -376,7 +384,7 @@ def rbf_section(ctx, model_path):
         def learned(net):
             M = ab.learned_preconditioner(K32, net, eps, exact_phi=EXACT_PHI)
             x, it, res, fb = ab.gmres_with_fallback(K32, f, M, K64, restart=100,
-                                                    learned_max_iters=60, max_iters=2000,
+                                                    learned_max_iters=100, max_iters=2000,
                                                     tol=1e-8, A_check=K64)
             return x, it, fb, M.stats()["domains"]
         (x, it, fb, nex), t = _timed(lambda: learned(mlp), ctx)
@@ -396,7 +404,7 @@ def rbf_section(ctx, model_path):
         return x, it
     (x, it), t = _timed(local_inverse, ctx)
     out["local_inverse_mixed"] = {"seconds": t, "iterations": it, "residual": check(x)}
-    if "learned_mixed" in out:
+    if "learned_mixed" in out and "plain_schwarz_fp64" in out:
         out["speedup_learned_vs_plain"] = (out["plain_schwarz_fp64"]["seconds"]
                                            / out["learned_mixed"]["seconds"])
     return out

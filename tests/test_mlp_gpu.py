@@ -12,6 +12,7 @@ import workloads
 
 pytestmark = pytest.mark.gpu
 MODEL = Path(__file__).resolve().parent.parent / "aboria_gb300" / "models" / "spai_mlp_2d.bin"
+MODEL3 = MODEL.with_name("spai_mlp_3d.bin")
 
 
 def small_model(seed=91):
@@ -145,6 +146,31 @@ def test_trained_network_gain_over_the_method_without_it():
     assert np.array_equal(cols_t, cols_x) and np.array_equal(cols_t, idx)
     assert np.array_equal(vals[~easy], vals_x[~easy])
     assert (~easy).sum() == Mt.stats()["domains"]
+
+
+@pytest.mark.skipif(not MODEL3.exists(), reason="trained model not present")
+def test_trained_3d_network_gain():
+    """The 3-D model on a 3-D test instance: the hybrid approximate inverse with
+    the network reaches 1e-8 (FP64-checked) in under 60% of the iterations of
+    the same method with identity rows (measured 8 vs 22 at N=50,000)."""
+    n, eh = 30000, 2.5
+    pos = workloads.uniform(n, 3, seed=199)
+    eps = eh * n ** (1 / 3)
+    p = ab.Particles(3).set(pos)
+    p.init_octree([0] * 3, [1] * 3, [False] * 3, 256)
+    kern = ab.Kernel.make(ab.K_COMPACT_GAUSSIAN, eps * eps)
+    K64 = ab.create_sparse_operator(p, p, 4 / eps, kern)
+    K32 = ab.create_sparse_operator(p, p, 4 / eps, kern, ab.PREC_MIXED)
+    trained = ab.MLP.load(MODEL3)
+    ident = ab.MLP.load(MODEL3)
+    ident.params = np.zeros(ident.num_params, np.float32)
+    b = np.random.default_rng(200).standard_normal(n)
+    _, it_t, res_t = ab.gmres(K32, b, M=ab.learned_preconditioner(K32, trained, eps), restart=100,
+                              max_iters=1000, tol=1e-8, A_check=K64)
+    _, it_i, res_i = ab.gmres(K32, b, M=ab.learned_preconditioner(K32, ident, eps), restart=100,
+                              max_iters=1000, tol=1e-8, A_check=K64)
+    assert res_t <= 1e-8 and res_i <= 1e-8
+    assert it_t < 0.6 * it_i, (it_t, it_i)
 
 
 def test_fallback_taken_when_learned_fails():
