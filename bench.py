@@ -136,6 +136,24 @@ def dist_setup(args):
     return world, rank, local
 
 
+def slowest_rank(times, world):
+    """Each entry of `times` maximised over the ranks (the job's time is the
+    slowest replica's); gloo reduces on the CPU, NCCL on the GPU."""
+    if world <= 1:
+        return list(times)
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor(list(times), dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
+def replica_throughput(world, steps, seconds):
+    """Whole-job matvecs per second: every replica performs `steps` matvecs."""
+    return world * steps / seconds
+
+
 def barrier(world):
     if world > 1:
         import torch.distributed as dist
@@ -234,14 +252,9 @@ def run_ours(args):
     assert np.array_equal(c_np, c32), "host-buffer matvec differs from device-buffer matvec"
 
     ms = float(np.mean(step_ms))
-    t_total = sum(step_ms) / 1e3
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([t_total, e2e_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_total, e2e_s = float(t[0]), float(t[1])
-    value = world * args.steps / t_total
-    e2e_value = world * args.steps / e2e_s
+    t_total, e2e_s = slowest_rank([sum(step_ms) / 1e3, e2e_s], world)
+    value = replica_throughput(world, args.steps, t_total)
+    e2e_value = replica_throughput(world, args.steps, e2e_s)
 
     peaks, peak_kind = measured_peaks()
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
