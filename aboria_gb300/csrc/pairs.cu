@@ -629,7 +629,7 @@ __device__ __forceinline__ void unit_box(const KParams &P, const int4 qc, bool a
 //   pairs in the rounding band (r2lo, r2hi] are re-decided afterwards with the
 //   exact FP64 test, which is rare enough to run divergently.
 template <int POL, int KIND>
-__global__ void __launch_bounds__(WARPS_PER_CTA * 32, 6)
+__global__ void __launch_bounds__(WARPS_PER_CTA * 32, 7)
     k_pairs_mixed(KParams P) {
   __shared__ WarpSeg seg_all[WARPS_PER_CTA];
   __shared__ WarpTile32 tile_all[WARPS_PER_CTA];
