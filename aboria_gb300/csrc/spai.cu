@@ -433,8 +433,7 @@ __global__ void k_spai_features(const double *__restrict__ pos, int64_t n, int d
                                 float *__restrict__ feats) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * k) return;
-  const int64_t i = t / k;
-  const int j = (int)(t % k);
+  const int64_t i = t / k;  // row; t % k is the support slot
   const int s = knn[t];
   for (int d = 0; d < dim; ++d) {
     double dx = s >= 0 ? pos[(int64_t)d * n + s] - pos[(int64_t)d * n + i] : 0.0;
