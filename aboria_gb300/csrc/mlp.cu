@@ -502,6 +502,8 @@ int mlp_prepare_inference(abx_mlp *M) {
 
 }  // namespace
 
+abx_context *mlp_context(const abx_mlp *M) { return M->ctx; }
+
 int mlp_infer_bf16(abx_mlp *M, const float *x, int64_t n, float *y) {
   ABX_TRY(mlp_prepare_inference(M));
   if (n == 0) return ABX_OK;

@@ -425,6 +425,22 @@ extern "C" int abx_spai_exact_rows(abx_operator *op, int k, int32_t *cols, doubl
 namespace abx {
 int mlp_infer_bf16(abx_mlp *M, const float *x, int64_t n, float *y);
 int mlp_infer_fp32(abx_mlp *M, const float *x, int64_t n, float *y);
+abx_context *mlp_context(const abx_mlp *M);
+
+// Work queued on `to` after this call waits for everything queued on `from`.
+static int stream_order(cudaStream_t from, cudaStream_t to) {
+  if (from == to) return ABX_OK;
+  cudaEvent_t e;
+  ABX_CHECK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  cudaError_t r = cudaEventRecord(e, from);
+  if (r == cudaSuccess) r = cudaStreamWaitEvent(to, e, 0);
+  cudaEventDestroy(e);  // released once the recorded work completes
+  if (r != cudaSuccess) {
+    set_error("stream ordering: %s", cudaGetErrorString(r));
+    return ABX_ERR_CUDA;
+  }
+  return ABX_OK;
+}
 
 namespace {
 // feats[i][j*D + d] = eps * (x_{S_ij} - x_i)_d with periodic minimum image.
@@ -512,6 +528,8 @@ extern "C" int abx_precond_create_learned(abx_operator *op, abx_mlp *mlp, double
   abx_particles *p = op->rows;
   ABX_REQUIRE(p->searchable, ABX_ERR_STATE, "init_neighbour_search not called");
   ABX_REQUIRE(k >= 1 && k <= 64, ABX_ERR_INVALID, "k must be in 1..64");
+  ABX_REQUIRE(mlp_context(mlp)->device == p->ctx->device, ABX_ERR_INVALID,
+              "the model and the operator must be on one device");
   ABX_TRY(ctx_activate(p->ctx));
   const int64_t n = p->n;
   abx_precond *pc = new abx_precond();
@@ -531,9 +549,14 @@ extern "C" int abx_precond_create_learned(abx_operator *op, abx_mlp *mlp, double
       (st = d2.reserve((size_t)n * k + 1)) ||
       (n > 0 && ((st = knn_device(p, k, S->cols.ptr, d2.ptr)) ||
                  (st = spai_features_device(p, S->cols.ptr, k, eps, feats.ptr)) ||
+                 // the model may live on another context (stream) of the same
+                 // device: order its inference after the features and the
+                 // weights' use after the inference
+                 (st = stream_order(p->ctx->stream, mlp_context(mlp)->stream)) ||
                  (st = precision == ABX_PREC_FP64
                            ? mlp_infer_fp32(mlp, feats.ptr, n, y.ptr)
-                           : mlp_infer_bf16(mlp, feats.ptr, n, y.ptr))))) {
+                           : mlp_infer_bf16(mlp, feats.ptr, n, y.ptr)) ||
+                 (st = stream_order(mlp_context(mlp)->stream, p->ctx->stream))))) {
     delete pc->spai;
     delete pc;
     return st;

@@ -311,6 +311,8 @@ def run_ours(args):
     }
     if not args.matvec_only:
         del K
+        out["cfg1"] = cfg1_section(ctx)
+        out["rbf_as_specified"] = cfg4_as_specified(ctx)
         models = ROOT / "aboria_gb300" / "models"
         out["rbf_solve"] = rbf_section(ctx, models / "spai_mlp_2d.bin")
         out["rbf_solve_3d"] = rbf_section(ctx, models / "spai_mlp_3d.bin", dim=3, n=50000)
@@ -392,7 +394,7 @@ def rbf_section(ctx, model_path, dim=2, n=None, run_schwarz=True, seed=4040):
                                      "schwarz_setup_s": st["setup_s"], "domains": st["domains"]}
 
     if model_path.exists():
-        mlp = ab.MLP.load(model_path)
+        mlp = ab.MLP.load(model_path, ctx=ctx)
 
         def learned(net):
             M = ab.learned_preconditioner(K32, net, eps, exact_phi=EXACT_PHI)
@@ -404,7 +406,7 @@ def rbf_section(ctx, model_path, dim=2, n=None, run_schwarz=True, seed=4040):
         out["learned_mixed"] = {"seconds": t, "iterations": it, "residual": check(x),
                                 "fallback_taken": bool(fb), "rows_solved_exactly": nex}
         # the same method without the network: identity rows where it answers
-        ident = ab.MLP.load(model_path)
+        ident = ab.MLP.load(model_path, ctx=ctx)
         ident.params = np.zeros(ident.num_params, np.float32)
         (x, it, fb, nex), t = _timed(lambda: learned(ident), ctx)
         out["without_network_mixed"] = {"seconds": t, "iterations": it, "residual": check(x),
@@ -470,6 +472,93 @@ def fmm_section(ctx, n=1 << 20, orders=(3, 5, 7), n_targets=10000, steps=3):
         res[f"order{order}"] = row
         del K
     return res
+
+
+def _event_ms(fn, stream, reps):
+    import torch
+    ts = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return float(np.median(ts))
+
+
+def cfg1_section(ctx):
+    """The reference's CPU-runnable case: N=100,000 uniform in the unit cube,
+    non-periodic, n_leaf 10, r=0.05, Gaussian exp(-|dx|^2/(r/2)^2), b U[0,1].
+    Cell build, radius counts and K*b in FP64 and mixed precision (CUDA events,
+    medians), pairs per matvec and the mixed error against FP64."""
+    import torch
+    import aboria_gb300 as ab
+    import workloads
+    n, r = 100_000, 0.05
+    stream = torch.cuda.current_stream()
+    pos = workloads.uniform(n, 3, seed=1001)
+    p = ab.Particles(3, ctx).set(pos)
+    p.init_neighbour_search([0, 0, 0], [1, 1, 1], [False] * 3, 10.0)
+    build_ms = _event_ms(lambda: p.init_neighbour_search([0, 0, 0], [1, 1, 1], [False] * 3, 10.0),
+                         stream, 5)
+    P = p.positions
+    count_ms = _event_ms(lambda: ab.radius_count(p, P, r), stream, 5)
+    counts = ab.radius_count(p, P, r)
+    kern = ab.Kernel.make(ab.K_GAUSSIAN, 1.0 / (r / 2) ** 2)
+    b = torch.from_numpy(np.random.default_rng(1002).uniform(0, 1, n)).cuda()
+    c = torch.empty_like(b)
+    out = {"workload": "3-D N=100000 uniform, non-periodic, r=0.05, Gaussian exp(-|dx|^2/(r/2)^2)",
+           "pairs": int(counts.astype(np.int64).sum()),
+           "mean_neighbours": float(counts.mean()),
+           "cell_build_ms": build_ms, "radius_count_ms": count_ms}
+    res = {}
+    for prec, name in ((ab.PREC_FP64, "fp64"), (ab.PREC_MIXED, "mixed")):
+        K = ab.create_sparse_operator(p, p, r, kern, prec)
+        K.matvec(b, out=c)
+        out[f"{name}_matvec_ms"] = _event_ms(lambda: K.matvec(b, out=c, sync=False), stream, 10)
+        res[name] = c.cpu().numpy()
+    out["mixed_vs_fp64_rel_l2"] = float(np.linalg.norm(res["mixed"] - res["fp64"])
+                                        / np.linalg.norm(res["fp64"]))
+    return out
+
+
+def cfg4_as_specified(ctx, iters=100):
+    """Configuration 4 exactly as specified: 2-D, N=200,000 uniform, compact
+    Gaussian with eps=20 and cut-off 0.2 (eps*h = 0.045, ~21,000 neighbours
+    per row).  The truncated flat Gaussian matrix is numerically singular; one
+    GMRES(100) cycle with the plain Schwarz/FP64 preconditioner and the mixed
+    operator, FP64-checked, records how far it gets."""
+    import torch
+    import aboria_gb300 as ab
+    import workloads
+    n, eps, r = 200_000, 20.0, 0.2
+    stream = torch.cuda.current_stream()
+    pos = workloads.uniform(n, 2, seed=4040)
+    p = ab.Particles(2, ctx).set(pos)
+    p.init_octree([0.0, 0.0], [1.0, 1.0], [False, False], 256)
+    P = p.positions
+    f = np.sin(4 * np.pi * P[:, 0]) * np.cos(3 * np.pi * P[:, 1])
+    f += 1e-3 * np.random.default_rng(4041).standard_normal(n)
+    kern = ab.Kernel.make(ab.K_COMPACT_GAUSSIAN, eps * eps)
+    K64 = ab.create_sparse_operator(p, p, r, kern, ab.PREC_FP64)
+    K32 = ab.create_sparse_operator(p, p, r, kern, ab.PREC_MIXED)
+    bd = torch.from_numpy(f).cuda()
+    cd = torch.empty_like(bd)
+    K32.matvec(bd, out=cd)
+    mv_ms = _event_ms(lambda: K32.matvec(bd, out=cd, sync=False), stream, 5)
+    counts = ab.radius_count(p, P, r)
+    M, t_setup = _timed(lambda: ab.schwarz_preconditioner(K64), ctx)
+    st = M.stats()
+    (x, it, res), t = _timed(lambda: ab.gmres(K32, f, M=M, restart=100, max_iters=iters,
+                                               tol=1e-8, A_check=K64), ctx)
+    return {"workload": "2-D N=200000 uniform, compact Gaussian eps=20, cut-off 0.2, GMRES(100), "
+                        "Schwarz FP64 on leaves of 256",
+            "mean_neighbours": float(counts.mean()), "mixed_matvec_ms": mv_ms,
+            "schwarz_setup_s": t_setup, "schwarz_domains": st["domains"],
+            "schwarz_max_size": st["max_size"], "gmres_iterations": it,
+            "fp64_residual_after": res, "gmres_s": t,
+            "note": "numerically singular at eps*h = 0.045: the solve stalls far above 1e-8"}
 
 
 def cpu_baseline(pos, b_by_id, budget_s=15.0):

@@ -11,7 +11,9 @@
  * library's FP64 radius search (abx_radius_query_csr: the same inclusive
  * |dx|^2 <= r^2 test) and keeps the neighbour lists on the device; each
  * K * b launches one kernel instantiated for F in the caller's translation
- * unit, one warp per row, FP64 evaluation and accumulation.  Memory is 8 B
+ * unit, one warp per row, FP64 evaluation and accumulation.  A functor that
+ * returns Vector<double, BR> makes a block operator with BR rows per particle
+ * (the reference's Eigen-block kernels, src/Kernels.h:692-718).  Memory is 8 B
  * per row plus 4 B per pair, so this path is meant for user closures at
  * moderate sizes; the built-in kernels (Aboria::kernels) run on the library's
  * tiled pair kernels without neighbour lists.
@@ -42,6 +44,18 @@ template <unsigned D> struct Domain {
   int periodic[D];
 };
 
+// Rows of a functor's value: 1 for a double, BR for Vector<double, BR> (the
+// reference's block operators, whose kernels return an Eigen BR x 1 block:
+// row i of the operator becomes rows i*BR .. i*BR+BR-1).
+template <typename R> struct BlockRows {
+  static constexpr unsigned value = 1;
+  static __host__ __device__ double get(const R &r, unsigned) { return r; }
+};
+template <unsigned BR> struct BlockRows<Vector<double, BR>> {
+  static constexpr unsigned value = BR;
+  static __host__ __device__ double get(const Vector<double, BR> &r, unsigned k) { return r[k]; }
+};
+
 template <unsigned D, typename F>
 __global__ void functor_sparse_matvec(const int64_t *__restrict__ rowptr,
                                       const int32_t *__restrict__ cols,
@@ -49,13 +63,16 @@ __global__ void functor_sparse_matvec(const int64_t *__restrict__ rowptr,
                                       const double *__restrict__ cpos, Domain<D> dom, F f,
                                       const double *__restrict__ b, double *__restrict__ c,
                                       int64_t nrows) {
+  using R = decltype(f(Vector<double, D>(), int64_t(0), int64_t(0)));
+  constexpr unsigned BR = BlockRows<R>::value;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= nrows) return;
   const int64_t i = warp;
   double xi[D];
   for (unsigned d = 0; d < D; ++d) xi[d] = rpos[i * D + d];
-  double acc = 0.0;
+  double acc[BR];
+  for (unsigned k = 0; k < BR; ++k) acc[k] = 0.0;
   for (int64_t t = rowptr[i] + lane; t < rowptr[i + 1]; t += 32) {
     const int32_t j = cols[t];
     Vector<double, D> dx;
@@ -68,10 +85,14 @@ __global__ void functor_sparse_matvec(const int64_t *__restrict__ rowptr,
       }
       dx[d] = v;
     }
-    acc += f(dx, i, (int64_t)j) * b[j];
+    const R v = f(dx, i, (int64_t)j);
+    for (unsigned k = 0; k < BR; ++k) acc[k] += BlockRows<R>::get(v, k) * b[j];
   }
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if (lane == 0) c[i] = acc;
+  for (unsigned k = 0; k < BR; ++k) {
+    double a = acc[k];
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) c[i * BR + k] = a;
+  }
 }
 
 template <typename T> struct DeviceArray {
@@ -91,7 +112,11 @@ template <typename T> struct DeviceArray {
 /* The operator returned for a user functor; same K * b interface as
  * Aboria::Operator. */
 template <unsigned D, typename F> class FunctorOperator {
+  using R = decltype(std::declval<F>()(Vector<double, D>(), int64_t(0), int64_t(0)));
+
  public:
+  static constexpr unsigned block_rows = detail::BlockRows<R>::value;
+
   template <typename RowP, typename ColP>
   FunctorOperator(const RowP &rows, const ColP &cols, double radius, F f)
       : nrows_(int64_t(rows.size())), ncols_(int64_t(cols.size())), f_(f) {
@@ -134,9 +159,10 @@ template <unsigned D, typename F> class FunctorOperator {
     nnz_ = nnz;
   }
 
-  int64_t rows() const { return nrows_; }
+  int64_t rows() const { return nrows_ * block_rows; }
   int64_t cols() const { return ncols_; }
-  int64_t nonzeros() const { return nnz_; }
+  /* stored pairs times the block size (the reference's assembled nnz) */
+  int64_t nonzeros() const { return nnz_ * block_rows; }
 
   /* c = K * b with b and c in device memory, on the legacy default stream. */
   void apply_device(const double *b, double *c) const {
@@ -153,15 +179,16 @@ template <unsigned D, typename F> class FunctorOperator {
       detail::check(ABX_ERR_INVALID, "K*b: size of b does not match the operator's columns");
       return Vec();
     }
-    Vec c(static_cast<size_t>(nrows_));
-    detail::DeviceArray<double> db(static_cast<size_t>(ncols_)), dc(static_cast<size_t>(nrows_));
+    Vec c(static_cast<size_t>(nrows_ * block_rows));
+    detail::DeviceArray<double> db(static_cast<size_t>(ncols_)),
+        dc(static_cast<size_t>(nrows_ * block_rows));
     if (ncols_)
       detail::check_cuda(cudaMemcpy(db.ptr, b.data(), size_t(ncols_) * sizeof(double),
                                     cudaMemcpyHostToDevice),
                          "cudaMemcpy");
     apply_device(db.ptr, dc.ptr);
     if (nrows_)
-      detail::check_cuda(cudaMemcpy(c.data(), dc.ptr, size_t(nrows_) * sizeof(double),
+      detail::check_cuda(cudaMemcpy(c.data(), dc.ptr, size_t(nrows_ * block_rows) * sizeof(double),
                                     cudaMemcpyDeviceToHost),
                          "cudaMemcpy");
     return c;

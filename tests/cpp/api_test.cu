@@ -28,6 +28,16 @@ template <typename T> static void write(const std::string &path, const std::vect
 }
 
 #ifdef __CUDACC__
+struct SumFunctor {  // get<scalar1>(a) + get<scalar2>(b) with constant scalars
+  double s1, s2;
+  __host__ __device__ double operator()(const vdouble3 &, int64_t, int64_t) const { return s1 + s2; }
+};
+struct BlockFunctor {  // the 2 x 1 block kernel (s1 + s2, s1 - s2)
+  double s1, s2;
+  __host__ __device__ Vector<double, 2> operator()(const vdouble3 &, int64_t, int64_t) const {
+    return Vector<double, 2>(s1 + s2, s1 - s2);
+  }
+};
 struct GaussianFunctor {
   double inv_c2;
   __host__ __device__ double operator()(const vdouble3 &dx, int64_t, int64_t) const {
@@ -92,6 +102,32 @@ static int run(const char *in, const std::string &out) {
   auto Kf = create_sparse_operator(particles, particles, r, GaussianFunctor{1.0 / (c * c)});
   std::vector<double> kf = Kf * bs;
   write(out + "/kf.bin", kf);
+  {
+    // tests/operators.h:810-963: three particles 0.09 apart, diameter 0.1,
+    // scalar1 = 1 and scalar2 = 2 on every particle; the scalar kernel
+    // s1_a + s2_b and the 2 x 1 block kernel (s1_a + s2_b, s1_a - s2_b)
+    Cells3 kat;
+    for (int q = 0; q < 3; ++q) kat.push_back(vdouble3(0.09 * q, 0, 0));
+    kat.init_neighbour_search(vdouble3(-1, -1, -1), vdouble3(1, 1, 1), vbool3(false, false, false));
+    std::vector<double> v(3);
+    for (int q = 0; q < 3; ++q) v[size_t(q)] = double(get<id>(kat)[size_t(q)] + 1);  // v = (1, 2, 3) by id
+    auto C = create_sparse_operator(kat, kat, 0.1, SumFunctor{1.0, 2.0});
+    auto C2 = create_sparse_operator(kat, kat, 0.1, BlockFunctor{1.0, 2.0});
+    std::vector<double> a1 = C * v, a2 = C2 * v;
+    std::vector<double> res;  // by id: answer, then block answer, then nnz
+    std::vector<double> r1(3), r2(6);
+    for (int q = 0; q < 3; ++q) {
+      const int64_t pid = get<id>(kat)[size_t(q)];
+      r1[size_t(pid)] = a1[size_t(q)];
+      r2[size_t(2 * pid)] = a2[size_t(2 * q)];
+      r2[size_t(2 * pid + 1)] = a2[size_t(2 * q + 1)];
+    }
+    res.insert(res.end(), r1.begin(), r1.end());
+    res.insert(res.end(), r2.begin(), r2.end());
+    res.push_back(double(C.nonzeros()));
+    res.push_back(double(C2.nonzeros()));
+    write(out + "/kat.bin", res);
+  }
 #endif
 
   // tests/rbf_interpolation.h pattern: GMRES with SchwartzPreconditioner on an

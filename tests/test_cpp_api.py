@@ -10,6 +10,7 @@ tests; its outputs are compared with the oracle: storage order and neighbour
 sets bit-exact, K*b to 1e-12, the functor operator against the built-in
 kernel to 1e-12, the Schwarz-preconditioned GMRES residual, FMM to 1e-10.
 """
+import json
 import os
 import shutil
 import signal
@@ -96,6 +97,18 @@ def test_cpp_api_parity(tmp_path):
     assert np.max(np.abs(kb - ref)) <= 1e-12 * np.max(np.abs(ref))
     kf = np.fromfile(out / "kf.bin", np.float64)
     assert np.max(np.abs(kf - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+    # the reference's sparse and block operator known answers, with the
+    # user-functor path (tests/operators.h:810-963)
+    kat = json.loads((ROOT / "tests" / "golden" / "reference_kats.json").read_text())["sparse_operator"]
+    got = np.fromfile(out / "kat.bin", np.float64)
+    assert np.array_equal(got[:3], kat["answer"])
+    # the block answer: the entries the reference asserts, then the whole
+    # vector against the product of the 6 x 3 block matrix its kernel defines
+    assert np.array_equal(got[3:6], kat["block_answer_asserted"])
+    C2 = np.array([[3, 3, 0], [-1, -1, 0], [3, 3, 3], [-1, -1, -1], [0, 3, 3], [0, -1, -1]], float)
+    assert np.array_equal(got[3:9], C2 @ np.array([1.0, 2.0, 3.0]))
+    assert got[9] == kat["nonzeros"] and got[10] == kat["block_nonzeros"]
 
     it, err, true_res = np.fromfile(out / "solve.bin", np.float64)
     assert err <= 1e-10 and true_res <= 1.0001e-10 and it < 500

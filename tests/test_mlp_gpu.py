@@ -148,6 +148,20 @@ def test_trained_network_gain_over_the_method_without_it():
     assert (~easy).sum() == Mt.stats()["domains"]
 
 
+@pytest.mark.skipif(not MODEL.exists(), reason="trained model not present")
+def test_model_on_another_context_gives_the_same_rows():
+    """The model and the operator may live on different contexts (streams) of
+    one device: the library orders the inference between them, so the rows
+    are bit-identical to the same-context ones."""
+    p, K, eps = rbf_problem(40000, 2.5, seed=103)
+    same = ab.MLP.load(MODEL, ctx=p.ctx)
+    other = ab.MLP.load(MODEL, ctx=ab.Context(0))
+    _, v_same = ab.spai_rows(ab.learned_preconditioner(K, same, eps))
+    for _ in range(3):
+        _, v_other = ab.spai_rows(ab.learned_preconditioner(K, other, eps))
+        assert np.array_equal(v_same, v_other)
+
+
 @pytest.mark.skipif(not MODEL3.exists(), reason="trained model not present")
 def test_trained_3d_network_gain():
     """The 3-D model on a 3-D test instance: the hybrid approximate inverse with
