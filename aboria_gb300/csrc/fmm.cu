@@ -64,7 +64,8 @@ struct FmmPlan {
   DevBuf<int> m2l;
   int n_m2l = 0;
   DevBuf<double> Km;      // nmat x ncheb x ncheb
-  DevBuf<float> Kmh, Kml; // split-TF32 hi/lo parts of the FP32 copy (tensor-core M2L)
+  DevBuf<float> Kmh, Kml; // split-TF32 hi/lo parts of the FP32 copy (mma.sync M2L, ncheb <= 64)
+  DevBuf<float> Kp;       // the same packed as tcgen05 stage images (ncheb > 64, k_pack_tf32)
   DevBuf<float> W32l;     // lo part of W (the tcgen05 M2L reads W32 as the hi part)
   int nmat = 0;
   // M2L grouped by matrix (for the tensor-core GEMM): per matrix a list of
@@ -432,26 +433,66 @@ __global__ void __launch_bounds__(64 * WM) k_m2l_tc2(int ncheb, int ldk, int ldg
 }
 
 // ------------------------------------------------- M2L on tcgen05 (TMEM) ---
-// The same tile GEMM on the 5th-generation tensor cores: one CTA (4 warps)
-// per (M2L matrix, T5_N-pair tile, 128-row block).  K (hi, lo: split once per
-// plan) and the gathered source expansions W (hi, lo: split once per matvec)
-// are copied T5_KB columns at a time by cp.async into a T5_S-stage ring in the
+// The same tile GEMM on the 5th-generation tensor cores.  One CTA (4 warps)
+// per (M2L matrix, T5_N-pair tile) computes all NRB = ceil(ncheb/128) row
+// blocks, so the gathered source expansions of the tile are read once:
+//   G[targets][rb*128 + r] += sum_k K[rb*128 + r][k] * W[sources][k]
+// as split TF32 (K = Kh + Kl, W = Wh + Wl; Kl Wh + Kh Wl + Kh Wh) on
+// tcgen05.mma kind::tf32 into NRB accumulators of 128 x T5_N FP32 in TMEM.
+// The K matrices are packed once per plan into the shared-memory image of a
+// pipeline stage (k_pack_tf32), so a stage's A operand is one bulk copy on the
+// TMA engine (cp.async.bulk, completion counted on the stage's `full`
+// mbarrier) and bypasses the load/store pipeline; the W rows of the tile's
+// sources are gathered 16 bytes per thread with cp.async.  Operands use the
 // no-swizzle K-major core-matrix layout (8 rows x 16 bytes per core matrix;
-// the descriptor's leading byte offset is the core-matrix stride along K,
-// the stride byte offset along rows).  Thread 0 issues, per 8-column step,
-// the three split-TF32 products lo*hi, hi*lo, hi*hi as tcgen05.mma
-// kind::tf32 into one 128 x T5_N FP32 accumulator in TMEM and commits each
-// stage to its mbarrier; a stage is refilled only after that barrier
+// the descriptor's leading byte offset is the core-matrix stride along K, the
+// stride byte offset along rows).  Thread 0 waits for the stage's bulk copy,
+// issues the 3 NRB MMAs of each 8-column block and commits them to the
+// stage's `done` mbarrier; a stage is refilled only after that barrier
 // completes.  Every wait is bounded: on timeout the kernel sets *status,
-// skips the epilogue and still releases its TMEM.  Epilogue: each warp reads
-// its 32 accumulator lanes (rows) with tcgen05.ld and adds them into G with
+// skips the epilogue, waits (bounded) for its last commit and still releases
+// its TMEM.  The ring depth keeps the CTAs resident on an SM (by shared
+// memory) within the SM's 512 TMEM columns.  Epilogue: each warp reads its 32
+// accumulator lanes (rows) with tcgen05.ld and adds them into G with
 // reductions that are coalesced along the rows.
-constexpr int T5_M = 128, T5_N = 128, T5_KB = 8, T5_S = 3;
-static_assert(T5_N % 16 == 0 && T5_N <= 128, "one pair per thread when loading the tile");
-constexpr int T5_A = T5_M * T5_KB * 4, T5_B = T5_N * T5_KB * 4;  // bytes per operand part
-constexpr int T5_STAGE = 2 * T5_A + 2 * T5_B;                     // hi + lo of A and B
-constexpr size_t T5_SMEM = T5_S * (size_t)T5_STAGE + 1024 + 2048;  // + alignment, barriers, indices
-constexpr int T5_SPIN = 1 << 26;  // mbarrier polls before giving up (seconds at most)
+constexpr int T5_N = 128, T5_KB = 8;
+constexpr int T5_PART = 128 * T5_KB * 4;  // bytes of one operand part: 128 rows x 8 columns
+constexpr int T5_SPIN = 1 << 26;          // mbarrier polls before giving up (seconds at most)
+template <int NRB> struct T5Cfg {
+  static constexpr int S = NRB == 1 ? 3 : (NRB == 2 ? 4 : (NRB == 3 ? 6 : 5));  // ring depth
+  static constexpr int A_BYTES = NRB * 2 * T5_PART;       // K hi, lo of every row block
+  static constexpr int STAGE = A_BYTES + 2 * T5_PART;     // + W hi, lo of the T5_N pairs
+  static constexpr size_t SMEM = (size_t)S * STAGE + 1024 + 2048;  // + alignment, barriers, indices
+  static constexpr uint32_t TCOLS = NRB == 1 ? 128u : (NRB == 2 ? 256u : 512u);
+};
+static_assert(T5Cfg<1>::SMEM * 5 > 228 * 1024 && T5Cfg<2>::SMEM * 3 > 228 * 1024 &&
+                  T5Cfg<3>::SMEM * 2 > 228 * 1024 && T5Cfg<4>::SMEM * 2 > 228 * 1024,
+              "resident CTAs per SM must fit the SM's 512 TMEM columns");
+static_assert(T5Cfg<3>::SMEM <= 227 * 1024 && T5Cfg<4>::SMEM <= 227 * 1024, "shared memory per CTA");
+
+// Packed split-TF32 M2L matrices: per (matrix, 8-column block kb, 128-row
+// block rb, part hi/lo) the 4 KB shared-memory image of the operand tile,
+// element (r, k) at ((k/4) * 16 + r/8) * 128 + (r%8) * 16 + (k%4) * 4 bytes;
+// zero beyond ncheb.  hi = tf32(K), lo = tf32(K - hi).
+__global__ void k_pack_tf32(const double *__restrict__ K, int64_t nmat, int ncheb, int nkb,
+                            int nrb, float *__restrict__ out) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nmat * nkb * nrb * 2 * (T5_PART / 4)) return;
+  int64_t t = e;
+  const int w = (int)(t % (T5_PART / 4));
+  t /= T5_PART / 4;
+  const int part = (int)(t % 2);
+  t /= 2;
+  const int rb = (int)(t % nrb);
+  t /= nrb;
+  const int kb = (int)(t % nkb);
+  const int64_t m = t / nkb;
+  const int kk = w & 3, rl = (w >> 2) & 7, rh = (w >> 5) & 15, kq = w >> 9;
+  const int i = rb * 128 + rh * 8 + rl, k = kb * T5_KB + kq * 4 + kk;
+  const float f = (i < ncheb && k < ncheb) ? (float)K[(m * ncheb + i) * ncheb + k] : 0.f;
+  const uint32_t h = f2tf32(f);
+  out[e] = part == 0 ? __uint_as_float(h) : __uint_as_float(f2tf32(f - __uint_as_float(h)));
+}
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -489,9 +530,9 @@ __device__ __forceinline__ void cp16(uint32_t dst, const void *src, int nbytes) 
                : "memory");
 }
 
-__global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int ldk, int ldg,
-                                                 const float *__restrict__ Kh,
-                                                 const float *__restrict__ Kl,
+template <int NRB>
+__global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int nkb, int ldk, int ldg,
+                                                 const float *__restrict__ Ap,
                                                  const int2 *__restrict__ pairs,
                                                  const int *__restrict__ mat_off,
                                                  const int *__restrict__ tile_mat,
@@ -499,13 +540,16 @@ __global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int ldk, int ldg,
                                                  const float *__restrict__ Wh,
                                                  const float *__restrict__ Wl,
                                                  float *__restrict__ G32, int *__restrict__ status) {
+  using C = T5Cfg<NRB>;
+  constexpr int S = C::S;
   extern __shared__ __align__(128) unsigned char t5raw[];
   unsigned char *sm = (unsigned char *)(((uintptr_t)t5raw + 1023) & ~(uintptr_t)1023);
-  uint64_t *mbar = (uint64_t *)(sm + T5_S * T5_STAGE);
-  uint32_t *tslot = (uint32_t *)(mbar + T5_S);
-  int *sSrc = (int *)(tslot + 4), *sTgt = sSrc + T5_N;
+  uint64_t *full = (uint64_t *)(sm + S * C::STAGE);
+  uint64_t *done = full + S;
+  uint32_t *tslot = (uint32_t *)(done + S);
+  int *sSrc = (int *)(tslot + 4), *sTgt = sSrc + T5_N, *sLast = sTgt + T5_N;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int tile = blockIdx.x, i0 = blockIdx.y * T5_M;
+  const int tile = blockIdx.x;
   const int m = tile_mat[tile], p0 = tile_first[tile];
   const int np = min(T5_N, mat_off[m + 1] - p0);
   if (tid < T5_N) {
@@ -514,95 +558,108 @@ __global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int ldk, int ldg,
     sSrc[tid] = pr.y;
   }
   if (tid == 0) {
-    for (int q = 0; q < T5_S; ++q)
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[q])));
+    for (int q = 0; q < S; ++q) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&full[q])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&done[q])));
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_addr(tslot)),
-                 "r"(T5_N));
+                 "r"(C::TCOLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   }
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tslot;
-  const float *Ah = Kh + (size_t)m * ncheb * ldk, *Al = Kl + (size_t)m * ncheb * ldk;
-  const int nkb = ldk / T5_KB;
-  constexpr uint32_t idesc = umma_idesc_tf32(T5_M, T5_N);
+  const unsigned char *Am = (const unsigned char *)Ap + (size_t)m * nkb * C::A_BYTES;
+  constexpr uint32_t idesc = umma_idesc_tf32(128, T5_N);
   const uint32_t smbase = smem_addr(sm);
+  int nfill = 0, ncons = 0;  // thread 0: bulk copies issued / waited for
 
-  // copies of k-block kb into stage kb % T5_S (one cp.async group)
+  // block kb into stage kb % S: K by one bulk copy (thread 0), W by cp.async
+  // (one group per thread)
   auto load_block = [&](int kb) {
-    const int k0 = kb * T5_KB;
-    const uint32_t st = smbase + (uint32_t)((kb % T5_S) * T5_STAGE);
-    // A: element (r, k) at ((k/4) * 16 + r/8) * 128 + (r%8) * 16 + (k%4) * 4
-    for (int e = tid; e < T5_M * (T5_KB / 4); e += 128) {
-      const int rl = e & 7, kq = (e >> 3) % (T5_KB / 4), rh = (e >> 3) / (T5_KB / 4);
-      const int r = rh * 8 + rl, i = i0 + r;
-      const int ic = min(i, ncheb - 1);
-      const uint32_t off = (uint32_t)((kq * (T5_M / 8) + rh) * 128 + rl * 16);
-      const size_t g = (size_t)ic * ldk + k0 + kq * 4;
-      cp16(st + off, Ah + g, i < ncheb ? 16 : 0);
-      cp16(st + T5_A + off, Al + g, i < ncheb ? 16 : 0);
+    const uint32_t st = smbase + (uint32_t)((kb % S) * C::STAGE);
+    if (tid == 0) {
+      ++nfill;
+      const uint32_t fb = smem_addr(&full[kb % S]);
+      asm volatile(
+          "{\n\t.reg .b64 state;\n\t"
+          "mbarrier.arrive.expect_tx.shared::cta.b64 state, [%0], %1;\n\t}" ::"r"(fb),
+          "r"(C::A_BYTES)
+          : "memory");
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+              st),
+          "l"(Am + (size_t)kb * C::A_BYTES), "r"(C::A_BYTES), "r"(fb)
+          : "memory");
     }
-    // B: the tile's source expansions
+#pragma unroll
     for (int e = tid; e < T5_N * (T5_KB / 4); e += 128) {
-      const int rl = e & 7, kq = (e >> 3) % (T5_KB / 4), rh = (e >> 3) / (T5_KB / 4);
-      const int q = rh * 8 + rl;
-      const int src = sSrc[q];
+      const int rl = e & 7, kq = (e >> 3) & 1, rh = e >> 4;
+      const int src = sSrc[rh * 8 + rl];
       const uint32_t off = (uint32_t)((kq * (T5_N / 8) + rh) * 128 + rl * 16);
-      const size_t g = (size_t)(src >= 0 ? src : 0) * ldk + k0 + kq * 4;
-      cp16(st + 2 * T5_A + off, Wh + g, src >= 0 ? 16 : 0);
-      cp16(st + 2 * T5_A + T5_B + off, Wl + g, src >= 0 ? 16 : 0);
+      const size_t g = (size_t)(src >= 0 ? src : 0) * ldk + kb * T5_KB + kq * 4;
+      cp16(st + C::A_BYTES + off, Wh + g, src >= 0 ? 16 : 0);
+      cp16(st + C::A_BYTES + T5_PART + off, Wl + g, src >= 0 ? 16 : 0);
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
   };
 
-  for (int kb = 0; kb < T5_S - 1; ++kb) {
+  for (int kb = 0; kb < S - 1; ++kb) {
     if (kb < nkb) load_block(kb);
     else asm volatile("cp.async.commit_group;" ::: "memory");
   }
   bool ok = true;
+  int last = -1;  // thread 0: the last block whose MMAs were committed
   for (int kb = 0; kb < nkb; ++kb) {
-    const int st = kb % T5_S;
-    // this thread's copies of block kb have landed (at most T5_S - 2 newer groups pending)
-    asm volatile("cp.async.wait_group %0;" ::"n"(T5_S - 2) : "memory");
+    const int st = kb % S;
+    // this thread's W copies of block kb have landed (at most S - 2 newer groups pending)
+    asm volatile("cp.async.wait_group %0;" ::"n"(S - 2) : "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
-    if (tid == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t base = smbase + (uint32_t)(st * T5_STAGE);
-      const uint32_t a_ks = (T5_M / 8) * 128, b_ks = (T5_N / 8) * 128;
+    if (tid == 0 && ok) {
+      if (!mbar_wait(smem_addr(&full[st]), (kb / S) & 1)) {
+        ok = false;
+      } else {
+        ++ncons;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t base = smbase + (uint32_t)(st * C::STAGE);
+        constexpr uint32_t ks = (128 / 8) * 128;  // core-matrix stride along K
+        const uint64_t bh = umma_desc(base + C::A_BYTES, ks, 128);
+        const uint64_t bl = umma_desc(base + C::A_BYTES + T5_PART, ks, 128);
 #pragma unroll
-      for (int j = 0; j < T5_KB / 8; ++j) {
-        const uint64_t ah = umma_desc(base + 2 * j * a_ks, a_ks, 128);
-        const uint64_t al = umma_desc(base + T5_A + 2 * j * a_ks, a_ks, 128);
-        const uint64_t bh = umma_desc(base + 2 * T5_A + 2 * j * b_ks, b_ks, 128);
-        const uint64_t bl = umma_desc(base + 2 * T5_A + T5_B + 2 * j * b_ks, b_ks, 128);
-        const uint64_t ad[3] = {al, ah, ah}, bd[3] = {bh, bl, bh};
+        for (int rb = 0; rb < NRB; ++rb) {
+          const uint64_t ah = umma_desc(base + rb * 2 * T5_PART, ks, 128);
+          const uint64_t al = umma_desc(base + rb * 2 * T5_PART + T5_PART, ks, 128);
+          const uint64_t ad[3] = {al, ah, ah}, bd[3] = {bh, bl, bh};
 #pragma unroll
-        for (int t = 0; t < 3; ++t) {
-          const uint32_t acc = (kb > 0 || j > 0 || t > 0) ? 1u : 0u;
-          asm volatile(
-              "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-              "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
-              "l"(ad[t]), "l"(bd[t]), "r"(idesc), "r"(acc));
+          for (int t = 0; t < 3; ++t) {
+            const uint32_t acc = (kb > 0 || t > 0) ? 1u : 0u;
+            asm volatile(
+                "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(
+                    tmem + (uint32_t)(rb * T5_N)),
+                "l"(ad[t]), "l"(bd[t]), "r"(idesc), "r"(acc));
+          }
         }
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                smem_addr(&done[st])));
+        last = kb;
       }
-      asm volatile(
-          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-              smem_addr(&mbar[st])));
     }
-    // refill the stage that block kb - 1 used with block kb + T5_S - 1, once
+    // refill the stage that block kb - 1 used with block kb + S - 1, once
     // block kb - 1's MMAs have completed (the c-th commit on a stage's barrier
     // completes its phase c)
-    const int nb = kb + T5_S - 1;
+    const int nb = kb + S - 1;
     if (nb < nkb) {
-      if (kb >= 1) {
-        const int pst = (kb - 1) % T5_S;
-        if (!mbar_wait(smem_addr(&mbar[pst]), ((kb - 1) / T5_S) & 1)) ok = false;
+      if (kb >= 1 && ok) {
+        const int pst = (kb - 1) % S;
+        if (!mbar_wait(smem_addr(&done[pst]), ((kb - 1) / S) & 1)) ok = false;
       }
       if (!__syncthreads_and(ok)) {
         ok = false;
@@ -614,34 +671,41 @@ __global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int ldk, int ldg,
     }
   }
   asm volatile("cp.async.wait_all;" ::: "memory");
-  // the last block's commit covers every MMA issued before it
-  const int lst = (nkb - 1) % T5_S;
-  const uint32_t lpar = ((nkb - 1) / T5_S) & 1;
-  if (ok && nkb > 0 && !mbar_wait(smem_addr(&mbar[lst]), lpar)) ok = false;
+  if (tid == 0) *sLast = last;
+  __syncthreads();
+  // the last commit covers every MMA issued before it
+  const int lst = *sLast;
+  if (lst >= 0 && !mbar_wait(smem_addr(&done[lst % S]), (lst / S) & 1)) ok = false;
+  if (lst != nkb - 1) ok = false;
   ok = __syncthreads_and(ok);
   if (!ok) {
-    if (tid == 0) atomicExch(status, 1);
-    // let anything still in flight drain (bounded) before the TMEM is released
-    if (nkb > 0) mbar_wait(smem_addr(&mbar[lst]), lpar);
+    if (tid == 0) {
+      atomicExch(status, 1);
+      // bulk copies still in flight land before the shared memory is released
+      for (int kb = ncons; kb < nfill; ++kb) mbar_wait(smem_addr(&full[kb % S]), (kb / S) & 1);
+    }
   } else {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const int r = 32 * warp + lane, i = i0 + r;
 #pragma unroll
-    for (int c0 = 0; c0 < T5_N; c0 += 16) {
-      uint32_t v[16];
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-          "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-            "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
-            "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-          : "r"(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0));
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (i < ncheb) {
+    for (int rb = 0; rb < NRB; ++rb) {
+      const int i = rb * 128 + 32 * warp + lane;
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          const int tgt = sTgt[c0 + q];
-          if (tgt >= 0) atomicAdd(&G32[(size_t)tgt * ldg + i], __uint_as_float(v[q]));
+      for (int c0 = 0; c0 < T5_N; c0 += 16) {
+        uint32_t v[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+            "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+              "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+              "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+            : "r"(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(rb * T5_N + c0)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (i < ncheb) {
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            const int tgt = sTgt[c0 + q];
+            if (tgt >= 0) atomicAdd(&G32[(size_t)tgt * ldg + i], __uint_as_float(v[q]));
+          }
         }
       }
     }
@@ -649,7 +713,7 @@ __global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int ldk, int ldg,
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(T5_N));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::TCOLS));
 }
 
 // G[node][i] += G32[node][i] for the padded FP32 accumulator (row stride ldg).
@@ -1219,43 +1283,60 @@ int fmm_matvec_device(abx_operator *op, const double *b, double *c) {
       const int ldk = (nc + 31) / 32 * 32;
       ABX_TRY(P->W32.reserve((size_t)P->nnodes * ldk));
       ABX_TRY(P->G32.reserve((size_t)P->nnodes * ldg));
-      if (!P->Kmh.ptr) {
-        const size_t nk = (size_t)P->nmat * nc * ldk;
-        ABX_TRY(P->Kmh.reserve(nk));
-        ABX_TRY(P->Kml.reserve(nk));
-        k_split_tf32<<<ceil_div(nk, 256), 256, 0, s>>>(P->Km.ptr, (int64_t)P->nmat * nc, nc, ldk,
-                                                       P->Kmh.ptr, P->Kml.ptr);
-      }
-      k_to_f32_padded<<<ceil_div((size_t)P->nnodes * ldk, 256), 256, 0, s>>>(
-          P->W.ptr, P->nnodes, nc, ldk, P->W32.ptr);
       ABX_CHECK_CUDA(cudaMemsetAsync(P->G32.ptr, 0, (size_t)P->nnodes * ldg * 4, s));
-      auto launch_m2l = [&](auto kern, int mt, int threads, size_t smem) -> int {
-        ABX_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)smem));
-        const dim3 grid(P->ntiles, (nc + mt - 1) / mt);
-        kern<<<grid, threads, smem, s>>>(nc, ldk, ldg, P->Kmh.ptr, P->Kml.ptr, P->m2l_by_mat.ptr,
-                                         P->mat_off_d.ptr, P->tile_mat.ptr, P->tile_first.ptr,
-                                         P->W32.ptr, P->G32.ptr);
-        return ABX_OK;
-      };
-      if (nc <= 32) {
-        ABX_TRY(launch_m2l(k_m2l_tc2<1>, M2Cfg<1>::MT, M2Cfg<1>::THREADS, M2Cfg<1>::SMEM));
-      } else if (nc <= 64) {
-        ABX_TRY(launch_m2l(k_m2l_tc2<2>, M2Cfg<2>::MT, M2Cfg<2>::THREADS, M2Cfg<2>::SMEM));
+      if (nc <= 64) {
+        // mma.sync tiles (a 128-row tcgen05 tile would be mostly padding)
+        if (!P->Kmh.ptr) {
+          const size_t nk = (size_t)P->nmat * nc * ldk;
+          ABX_TRY(P->Kmh.reserve(nk));
+          ABX_TRY(P->Kml.reserve(nk));
+          k_split_tf32<<<ceil_div(nk, 256), 256, 0, s>>>(P->Km.ptr, (int64_t)P->nmat * nc, nc,
+                                                         ldk, P->Kmh.ptr, P->Kml.ptr);
+        }
+        k_to_f32_padded<<<ceil_div((size_t)P->nnodes * ldk, 256), 256, 0, s>>>(
+            P->W.ptr, P->nnodes, nc, ldk, P->W32.ptr);
+        auto launch_m2l = [&](auto kern, int mt, int threads, size_t smem) -> int {
+          ABX_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem));
+          const dim3 grid(P->ntiles, (nc + mt - 1) / mt);
+          kern<<<grid, threads, smem, s>>>(nc, ldk, ldg, P->Kmh.ptr, P->Kml.ptr,
+                                           P->m2l_by_mat.ptr, P->mat_off_d.ptr, P->tile_mat.ptr,
+                                           P->tile_first.ptr, P->W32.ptr, P->G32.ptr);
+          return ABX_OK;
+        };
+        if (nc <= 32)
+          ABX_TRY(launch_m2l(k_m2l_tc2<1>, M2Cfg<1>::MT, M2Cfg<1>::THREADS, M2Cfg<1>::SMEM));
+        else
+          ABX_TRY(launch_m2l(k_m2l_tc2<2>, M2Cfg<2>::MT, M2Cfg<2>::THREADS, M2Cfg<2>::SMEM));
       } else {
-        // 5th-generation tensor cores (tcgen05, TMEM accumulator)
+        // 5th-generation tensor cores (tcgen05, TMEM accumulators)
+        const int nkb = (nc + T5_KB - 1) / T5_KB;
+        const int nrb = (nc + 127) / 128;  // 1..4 for orders 5..8
+        if (!P->Kp.ptr) {
+          const size_t nk = (size_t)P->nmat * nkb * nrb * 2 * (T5_PART / 4);
+          ABX_TRY(P->Kp.reserve(nk));
+          k_pack_tf32<<<ceil_div(nk, 256), 256, 0, s>>>(P->Km.ptr, P->nmat, nc, nkb, nrb,
+                                                        P->Kp.ptr);
+        }
         ABX_TRY(P->W32l.reserve((size_t)P->nnodes * ldk));
         k_split_tf32<<<ceil_div((size_t)P->nnodes * ldk, 256), 256, 0, s>>>(
             P->W.ptr, P->nnodes, nc, ldk, P->W32.ptr, P->W32l.ptr);
         int *status = p->ctx->dev_flag.ptr + 8;
         ABX_CHECK_CUDA(cudaMemsetAsync(status, 0, sizeof(int), s));
-        ABX_CHECK_CUDA(cudaFuncSetAttribute(k_m2l_tc5, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)T5_SMEM));
-        const dim3 grid(P->ntiles, (nc + T5_M - 1) / T5_M);
-        k_m2l_tc5<<<grid, 128, T5_SMEM, s>>>(nc, ldk, ldg, P->Kmh.ptr, P->Kml.ptr,
-                                              P->m2l_by_mat.ptr, P->mat_off_d.ptr,
-                                              P->tile_mat.ptr, P->tile_first.ptr, P->W32.ptr,
-                                              P->W32l.ptr, P->G32.ptr, status);
+        auto launch_tc5 = [&](auto kern, size_t smem) -> int {
+          ABX_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem));
+          kern<<<P->ntiles, 128, smem, s>>>(nc, nkb, ldk, ldg, P->Kp.ptr, P->m2l_by_mat.ptr,
+                                            P->mat_off_d.ptr, P->tile_mat.ptr, P->tile_first.ptr,
+                                            P->W32.ptr, P->W32l.ptr, P->G32.ptr, status);
+          return ABX_OK;
+        };
+        switch (nrb) {
+          case 1: ABX_TRY(launch_tc5(k_m2l_tc5<1>, T5Cfg<1>::SMEM)); break;
+          case 2: ABX_TRY(launch_tc5(k_m2l_tc5<2>, T5Cfg<2>::SMEM)); break;
+          case 3: ABX_TRY(launch_tc5(k_m2l_tc5<3>, T5Cfg<3>::SMEM)); break;
+          default: ABX_TRY(launch_tc5(k_m2l_tc5<4>, T5Cfg<4>::SMEM)); break;
+        }
         ABX_CHECK_CUDA(cudaGetLastError());
         int st = 0;
         ABX_CHECK_CUDA(cudaMemcpyAsync(&st, status, sizeof(int), cudaMemcpyDeviceToHost, s));

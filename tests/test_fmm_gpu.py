@@ -68,3 +68,22 @@ def test_laplace_vs_direct_sum(order, tol64):
     c32 = (K * b)[targets] - 1e12 * b[targets]
     e32 = np.linalg.norm(c32 - direct) / np.linalg.norm(direct)
     assert e32 < tol64 * 1.5 + 1e-5, (e32, e64)
+
+
+@pytest.mark.parametrize("order", [4, 5, 6, 7, 8])
+def test_mixed_m2l_matches_fp64_for_every_row_block_count(order):
+    """Mixed mode against FP64 mode on the same tree, self term removed.
+    Orders 5..8 (125..512 Chebyshev nodes) run the tcgen05 M2L with 1..4 row
+    blocks of 128 per CTA; order 4 runs the mma.sync M2L.  A row block or a
+    split part that went missing would show as an error of order 1 or 1e-3."""
+    n = 30000
+    pos = workloads.uniform(n, 3, seed=150 + order)
+    p = octree(pos, 64)
+    b = np.random.default_rng(151 + order).uniform(-1, 1, n)
+    K = ab.create_fmm_operator(p, ab.Kernel.make(ab.K_LAPLACE, 1e-12), order)
+    c64 = K * b - 1e12 * b
+    K.set_precision(ab.PREC_MIXED)
+    c32 = K * b - 1e12 * b
+    assert ab.fmm_stats(K)["m2l_pairs"] > 0
+    err = np.linalg.norm(c32 - c64) / np.linalg.norm(c64)
+    assert err < 1e-5, err
