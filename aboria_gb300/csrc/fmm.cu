@@ -41,6 +41,9 @@ constexpr int MAXN_TAB = 8;  // max Chebyshev order of the coefficient table
 struct ChebTab {
   double c[MAXN_TAB][MAXN_TAB];
 };
+struct ChebTab32 {  // the same in FP32 (mixed-precision P2M and L2P)
+  float c[MAXN_TAB][MAXN_TAB];
+};
 
 struct FmmPlan {
   int D = 3, n = 3, ncheb = 27, nchild = 8;
@@ -51,15 +54,18 @@ struct FmmPlan {
   // device
   DevBuf<double> W, G;            // nnodes x ncheb
   DevBuf<double> Tc;              // nchild x ncheb x ncheb (child->parent interpolation)
-  DevBuf<float> Tc32;             // FP32 copy (mixed-precision M2M / L2L)
+  DevBuf<float> Tc32;             // FP32 copy (mixed-precision L2L)
+  DevBuf<double> TcT;             // transposed: TcT[o][j][i] = Tc[o][i][j] (M2M)
+  DevBuf<float> Tc32T;            // FP32 copy of TcT (mixed-precision M2M)
   DevBuf<double> box;             // nnodes x 6 (lo[3], hi[3])
   DevBuf<int> leaf_ids;           // leaves (node ids)
   DevBuf<int> node_begin, node_end;
   // per level: nodes with children (M2M/L2L), (parent, child, octant) links
   std::vector<int> max_level;
   std::vector<std::vector<int>> level_links;  // host: flattened (parent, child, octant)
-  DevBuf<int> links;                          // all levels concatenated
-  std::vector<int> link_off, link_cnt;
+  DevBuf<int> links;                          // all levels, octant-major within a level
+  DevBuf<int2> batches;                       // (first link, count <= NBL) of one octant
+  std::vector<int> batch_off, batch_cnt;      // per level
   // M2L: pairs (target, source, matrix id), grouped by level
   DevBuf<int> m2l;
   int n_m2l = 0;
@@ -80,6 +86,7 @@ struct FmmPlan {
   double chebsetup_s = 0.0;
   DevBuf<float> W32, G32;
   ChebTab tab{};        // Clenshaw coefficients of the order
+  ChebTab32 tab32{};    // the same in FP32 (mixed-precision P2M / L2P)
   DevBuf<float4> posf;  // mixed near field: FP32 position relative to the leaf centre
   DevBuf<float> b32;    // mixed near field: FP32 weights of the current matvec
   DevBuf<int> mi_d;                 // ncheb x 3 multi-indices
@@ -128,6 +135,29 @@ __device__ __forceinline__ void cheb_sn_tab(double x, int n, const ChebTab &t, d
     double b1 = 0.0, b2 = 0.0;
     for (int k = n - 1; k >= 1; --k) {
       const double bk = t.c[m][k] + 2.0 * x * b1 - b2;
+      b2 = b1;
+      b1 = bk;
+    }
+    S[m] = invn + x * b1 - b2;
+  }
+}
+
+// FP32 copy of the Clenshaw coefficients and the same recurrence in FP32
+// (mixed-precision P2M and L2P).
+
+inline ChebTab32 cheb_table32(const ChebTab &t) {
+  ChebTab32 f{};
+  for (int m = 0; m < MAXN_TAB; ++m)
+    for (int k = 0; k < MAXN_TAB; ++k) f.c[m][k] = (float)t.c[m][k];
+  return f;
+}
+
+__device__ __forceinline__ void cheb_sn_tab32(float x, int n, const ChebTab32 &t, float *S) {
+  const float invn = 1.0f / (float)n;
+  for (int m = 0; m < n; ++m) {
+    float b1 = 0.f, b2 = 0.f;
+    for (int k = n - 1; k >= 1; --k) {
+      const float bk = t.c[m][k] + 2.f * x * b1 - b2;
       b2 = b1;
       b1 = bk;
     }
@@ -203,44 +233,128 @@ __global__ void __launch_bounds__(FT) k_p2m(int D, int n, int ncheb, const int *
   }
 }
 
-// ------------------------------------------------------------ M2M / L2L ---
-// links: (parent, child, octant); one CTA per link group of one parent.
-// M2M: W[p][i] += sum_j Tc[o][i][j] W[c][j]   (atomic over children).
-// T is the compute type: double in FP64 mode; float in mixed mode (FP32
-// copy of Tc, FP32 sums of ncheb terms, FP64 storage).
-template <typename T>
-__global__ void __launch_bounds__(FT) k_m2m(int ncheb, const int *__restrict__ links, int nlinks,
-                                            const T *__restrict__ Tc, double *__restrict__ W) {
-  const int l = blockIdx.x;
-  if (l >= nlinks) return;
-  const int p = links[3 * l], c = links[3 * l + 1], o = links[3 * l + 2];
-  __shared__ T wc[MAXC];
-  for (int j = threadIdx.x; j < ncheb; j += FT) wc[j] = (T)W[(size_t)c * ncheb + j];
-  __syncthreads();
-  const T *Tm = Tc + (size_t)o * ncheb * ncheb;
-  for (int i = threadIdx.x; i < ncheb; i += FT) {
-    T a = 0;
-    for (int j = 0; j < ncheb; ++j) a += Tm[(size_t)i * ncheb + j] * wc[j];
-    atomicAdd(&W[(size_t)p * ncheb + i], (double)a);
+// Mixed-precision P2M: the same sums in FP32 from the leaf-relative FP32
+// positions (x = offset / half-width) and FP32 weights; each chunk of FT
+// points is summed in FP32 and chunks are added in FP64.
+__global__ void __launch_bounds__(FT) k_p2m32(int D, int n, int ncheb, const int *__restrict__ leaves,
+                                              const int *__restrict__ nb, const int *__restrict__ ne,
+                                              const double *__restrict__ box,
+                                              const float4 *__restrict__ posf,
+                                              const float *__restrict__ b32,
+                                              const int *__restrict__ mi, const ChebTab32 tab,
+                                              double *__restrict__ W) {
+  __shared__ float S[FT][MAXN * 3 + 1];
+  __shared__ float sb[FT];
+  __shared__ int smi[MAXC * 3];
+  const int leaf = leaves[blockIdx.x];
+  const double *bx = box + (size_t)leaf * 6;
+  float ihw[3] = {0.f, 0.f, 0.f};
+  for (int d = 0; d < D; ++d) {
+    const double hw = 0.5 * (bx[3 + d] - bx[d]);
+    ihw[d] = hw > 0.0 ? (float)(1.0 / hw) : 0.f;
+  }
+  for (int e = threadIdx.x; e < ncheb * 3; e += FT) smi[e] = mi[e];
+  double acc[MAXC / FT];
+  for (int q = 0; q < MAXC / FT; ++q) acc[q] = 0.0;
+  for (int i0 = nb[leaf]; i0 < ne[leaf]; i0 += FT) {
+    const int i = i0 + threadIdx.x;
+    if (i < ne[leaf]) {
+      const float4 t = posf[i];
+      const float xr[3] = {t.x, t.y, t.z};
+      for (int d = 0; d < D; ++d) cheb_sn_tab32(xr[d] * ihw[d], n, tab, &S[threadIdx.x][d * MAXN]);
+      sb[threadIdx.x] = b32[i];
+    }
+    __syncthreads();
+    const int cnt = min(FT, ne[leaf] - i0);
+    for (int q = 0; q < MAXC / FT; ++q) {
+      const int j = threadIdx.x + q * FT;
+      if (j >= ncheb) break;
+      const int m0 = smi[j * 3], m1 = MAXN + smi[j * 3 + 1], m2 = 2 * MAXN + smi[j * 3 + 2];
+      float a = 0.f;
+      if (D == 3) {
+        for (int p = 0; p < cnt; ++p) a = fmaf(sb[p] * S[p][m0], S[p][m1] * S[p][m2], a);
+      } else {
+        for (int p = 0; p < cnt; ++p) {
+          float r = sb[p];
+          for (int d = 0; d < D; ++d) r *= S[p][d * MAXN + smi[j * 3 + d]];
+          a += r;
+        }
+      }
+      acc[q] += (double)a;
+    }
+    __syncthreads();
+  }
+  for (int q = 0; q < MAXC / FT; ++q) {
+    const int j = threadIdx.x + q * FT;
+    if (j < ncheb) W[(size_t)leaf * ncheb + j] = acc[q];
   }
 }
 
-// L2L: G[c][i] += sum_j Tc[o][j][i] G[p][j]   (compute type T as for M2M)
-template <typename T>
-__global__ void __launch_bounds__(FT) k_l2l(int ncheb, const int *__restrict__ links, int nlinks,
-                                            const T *__restrict__ Tc, double *__restrict__ G) {
-  const int l = blockIdx.x;
-  if (l >= nlinks) return;
-  const int p = links[3 * l], c = links[3 * l + 1], o = links[3 * l + 2];
-  __shared__ T gp[MAXC];
-  for (int j = threadIdx.x; j < ncheb; j += FT) gp[j] = (T)G[(size_t)p * ncheb + j];
-  __syncthreads();
-  const T *Tm = Tc + (size_t)o * ncheb * ncheb;
-  for (int i = threadIdx.x; i < ncheb; i += FT) {
-    T a = 0;
-    for (int j = 0; j < ncheb; ++j) a += Tm[(size_t)j * ncheb + i] * gp[j];
-    G[(size_t)c * ncheb + i] += (double)a;
+// ------------------------------------------------------------ M2M / L2L ---
+// links: (parent, child, octant), sorted by octant within each level; one CTA
+// per (batch of <= NBL links of one level and one octant, FT rows i), so
+// that the CTA reads its rows of the octant's ncheb x ncheb matrix once for
+// all the batch's links.
+// M2M: W[p][i] += sum_j Tc[o][i][j] W[c][j]   (atomic over the parent's
+//      children, which other batches hold); read through TcT[o][j][i] =
+//      Tc[o][i][j] so that the loads are coalesced along i.
+// L2L: G[c][i] += sum_j Tc[o][j][i] G[p][j]   (each child once).
+// T is the compute type: double in FP64 mode; float in mixed mode (FP32
+// copies of the matrices, FP32 sums of ncheb terms, FP64 storage).
+constexpr int NBL = 8;  // links per M2M / L2L batch
+template <typename T, bool M2M>
+__global__ void __launch_bounds__(FT) k_m2m_l2l(int ncheb, const int *__restrict__ links,
+                                                const int2 *__restrict__ batches,
+                                                const T *__restrict__ Tm_all,
+                                                double *__restrict__ V) {
+  const int2 bt = batches[blockIdx.x];
+  __shared__ T vin[NBL][MAXC];
+  __shared__ int sout[NBL];
+  const int o = links[3 * bt.x + 2];
+  // M2M reads the children and writes the parents; L2L the other way round
+  for (int e = threadIdx.x; e < NBL * ncheb; e += FT) {
+    const int b = e / ncheb, j = e - b * ncheb;
+    T v = 0;
+    if (b < bt.y) {
+      const int nd = links[3 * (bt.x + b) + (M2M ? 1 : 0)];
+      v = (T)V[(size_t)nd * ncheb + j];
+    }
+    vin[b][j] = v;
   }
+  if (threadIdx.x < bt.y) sout[threadIdx.x] = links[3 * (bt.x + threadIdx.x) + (M2M ? 0 : 1)];
+  __syncthreads();
+  const T *Tm = Tm_all + (size_t)o * ncheb * ncheb;  // [j][i]
+  const int i = blockIdx.y * FT + threadIdx.x;
+  if (i < ncheb) {
+    T a[NBL];
+#pragma unroll
+    for (int b = 0; b < NBL; ++b) a[b] = 0;
+#pragma unroll 4
+    for (int j = 0; j < ncheb; ++j) {
+      const T t = Tm[(size_t)j * ncheb + i];
+#pragma unroll
+      for (int b = 0; b < NBL; ++b) a[b] += t * vin[b][j];
+    }
+#pragma unroll
+    for (int b = 0; b < NBL; ++b) {
+      if (b >= bt.y) break;
+      double *dst = &V[(size_t)sout[b] * ncheb + i];
+      if (M2M) atomicAdd(dst, (double)a[b]);
+      else *dst += (double)a[b];
+    }
+  }
+}
+
+// out[o][j][i] = (To)in[o][i][j] (transposed copy of the child matrices).
+template <typename To>
+__global__ void k_transpose_tc(const double *__restrict__ in, int nchild, int ncheb,
+                               To *__restrict__ out) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (int64_t)nchild * ncheb * ncheb) return;
+  const int64_t o = e / ((int64_t)ncheb * ncheb);
+  const int r = (int)(e % ((int64_t)ncheb * ncheb));
+  const int j = r / ncheb, i = r % ncheb;
+  out[e] = (To)in[(o * ncheb + i) * ncheb + j];
 }
 
 // --------------------------------------------------------------- M2L ---
@@ -441,25 +555,33 @@ __global__ void __launch_bounds__(64 * WM) k_m2l_tc2(int ncheb, int ldk, int ldg
 // tcgen05.mma kind::tf32 into NRB accumulators of 128 x T5_N FP32 in TMEM.
 // The K matrices are packed once per plan into the shared-memory image of a
 // pipeline stage (k_pack_tf32), so a stage's A operand is one bulk copy on the
-// TMA engine (cp.async.bulk, completion counted on the stage's `full`
+// TMA engine (cp.async.bulk, completion counted on the stage's `fullA`
 // mbarrier) and bypasses the load/store pipeline; the W rows of the tile's
-// sources are gathered 16 bytes per thread with cp.async.  Operands use the
+// sources are gathered 16 bytes per lane with cp.async.  Operands use the
 // no-swizzle K-major core-matrix layout (8 rows x 16 bytes per core matrix;
 // the descriptor's leading byte offset is the core-matrix stride along K, the
-// stride byte offset along rows).  Thread 0 waits for the stage's bulk copy,
-// issues the 3 NRB MMAs of each 8-column block and commits them to the
-// stage's `done` mbarrier; a stage is refilled only after that barrier
-// completes.  Every wait is bounded: on timeout the kernel sets *status,
-// skips the epilogue, waits (bounded) for its last commit and still releases
-// its TMEM.  The ring depth keeps the CTAs resident on an SM (by shared
-// memory) within the SM's 512 TMEM columns.  Epilogue: each warp reads its 32
+// stride byte offset along rows).
+// Roles, with no CTA-wide barrier inside the loop: warp 0 produces (waits for
+// the stage's `empty` barrier, issues block p, then waits for block p-LAG's
+// W copies, fences them to the async proxy and arrives on `fullB`); lane 0 of
+// warp 1 waits for `fullA` and `fullB`, issues the 3 NRB MMAs of the block
+// and commits them to `empty`, and after the last block to `accb`; all four
+// warps then wait for `accb` and run the epilogue: each reads its 32
 // accumulator lanes (rows) with tcgen05.ld and adds them into G with
-// reductions that are coalesced along the rows.
+// reductions that are coalesced along the rows.  Every wait is bounded: on
+// timeout the kernel sets *status, skips the epilogue, waits (bounded) for
+// its copies and MMAs in flight and still releases its TMEM.  The ring depth
+// keeps the CTAs resident on an SM (by shared memory) within the SM's 512
+// TMEM columns.
 constexpr int T5_N = 128, T5_KB = 8;
 constexpr int T5_PART = 128 * T5_KB * 4;  // bytes of one operand part: 128 rows x 8 columns
 constexpr int T5_SPIN = 1 << 26;          // mbarrier polls before giving up (seconds at most)
 template <int NRB> struct T5Cfg {
   static constexpr int S = NRB == 1 ? 3 : (NRB == 2 ? 4 : (NRB == 3 ? 6 : 5));  // ring depth
+  // the producer signals block p - LAG's W copies after issuing block p
+  // (LAG < S: the MMAs of block p - S, which free block p's stage, never wait
+  // for a block the producer has not signalled)
+  static constexpr int LAG = NRB == 1 ? 1 : (NRB == 4 ? 2 : (NRB == 3 ? 3 : 2));
   static constexpr int A_BYTES = NRB * 2 * T5_PART;       // K hi, lo of every row block
   static constexpr int STAGE = A_BYTES + 2 * T5_PART;     // + W hi, lo of the T5_N pairs
   static constexpr size_t SMEM = (size_t)S * STAGE + 1024 + 2048;  // + alignment, barriers, indices
@@ -469,6 +591,9 @@ static_assert(T5Cfg<1>::SMEM * 5 > 228 * 1024 && T5Cfg<2>::SMEM * 3 > 228 * 1024
                   T5Cfg<3>::SMEM * 2 > 228 * 1024 && T5Cfg<4>::SMEM * 2 > 228 * 1024,
               "resident CTAs per SM must fit the SM's 512 TMEM columns");
 static_assert(T5Cfg<3>::SMEM <= 227 * 1024 && T5Cfg<4>::SMEM <= 227 * 1024, "shared memory per CTA");
+static_assert(T5Cfg<1>::LAG < T5Cfg<1>::S && T5Cfg<2>::LAG < T5Cfg<2>::S &&
+                  T5Cfg<3>::LAG < T5Cfg<3>::S && T5Cfg<4>::LAG < T5Cfg<4>::S,
+              "producer lag below the ring depth");
 
 // Packed split-TF32 M2L matrices: per (matrix, 8-column block kb, 128-row
 // block rb, part hi/lo) the 4 KB shared-memory image of the operand tile,
@@ -541,13 +666,13 @@ __global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int nkb, int ldk, in
                                                  const float *__restrict__ Wl,
                                                  float *__restrict__ G32, int *__restrict__ status) {
   using C = T5Cfg<NRB>;
-  constexpr int S = C::S;
+  constexpr int S = C::S, LAG = C::LAG;
   extern __shared__ __align__(128) unsigned char t5raw[];
   unsigned char *sm = (unsigned char *)(((uintptr_t)t5raw + 1023) & ~(uintptr_t)1023);
-  uint64_t *full = (uint64_t *)(sm + S * C::STAGE);
-  uint64_t *done = full + S;
-  uint32_t *tslot = (uint32_t *)(done + S);
-  int *sSrc = (int *)(tslot + 4), *sTgt = sSrc + T5_N, *sLast = sTgt + T5_N;
+  uint64_t *fullA = (uint64_t *)(sm + S * C::STAGE);
+  uint64_t *fullB = fullA + S, *empty = fullB + S, *accb = empty + S;
+  uint32_t *tslot = (uint32_t *)(accb + 1);
+  int *sSrc = (int *)(tslot + 4), *sTgt = sSrc + T5_N, *sInfo = sTgt + T5_N;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int tile = blockIdx.x;
   const int m = tile_mat[tile], p0 = tile_first[tile];
@@ -559,10 +684,16 @@ __global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int nkb, int ldk, in
   }
   if (tid == 0) {
     for (int q = 0; q < S; ++q) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&full[q])));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&done[q])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&fullA[q])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&fullB[q])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&empty[q])));
     }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(accb)));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    sInfo[0] = 0;  // blocks issued by the producer
+    sInfo[1] = 0;  // blocks whose operands the MMA issuer received
+    sInfo[2] = 1;  // producer ok
+    sInfo[3] = 1;  // MMA issuer ok
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -574,115 +705,115 @@ __global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int nkb, int ldk, in
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tslot;
-  const unsigned char *Am = (const unsigned char *)Ap + (size_t)m * nkb * C::A_BYTES;
-  constexpr uint32_t idesc = umma_idesc_tf32(128, T5_N);
   const uint32_t smbase = smem_addr(sm);
-  int nfill = 0, ncons = 0;  // thread 0: bulk copies issued / waited for
 
-  // block kb into stage kb % S: K by one bulk copy (thread 0), W by cp.async
-  // (one group per thread)
-  auto load_block = [&](int kb) {
-    const uint32_t st = smbase + (uint32_t)((kb % S) * C::STAGE);
-    if (tid == 0) {
-      ++nfill;
-      const uint32_t fb = smem_addr(&full[kb % S]);
-      asm volatile(
-          "{\n\t.reg .b64 state;\n\t"
-          "mbarrier.arrive.expect_tx.shared::cta.b64 state, [%0], %1;\n\t}" ::"r"(fb),
-          "r"(C::A_BYTES)
-          : "memory");
-      asm volatile(
-          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-              st),
-          "l"(Am + (size_t)kb * C::A_BYTES), "r"(C::A_BYTES), "r"(fb)
-          : "memory");
-    }
-#pragma unroll
-    for (int e = tid; e < T5_N * (T5_KB / 4); e += 128) {
-      const int rl = e & 7, kq = (e >> 3) & 1, rh = e >> 4;
-      const int src = sSrc[rh * 8 + rl];
-      const uint32_t off = (uint32_t)((kq * (T5_N / 8) + rh) * 128 + rl * 16);
-      const size_t g = (size_t)(src >= 0 ? src : 0) * ldk + kb * T5_KB + kq * 4;
-      cp16(st + C::A_BYTES + off, Wh + g, src >= 0 ? 16 : 0);
-      cp16(st + C::A_BYTES + T5_PART + off, Wl + g, src >= 0 ? 16 : 0);
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");
-  };
-
-  for (int kb = 0; kb < S - 1; ++kb) {
-    if (kb < nkb) load_block(kb);
-    else asm volatile("cp.async.commit_group;" ::: "memory");
-  }
-  bool ok = true;
-  int last = -1;  // thread 0: the last block whose MMAs were committed
-  for (int kb = 0; kb < nkb; ++kb) {
-    const int st = kb % S;
-    // this thread's W copies of block kb have landed (at most S - 2 newer groups pending)
-    asm volatile("cp.async.wait_group %0;" ::"n"(S - 2) : "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (tid == 0 && ok) {
-      if (!mbar_wait(smem_addr(&full[st]), (kb / S) & 1)) {
-        ok = false;
-      } else {
-        ++ncons;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t base = smbase + (uint32_t)(st * C::STAGE);
-        constexpr uint32_t ks = (128 / 8) * 128;  // core-matrix stride along K
-        const uint64_t bh = umma_desc(base + C::A_BYTES, ks, 128);
-        const uint64_t bl = umma_desc(base + C::A_BYTES + T5_PART, ks, 128);
-#pragma unroll
-        for (int rb = 0; rb < NRB; ++rb) {
-          const uint64_t ah = umma_desc(base + rb * 2 * T5_PART, ks, 128);
-          const uint64_t al = umma_desc(base + rb * 2 * T5_PART + T5_PART, ks, 128);
-          const uint64_t ad[3] = {al, ah, ah}, bd[3] = {bh, bl, bh};
-#pragma unroll
-          for (int t = 0; t < 3; ++t) {
-            const uint32_t acc = (kb > 0 || t > 0) ? 1u : 0u;
-            asm volatile(
-                "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(
-                    tmem + (uint32_t)(rb * T5_N)),
-                "l"(ad[t]), "l"(bd[t]), "r"(idesc), "r"(acc));
-          }
-        }
+  if (warp == 0) {
+    // ---- producer
+    const unsigned char *Am = (const unsigned char *)Ap + (size_t)m * nkb * C::A_BYTES;
+    bool ok = true;
+    int p = 0;
+    for (; p < nkb; ++p) {
+      const int st = p % S;
+      if (p >= S && !mbar_wait(smem_addr(&empty[st]), ((p - S) / S) & 1)) ok = false;
+      if (!__all_sync(0xffffffffu, ok)) break;
+      const uint32_t sb = smbase + (uint32_t)(st * C::STAGE);
+      if (lane == 0) {
+        const uint32_t fb = smem_addr(&fullA[st]);
         asm volatile(
-            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                smem_addr(&done[st])));
-        last = kb;
+            "{\n\t.reg .b64 state;\n\t"
+            "mbarrier.arrive.expect_tx.shared::cta.b64 state, [%0], %1;\n\t}" ::"r"(fb),
+            "r"(C::A_BYTES)
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+            "[%3];" ::"r"(sb),
+            "l"(Am + (size_t)p * C::A_BYTES), "r"(C::A_BYTES), "r"(fb)
+            : "memory");
+      }
+#pragma unroll
+      for (int e = lane; e < T5_N * (T5_KB / 4); e += 32) {
+        const int rl = e & 7, kq = (e >> 3) & 1, rh = e >> 4;
+        const int src = sSrc[rh * 8 + rl];
+        const uint32_t off = (uint32_t)((kq * (T5_N / 8) + rh) * 128 + rl * 16);
+        const size_t g = (size_t)(src >= 0 ? src : 0) * ldk + p * T5_KB + kq * 4;
+        cp16(sb + C::A_BYTES + off, Wh + g, src >= 0 ? 16 : 0);
+        cp16(sb + C::A_BYTES + T5_PART + off, Wl + g, src >= 0 ? 16 : 0);
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+      if (p >= LAG) {
+        // block p - LAG's W copies have landed: hand them to the async proxy
+        asm volatile("cp.async.wait_group %0;" ::"n"(LAG) : "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0)
+          asm volatile("{\n\t.reg .b64 state;\n\tmbarrier.arrive.shared::cta.b64 state, [%0];\n\t}" ::"r"(
+                           smem_addr(&fullB[(p - LAG) % S]))
+                       : "memory");
       }
     }
-    // refill the stage that block kb - 1 used with block kb + S - 1, once
-    // block kb - 1's MMAs have completed (the c-th commit on a stage's barrier
-    // completes its phase c)
-    const int nb = kb + S - 1;
-    if (nb < nkb) {
-      if (kb >= 1 && ok) {
-        const int pst = (kb - 1) % S;
-        if (!mbar_wait(smem_addr(&done[pst]), ((kb - 1) / S) & 1)) ok = false;
-      }
-      if (!__syncthreads_and(ok)) {
+    // the last min(p, LAG) blocks
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncwarp();
+    if (lane == 0) {
+      for (int q = max(p - LAG, 0); q < p; ++q)
+        asm volatile("{\n\t.reg .b64 state;\n\tmbarrier.arrive.shared::cta.b64 state, [%0];\n\t}" ::"r"(
+                         smem_addr(&fullB[q % S]))
+                     : "memory");
+      sInfo[0] = p;
+      if (!ok) sInfo[2] = 0;
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---- MMA issuer
+    constexpr uint32_t idesc = umma_idesc_tf32(128, T5_N);
+    constexpr uint32_t ks = (128 / 8) * 128;  // core-matrix stride along K
+    bool ok = true;
+    int c = 0;
+    for (; c < nkb; ++c) {
+      const int st = c % S;
+      const uint32_t par = (c / S) & 1;
+      if (!mbar_wait(smem_addr(&fullA[st]), par) || !mbar_wait(smem_addr(&fullB[st]), par)) {
         ok = false;
         break;
       }
-      load_block(nb);
-    } else {
-      asm volatile("cp.async.commit_group;" ::: "memory");
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t base = smbase + (uint32_t)(st * C::STAGE);
+      const uint64_t bh = umma_desc(base + C::A_BYTES, ks, 128);
+      const uint64_t bl = umma_desc(base + C::A_BYTES + T5_PART, ks, 128);
+#pragma unroll
+      for (int rb = 0; rb < NRB; ++rb) {
+        const uint64_t ah = umma_desc(base + rb * 2 * T5_PART, ks, 128);
+        const uint64_t al = umma_desc(base + rb * 2 * T5_PART + T5_PART, ks, 128);
+        const uint64_t ad[3] = {al, ah, ah}, bd[3] = {bh, bl, bh};
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+          const uint32_t acc = (c > 0 || t > 0) ? 1u : 0u;
+          asm volatile(
+              "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+              "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(
+                  tmem + (uint32_t)(rb * T5_N)),
+              "l"(ad[t]), "l"(bd[t]), "r"(idesc), "r"(acc));
+        }
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_addr(&empty[st])));
     }
+    // completes once every MMA issued above has completed
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_addr(accb)));
+    sInfo[1] = c;
+    if (!ok) sInfo[3] = 0;
   }
-  asm volatile("cp.async.wait_all;" ::: "memory");
-  if (tid == 0) *sLast = last;
   __syncthreads();
-  // the last commit covers every MMA issued before it
-  const int lst = *sLast;
-  if (lst >= 0 && !mbar_wait(smem_addr(&done[lst % S]), (lst / S) & 1)) ok = false;
-  if (lst != nkb - 1) ok = false;
-  ok = __syncthreads_and(ok);
+  bool ok = mbar_wait(smem_addr(accb), 0);
+  ok = __syncthreads_and(ok && sInfo[2] && sInfo[3] && sInfo[1] == nkb);
   if (!ok) {
     if (tid == 0) {
       atomicExch(status, 1);
       // bulk copies still in flight land before the shared memory is released
-      for (int kb = ncons; kb < nfill; ++kb) mbar_wait(smem_addr(&full[kb % S]), (kb / S) & 1);
+      for (int q = sInfo[1]; q < sInfo[0]; ++q) mbar_wait(smem_addr(&fullA[q % S]), (q / S) & 1);
     }
   } else {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -853,7 +984,10 @@ constexpr int PT = 32;  // threads per target leaf (one warp) in the mixed near 
 constexpr int PW = 4;   // target leaves (warps) per CTA
 
 // Mixed-precision L2P + P2P: one warp per target leaf, one lane per target.
-// L2P in FP64 as in the FP64 kernel; each source leaf of the near field is
+// L2P in FP32 from the leaf-relative FP32 position (x = offset /
+// half-width): G of the leaf in FP32, the tensor-product sum nested by
+// dimension (the node index is lexicographic, last dimension fastest), the
+// innermost two levels in FP32 and the outermost in FP64; each source leaf of the near field is
 // staged in shared memory as FP32 offsets from the target leaf's centre
 // (leaf-relative FP32 position + FP32 centre offset), the pair terms are FP32
 // with a staged chunk (<= 32 terms) summed in FP32 and chunks summed in
@@ -865,20 +999,26 @@ __global__ void __launch_bounds__(PT * PW) k_l2p_p2p32(
     const int *__restrict__ ne, const double *__restrict__ box, const double *__restrict__ pos,
     int64_t npos, const float4 *__restrict__ posf, const float *__restrict__ b32,
     const double *__restrict__ b, const int *__restrict__ mi, const double *__restrict__ G,
-    const int *__restrict__ rp, const int *__restrict__ src, double p0, const ChebTab tab,
+    const int *__restrict__ rp, const int *__restrict__ src, double p0, const ChebTab32 tab,
     double *__restrict__ c) {
-  __shared__ double sg_all[PW][MAXC];
+  __shared__ float sg_all[PW][MAXC];
   __shared__ float4 ss_all[PW][PT];
+  __shared__ float sS_all[PW][3][MAXN][PT];  // per-lane Chebyshev values [d][m][lane]
   const int tid = threadIdx.x & 31, wl = threadIdx.x >> 5;
   const int li = blockIdx.x * PW + wl;
   if (li >= nleaves) return;  // whole warps: only warp-level synchronisation below
-  double *sg = sg_all[wl];
+  float *sg = sg_all[wl];
   float4 *ss = ss_all[wl];
   const int leaf = leaves[li];
   const double *bx = box + (size_t)leaf * 6;
   double ct[3] = {0.0, 0.0, 0.0};
-  for (int d = 0; d < D; ++d) ct[d] = 0.5 * (bx[d] + bx[3 + d]);
-  for (int j = tid; j < ncheb; j += PT) sg[j] = G[(size_t)leaf * ncheb + j];
+  float ihw[3] = {0.f, 0.f, 0.f};
+  for (int d = 0; d < D; ++d) {
+    ct[d] = 0.5 * (bx[d] + bx[3 + d]);
+    const double hw = 0.5 * (bx[3 + d] - bx[d]);
+    ihw[d] = hw > 0.0 ? (float)(1.0 / hw) : 0.f;
+  }
+  for (int j = tid; j < ncheb; j += PT) sg[j] = (float)G[(size_t)leaf * ncheb + j];
   __syncwarp();
   const float p0f = (float)p0;
   for (int i0 = nb[leaf]; i0 < ne[leaf]; i0 += PT) {
@@ -887,16 +1027,35 @@ __global__ void __launch_bounds__(PT * PW) k_l2p_p2p32(
     double acc = 0.0;
     float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
     if (act) {
-      double xi[3] = {0, 0, 0};
-      for (int d = 0; d < D; ++d) xi[d] = pos[(int64_t)d * npos + i];
-      double S[3][MAXN];
-      for (int d = 0; d < D; ++d) cheb_sn_tab(shift_coord(xi[d], bx[d], bx[3 + d]), n, tab, S[d]);
-      for (int j = 0; j < ncheb; ++j) {
-        double r = sg[j];
-        for (int d = 0; d < D; ++d) r *= S[d][mi[j * 3 + d]];
-        acc += r;
-      }
       t = posf[i];
+      const float xr[3] = {t.x, t.y, t.z};
+      float S[MAXN];
+      for (int d = 0; d < D; ++d) {
+        cheb_sn_tab32(xr[d] * ihw[d], n, tab, S);
+        for (int m = 0; m < n; ++m) sS_all[wl][d][m][tid] = S[m];
+      }
+      // sum_{m0} S0 sum_{m1} S1 sum_{m2} S2 g[m0, m1, m2] (D = 3; fewer levels below)
+      const float(*sS)[MAXN][PT] = sS_all[wl];
+      if (D == 3) {
+        for (int m0 = 0; m0 < n; ++m0) {
+          float p1 = 0.f;
+          for (int m1 = 0; m1 < n; ++m1) {
+            const float *gg = sg + (m0 * n + m1) * n;
+            float p2 = 0.f;
+            for (int m2 = 0; m2 < n; ++m2) p2 = fmaf(gg[m2], sS[2][m2][tid], p2);
+            p1 = fmaf(p2, sS[1][m1][tid], p1);
+          }
+          acc += (double)(p1 * sS[0][m0][tid]);
+        }
+      } else if (D == 2) {
+        for (int m0 = 0; m0 < n; ++m0) {
+          float p1 = 0.f;
+          for (int m1 = 0; m1 < n; ++m1) p1 = fmaf(sg[m0 * n + m1], sS[1][m1][tid], p1);
+          acc += (double)(p1 * sS[0][m0][tid]);
+        }
+      } else {
+        for (int m0 = 0; m0 < n; ++m0) acc += (double)(sg[m0] * sS[0][m0][tid]);
+      }
     }
     for (int e = rp[li]; e < rp[li + 1]; ++e) {
       const int sl = src[e];
@@ -979,6 +1138,7 @@ int fmm_plan_build(abx_operator *op, int order, FmmPlan *&out) {
   P->D = D;
   P->n = order;
   P->tab = cheb_table(order);
+  P->tab32 = cheb_table32(P->tab);
   P->nchild = 1 << D;
   P->ncheb = 1;
   for (int d = 0; d < D; ++d) P->ncheb *= order;
@@ -1068,17 +1228,26 @@ int fmm_plan_build(abx_operator *op, int order, FmmPlan *&out) {
   int maxlev = 0;
   for (auto &l : links) maxlev = std::max(maxlev, T.level[l[1]]);
   std::vector<int> flat;
-  P->link_off.assign(maxlev + 2, 0);
-  P->link_cnt.assign(maxlev + 2, 0);
+  std::vector<int2> batches;
+  P->batch_off.assign(maxlev + 2, 0);
+  P->batch_cnt.assign(maxlev + 2, 0);
   for (int lev = 1; lev <= maxlev; ++lev) {
-    P->link_off[lev] = (int)(flat.size() / 3);
-    for (auto &l : links)
-      if (T.level[l[1]] == lev) {
-        flat.push_back(l[0]);
-        flat.push_back(l[1]);
-        flat.push_back(l[2]);
-      }
-    P->link_cnt[lev] = (int)(flat.size() / 3) - P->link_off[lev];
+    P->batch_off[lev] = (int)batches.size();
+    // octant-major within the level: batches of <= NBL links share a matrix
+    for (int o = 0; o < P->nchild; ++o) {
+      int run = 0;
+      for (auto &l : links)
+        if (T.level[l[1]] == lev && l[2] == o) {
+          const int idx = (int)(flat.size() / 3);
+          if (run == 0) batches.push_back(make_int2(idx, 0));
+          ++batches.back().y;
+          run = (run + 1) % NBL;
+          flat.push_back(l[0]);
+          flat.push_back(l[1]);
+          flat.push_back(l[2]);
+        }
+    }
+    P->batch_cnt[lev] = (int)batches.size() - P->batch_off[lev];
   }
   // ---- M2L matrices keyed by (level, offset)
   std::map<std::array<long long, 4>, int> matid;
@@ -1159,6 +1328,7 @@ int fmm_plan_build(abx_operator *op, int order, FmmPlan *&out) {
       (st = P->Tc.reserve(Tc.size())) || (st = P->box.reserve(boxes.size())) ||
       (st = P->leaf_ids.reserve(leaves.size() + 1)) || (st = P->node_begin.reserve(NN)) ||
       (st = P->node_end.reserve(NN)) || (st = P->links.reserve(flat.size() + 1)) ||
+      (st = P->batches.reserve(batches.size() + 1)) || (st = P->TcT.reserve(Tc.size())) ||
       (st = P->m2l.reserve(trip.size() + 1)) ||
       (st = P->Km.reserve((size_t)std::max(1, P->nmat) * nc * nc)) ||
       (st = P->p2p_rowptr.reserve(rp.size())) || (st = P->p2p_src.reserve(srcs.size() + 1)) ||
@@ -1183,11 +1353,15 @@ int fmm_plan_build(abx_operator *op, int order, FmmPlan *&out) {
     if (bytes) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
   };
   up(P->Tc.ptr, Tc.data(), Tc.size() * 8);
+  if (!Tc.empty())
+    k_transpose_tc<double><<<ceil_div(Tc.size(), 256), 256, 0, s>>>(P->Tc.ptr, P->nchild, nc,
+                                                                   P->TcT.ptr);
   up(P->box.ptr, boxes.data(), boxes.size() * 8);
   up(P->leaf_ids.ptr, leaves.data(), leaves.size() * 4);
   up(P->node_begin.ptr, nb.data(), nb.size() * 4);
   up(P->node_end.ptr, ne.data(), ne.size() * 4);
   up(P->links.ptr, flat.data(), flat.size() * 4);
+  up(P->batches.ptr, batches.data(), batches.size() * sizeof(int2));
   up(P->m2l.ptr, trip.data(), trip.size() * 4);
   up(P->p2p_rowptr.ptr, rp.data(), rp.size() * 4);
   up(P->p2p_src.ptr, srcs.data(), srcs.size() * 4);
@@ -1230,13 +1404,12 @@ template <int KIND>
 int launch_l2p_p2p(FmmPlan *P, cudaStream_t s, const double *pos, int64_t npos, const double *b,
                    double *c, bool mixed) {
   if (mixed) {
-    ABX_TRY(P->b32.reserve((size_t)npos));
-    k_f64_to_f32<<<ceil_div((size_t)npos, 256), 256, 0, s>>>(b, npos, P->b32.ptr);
+    // P->b32 holds this matvec's FP32 weights (converted before the P2M)
     k_l2p_p2p32<KIND><<<ceil_div((size_t)P->nleaves, PW), PT * PW, 0, s>>>(
         P->D, P->n, P->ncheb, P->nleaves, P->leaf_ids.ptr, P->node_begin.ptr, P->node_end.ptr,
         P->box.ptr, pos,
         npos, P->posf.ptr, P->b32.ptr, b, P->mi_d.ptr, P->G.ptr, P->p2p_rowptr.ptr,
-        P->p2p_src.ptr, P->p0, P->tab, c);
+        P->p2p_src.ptr, P->p0, P->tab32, c);
   } else
     k_l2p_p2p<KIND, false><<<P->nleaves, FT, 0, s>>>(
         P->D, P->n, P->ncheb, P->leaf_ids.ptr, P->node_begin.ptr, P->node_end.ptr, P->box.ptr, pos,
@@ -1257,24 +1430,39 @@ int fmm_matvec_device(abx_operator *op, const double *b, double *c) {
   const bool mixed = op->precision == ABX_PREC_MIXED;
   ABX_CHECK_CUDA(cudaMemsetAsync(P->W.ptr, 0, (size_t)P->nnodes * nc * 8, s));
   ABX_CHECK_CUDA(cudaMemsetAsync(P->G.ptr, 0, (size_t)P->nnodes * nc * 8, s));
-  if (P->nleaves > 0)
-    k_p2m<<<P->nleaves, FT, 0, s>>>(P->D, P->n, nc, P->leaf_ids.ptr, P->node_begin.ptr,
-                                    P->node_end.ptr, P->box.ptr, p->pos.ptr, npos, b, P->mi_d.ptr,
-                                    P->tab, P->W.ptr);
-  if (mixed && !P->Tc32.ptr) {
-    const size_t nt = (size_t)P->nchild * nc * nc;
-    ABX_TRY(P->Tc32.reserve(nt));
-    k_f64_to_f32<<<ceil_div(nt, 256), 256, 0, s>>>(P->Tc.ptr, nt, P->Tc32.ptr);
+  if (mixed) {
+    ABX_TRY(P->b32.reserve((size_t)npos));
+    k_f64_to_f32<<<ceil_div((size_t)npos, 256), 256, 0, s>>>(b, npos, P->b32.ptr);
+    if (!P->Tc32.ptr) {
+      const size_t nt = (size_t)P->nchild * nc * nc;
+      ABX_TRY(P->Tc32.reserve(nt));
+      ABX_TRY(P->Tc32T.reserve(nt));
+      k_f64_to_f32<<<ceil_div(nt, 256), 256, 0, s>>>(P->Tc.ptr, nt, P->Tc32.ptr);
+      k_transpose_tc<float><<<ceil_div(nt, 256), 256, 0, s>>>(P->Tc.ptr, P->nchild, nc,
+                                                             P->Tc32T.ptr);
+    }
+  }
+  if (P->nleaves > 0) {
+    if (mixed)
+      k_p2m32<<<P->nleaves, FT, 0, s>>>(P->D, P->n, nc, P->leaf_ids.ptr, P->node_begin.ptr,
+                                        P->node_end.ptr, P->box.ptr, P->posf.ptr, P->b32.ptr,
+                                        P->mi_d.ptr, P->tab32, P->W.ptr);
+    else
+      k_p2m<<<P->nleaves, FT, 0, s>>>(P->D, P->n, nc, P->leaf_ids.ptr, P->node_begin.ptr,
+                                      P->node_end.ptr, P->box.ptr, p->pos.ptr, npos, b,
+                                      P->mi_d.ptr, P->tab, P->W.ptr);
   }
   const int maxlev = P->max_level.empty() ? 0 : P->max_level[0];
   for (int lev = maxlev; lev >= 1; --lev)
-    if (P->link_cnt[lev] > 0)
+    if (P->batch_cnt[lev] > 0) {
+      const int2 *bt = P->batches.ptr + P->batch_off[lev];
       if (mixed)
-        k_m2m<float><<<P->link_cnt[lev], FT, 0, s>>>(nc, P->links.ptr + 3 * P->link_off[lev],
-                                                     P->link_cnt[lev], P->Tc32.ptr, P->W.ptr);
+        k_m2m_l2l<float, true><<<dim3(P->batch_cnt[lev], ceil_div(nc, FT)), FT, 0, s>>>(nc, P->links.ptr, bt,
+                                                              P->Tc32T.ptr, P->W.ptr);
       else
-        k_m2m<double><<<P->link_cnt[lev], FT, 0, s>>>(nc, P->links.ptr + 3 * P->link_off[lev],
-                                                      P->link_cnt[lev], P->Tc.ptr, P->W.ptr);
+        k_m2m_l2l<double, true><<<dim3(P->batch_cnt[lev], ceil_div(nc, FT)), FT, 0, s>>>(nc, P->links.ptr, bt,
+                                                               P->TcT.ptr, P->W.ptr);
+    }
   ABX_CHECK_CUDA(cudaGetLastError());
   if (P->n_m2l > 0) {
     if (mixed) {
@@ -1350,13 +1538,15 @@ int fmm_matvec_device(abx_operator *op, const double *b, double *c) {
     ABX_CHECK_CUDA(cudaGetLastError());
   }
   for (int lev = 1; lev <= maxlev; ++lev)
-    if (P->link_cnt[lev] > 0)
+    if (P->batch_cnt[lev] > 0) {
+      const int2 *bt = P->batches.ptr + P->batch_off[lev];
       if (mixed)
-        k_l2l<float><<<P->link_cnt[lev], FT, 0, s>>>(nc, P->links.ptr + 3 * P->link_off[lev],
-                                                     P->link_cnt[lev], P->Tc32.ptr, P->G.ptr);
+        k_m2m_l2l<float, false><<<dim3(P->batch_cnt[lev], ceil_div(nc, FT)), FT, 0, s>>>(nc, P->links.ptr, bt,
+                                                               P->Tc32.ptr, P->G.ptr);
       else
-        k_l2l<double><<<P->link_cnt[lev], FT, 0, s>>>(nc, P->links.ptr + 3 * P->link_off[lev],
-                                                      P->link_cnt[lev], P->Tc.ptr, P->G.ptr);
+        k_m2m_l2l<double, false><<<dim3(P->batch_cnt[lev], ceil_div(nc, FT)), FT, 0, s>>>(nc, P->links.ptr, bt,
+                                                                P->Tc.ptr, P->G.ptr);
+    }
   ABX_CHECK_CUDA(cudaGetLastError());
   if (P->nleaves == 0) return ABX_OK;
   switch (P->kind) {
