@@ -548,11 +548,11 @@ __global__ void __launch_bounds__(64 * WM) k_m2l_tc2(int ncheb, int ldk, int ldg
 
 // ------------------------------------------------- M2L on tcgen05 (TMEM) ---
 // The same tile GEMM on the 5th-generation tensor cores.  One CTA (4 warps)
-// per (M2L matrix, T5_N-pair tile) computes all NRB = ceil(ncheb/128) row
+// per (M2L matrix, N-pair tile) computes all NRB = ceil(ncheb/128) row
 // blocks, so the gathered source expansions of the tile are read once:
 //   G[targets][rb*128 + r] += sum_k K[rb*128 + r][k] * W[sources][k]
 // as split TF32 (K = Kh + Kl, W = Wh + Wl; Kl Wh + Kh Wl + Kh Wh) on
-// tcgen05.mma kind::tf32 into NRB accumulators of 128 x T5_N FP32 in TMEM.
+// tcgen05.mma kind::tf32 into NRB accumulators of 128 x N FP32 in TMEM.
 // The K matrices are packed once per plan into the shared-memory image of a
 // pipeline stage (k_pack_tf32), so a stage's A operand is one bulk copy on the
 // TMA engine (cp.async.bulk, completion counted on the stage's `fullA`
@@ -573,22 +573,30 @@ __global__ void __launch_bounds__(64 * WM) k_m2l_tc2(int ncheb, int ldk, int ldg
 // its copies and MMAs in flight and still releases its TMEM.  The ring depth
 // keeps the CTAs resident on an SM (by shared memory) within the SM's 512
 // TMEM columns.
-constexpr int T5_N = 128, T5_KB = 8;
-constexpr int T5_PART = 128 * T5_KB * 4;  // bytes of one operand part: 128 rows x 8 columns
+constexpr int T5_KB = 8;
+constexpr int T5_PART = 128 * T5_KB * 4;  // bytes of one K operand part: 128 rows x 8 columns
 constexpr int T5_SPIN = 1 << 26;          // mbarrier polls before giving up (seconds at most)
+// Per row-block count: N pairs per tile, ring depth S, producer lag LAG and
+// TMEM columns.  Three or four row blocks use 64-pair tiles so that two CTAs
+// share an SM (their latencies overlap); one or two use 128-pair tiles.
 template <int NRB> struct T5Cfg {
-  static constexpr int S = NRB == 1 ? 3 : (NRB == 2 ? 4 : (NRB == 3 ? 6 : 5));  // ring depth
+  static constexpr int N = NRB <= 2 ? 128 : 64;
+  static constexpr int S = NRB == 2 ? 4 : 3;  // ring depth
   // the producer signals block p - LAG's W copies after issuing block p
   // (LAG < S: the MMAs of block p - S, which free block p's stage, never wait
   // for a block the producer has not signalled)
-  static constexpr int LAG = NRB == 1 ? 1 : (NRB == 4 ? 2 : (NRB == 3 ? 3 : 2));
+  static constexpr int LAG = NRB == 2 ? 2 : 1;
   static constexpr int A_BYTES = NRB * 2 * T5_PART;       // K hi, lo of every row block
-  static constexpr int STAGE = A_BYTES + 2 * T5_PART;     // + W hi, lo of the T5_N pairs
+  static constexpr int B_PART = N * T5_KB * 4;            // W of the N pairs, one part
+  static constexpr int STAGE = A_BYTES + 2 * B_PART;
   static constexpr size_t SMEM = (size_t)S * STAGE + 1024 + 2048;  // + alignment, barriers, indices
-  static constexpr uint32_t TCOLS = NRB == 1 ? 128u : (NRB == 2 ? 256u : 512u);
+  static constexpr uint32_t TCOLS = NRB * N <= 128 ? 128u : (NRB * N <= 256 ? 256u : 512u);
 };
+constexpr int t5_pairs(int nrb) { return nrb <= 2 ? T5Cfg<1>::N : T5Cfg<3>::N; }
+static_assert(T5Cfg<1>::N == T5Cfg<2>::N && T5Cfg<3>::N == T5Cfg<4>::N, "tile width per t5_pairs");
+// resident CTAs per SM (bounded by shared memory) x TCOLS <= the SM's 512 TMEM columns
 static_assert(T5Cfg<1>::SMEM * 5 > 228 * 1024 && T5Cfg<2>::SMEM * 3 > 228 * 1024 &&
-                  T5Cfg<3>::SMEM * 2 > 228 * 1024 && T5Cfg<4>::SMEM * 2 > 228 * 1024,
+                  T5Cfg<3>::SMEM * 3 > 228 * 1024 && T5Cfg<4>::SMEM * 3 > 228 * 1024,
               "resident CTAs per SM must fit the SM's 512 TMEM columns");
 static_assert(T5Cfg<3>::SMEM <= 227 * 1024 && T5Cfg<4>::SMEM <= 227 * 1024, "shared memory per CTA");
 static_assert(T5Cfg<1>::LAG < T5Cfg<1>::S && T5Cfg<2>::LAG < T5Cfg<2>::S &&
@@ -666,7 +674,7 @@ __global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int nkb, int ldk, in
                                                  const float *__restrict__ Wl,
                                                  float *__restrict__ G32, int *__restrict__ status) {
   using C = T5Cfg<NRB>;
-  constexpr int S = C::S, LAG = C::LAG;
+  constexpr int S = C::S, LAG = C::LAG, T5_N = C::N;
   extern __shared__ __align__(128) unsigned char t5raw[];
   unsigned char *sm = (unsigned char *)(((uintptr_t)t5raw + 1023) & ~(uintptr_t)1023);
   uint64_t *fullA = (uint64_t *)(sm + S * C::STAGE);
@@ -737,7 +745,7 @@ __global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int nkb, int ldk, in
         const uint32_t off = (uint32_t)((kq * (T5_N / 8) + rh) * 128 + rl * 16);
         const size_t g = (size_t)(src >= 0 ? src : 0) * ldk + p * T5_KB + kq * 4;
         cp16(sb + C::A_BYTES + off, Wh + g, src >= 0 ? 16 : 0);
-        cp16(sb + C::A_BYTES + T5_PART + off, Wl + g, src >= 0 ? 16 : 0);
+        cp16(sb + C::A_BYTES + C::B_PART + off, Wl + g, src >= 0 ? 16 : 0);
       }
       asm volatile("cp.async.commit_group;" ::: "memory");
       if (p >= LAG) {
@@ -766,7 +774,8 @@ __global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int nkb, int ldk, in
   } else if (warp == 1 && lane == 0) {
     // ---- MMA issuer
     constexpr uint32_t idesc = umma_idesc_tf32(128, T5_N);
-    constexpr uint32_t ks = (128 / 8) * 128;  // core-matrix stride along K
+    constexpr uint32_t ks = (128 / 8) * 128;    // core-matrix stride along K (K rows)
+    constexpr uint32_t bks = (T5_N / 8) * 128;  // the same for the T5_N pair rows
     bool ok = true;
     int c = 0;
     for (; c < nkb; ++c) {
@@ -778,8 +787,8 @@ __global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int nkb, int ldk, in
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t base = smbase + (uint32_t)(st * C::STAGE);
-      const uint64_t bh = umma_desc(base + C::A_BYTES, ks, 128);
-      const uint64_t bl = umma_desc(base + C::A_BYTES + T5_PART, ks, 128);
+      const uint64_t bh = umma_desc(base + C::A_BYTES, bks, 128);
+      const uint64_t bl = umma_desc(base + C::A_BYTES + C::B_PART, bks, 128);
 #pragma unroll
       for (int rb = 0; rb < NRB; ++rb) {
         const uint64_t ah = umma_desc(base + rb * 2 * T5_PART, ks, 128);
@@ -1339,8 +1348,8 @@ int fmm_plan_build(abx_operator *op, int order, FmmPlan *&out) {
   // tensor-core M2L tiles: 64 pairs of one matrix each
   std::vector<int> tmat, tfirst;
   // tensor-core M2L tiles: 64 pairs for the mma.sync kernel (<= 64 nodes),
-  // T5_N pairs for the tcgen05 kernel
-  const int tile_pairs = nc <= 64 ? TC_PAIRS : T5_N;
+  // t5_pairs pairs for the tcgen05 kernel
+  const int tile_pairs = nc <= 64 ? TC_PAIRS : t5_pairs((nc + 127) / 128);
   for (int m = 0; m < P->nmat; ++m)
     for (int q = P->mat_off[m]; q < P->mat_off[m + 1]; q += tile_pairs) {
       tmat.push_back(m);
