@@ -83,6 +83,7 @@ struct abx_operator {
   abx::PairLayout *pairs = nullptr;
   abx::FmmPlan *fmm = nullptr;
   abx::HostStage stage_b, stage_c;
+  abx::DevBuf<double> partial;  // dense mixed matvec: row sums per column chunk
   int64_t last_candidates = 0, last_pairs = 0;
 };
 

@@ -47,9 +47,17 @@ template <int KIND> __device__ __forceinline__ double dk64(double d2, double p0,
   return 0.0;
 }
 
+// Hardware base-2 exponential (MUFU, ~2 ulp), flush-to-zero: the kernel
+// weights it serves are negligible long before 2^-126.
+__device__ __forceinline__ float ex2_approx(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 template <int KIND> __device__ __forceinline__ float dk32(float d2, float p0f, float c_exp2) {
   if (KIND == ABX_K_CONST) return p0f;
-  if (KIND == ABX_K_GAUSSIAN || KIND == ABX_K_COMPACT_GAUSSIAN) return exp2f(d2 * c_exp2);
+  if (KIND == ABX_K_GAUSSIAN || KIND == ABX_K_COMPACT_GAUSSIAN) return ex2_approx(d2 * c_exp2);
   if (KIND == ABX_K_WENDLAND_C2) {
     const float q = d2 * rsqrtf(fmaxf(d2, 1e-36f)) * p0f;
     const float t = fmaxf(1.0f - q, 0.0f);
@@ -68,9 +76,12 @@ template <int KIND> __global__ void __launch_bounds__(DT) k_dense_fp64(DensePara
   __shared__ double sx[DT], sy[DT], sz[DT], sb[DT], ss[DT];
   const int64_t i = (int64_t)blockIdx.x * DT + threadIdx.x;
   const bool act = i < P.nr;
-  double xi[3] = {0, 0, 0};
-  if (act)
-    for (int d = 0; d < P.dim; ++d) xi[d] = P.rpos[(int64_t)d * P.nr + i];
+  double x0 = 0.0, x1 = 0.0, x2 = 0.0;
+  if (act) {
+    x0 = P.rpos[i];
+    if (P.dim > 1) x1 = P.rpos[P.nr + i];
+    if (P.dim > 2) x2 = P.rpos[2 * P.nr + i];
+  }
   const double si = (KIND == ABX_K_SCALAR_SUM && act) ? P.s_row[i] : 0.0;
   double acc = 0.0;
   for (int64_t t = 0; t < P.nc; t += DT) {
@@ -85,11 +96,16 @@ template <int KIND> __global__ void __launch_bounds__(DT) k_dense_fp64(DensePara
     __syncthreads();
     const int nt = (int)((P.nc - t) < DT ? (P.nc - t) : DT);
     for (int jj = 0; jj < nt; ++jj) {
-      const double pj[3] = {sx[jj], sy[jj], sz[jj]};
-      double d2 = 0.0;
-      for (int d = 0; d < P.dim; ++d) {
-        const double dx = __dsub_rn(pj[d], xi[d]);
-        d2 = __dadd_rn(d2, __dmul_rn(dx, dx));
+      // sum of squares in dimension order (0 + dx0^2 is exact)
+      const double dx0 = __dsub_rn(sx[jj], x0);
+      double d2 = __dmul_rn(dx0, dx0);
+      if (P.dim > 1) {
+        const double dx1 = __dsub_rn(sy[jj], x1);
+        d2 = __dadd_rn(d2, __dmul_rn(dx1, dx1));
+      }
+      if (P.dim > 2) {
+        const double dx2 = __dsub_rn(sz[jj], x2);
+        d2 = __dadd_rn(d2, __dmul_rn(dx2, dx2));
       }
       acc = __dadd_rn(acc, __dmul_rn(dk64<KIND>(d2, P.p0, si, ss[jj]), sb[jj]));
     }
@@ -98,44 +114,110 @@ template <int KIND> __global__ void __launch_bounds__(DT) k_dense_fp64(DensePara
   if (act) P.c[i] = acc;
 }
 
-template <int KIND> __global__ void __launch_bounds__(DT) k_dense_mixed(DenseParams P) {
-  __shared__ float4 sp[DT];
-  const int64_t i = (int64_t)blockIdx.x * DT + threadIdx.x;
-  const bool act = i < P.nr;
-  float xi[3] = {0.f, 0.f, 0.f};
-  if (act)
-    for (int d = 0; d < P.dim; ++d) xi[d] = (float)(P.rpos[(int64_t)d * P.nr + i] - P.origin[d]);
-  double acc = 0.0;
-  for (int64_t t = 0; t < P.nc; t += DT) {
-    const int64_t j = t + threadIdx.x;
-    if (j < P.nc) {
-      float4 v;
-      v.x = (float)(P.cpos[j] - P.origin[0]);
-      v.y = P.dim > 1 ? (float)(P.cpos[P.nc + j] - P.origin[1]) : 0.f;
-      v.z = P.dim > 2 ? (float)(P.cpos[2 * P.nc + j] - P.origin[2]) : 0.f;
-      v.w = (float)P.b[j];
-      sp[threadIdx.x] = v;
-    }
-    __syncthreads();
-    const int nt = (int)((P.nc - t) < DT ? (P.nc - t) : DT);
-    float a32 = 0.f;
-    for (int jj = 0; jj < nt; ++jj) {
-      const float4 v = sp[jj];
-      const float d0 = v.x - xi[0], d1 = v.y - xi[1], d2v = v.z - xi[2];
-      const float dd = fmaf(d2v, d2v, fmaf(d1, d1, d0 * d0));
-      a32 = fmaf(dk32<KIND>(dd, P.p0f, P.c_exp2), v.w, a32);
-    }
-    acc += (double)a32;
-    __syncthreads();
+// Kernel values of two pairs: packed FP32x2 where the formula allows.
+template <int KIND> __device__ __forceinline__ float2 dk32x2(float2 dd, float p0f, float c_exp2) {
+  if (KIND == ABX_K_GAUSSIAN || KIND == ABX_K_COMPACT_GAUSSIAN) {
+    const float2 e = __fmul2_rn(dd, make_float2(c_exp2, c_exp2));
+    return make_float2(ex2_approx(e.x), ex2_approx(e.y));
   }
-  if (act) P.c[i] = acc;
+  return make_float2(dk32<KIND>(dd.x, p0f, c_exp2), dk32<KIND>(dd.y, p0f, c_exp2));
 }
 
-template <int KIND> int launch_dense(abx_context *ctx, const DenseParams &P, bool mixed) {
+// Mixed precision: FP32 offsets from the column domain centre, FP32 kernel
+// values, one row per thread against two columns per packed FP32x2
+// instruction; each staged tile of DT columns is summed in FP32 and tiles are
+// added in FP64.  blockIdx.y selects a chunk of chunk_cols columns, so that
+// small row counts still fill the GPU; with more than one chunk each CTA
+// writes its row sums to partial[chunk][row] and k_dense_reduce adds the
+// chunks in order (deterministic).  Columns are staged as pairs, pp[2h] = (x_a, x_b, y_a, y_b),
+// pp[2h+1] = (z_a, z_b, b_a, b_b); an odd tail is paired with a far-away
+// column of weight 0 (finite for every kernel).
+template <int KIND>
+__global__ void __launch_bounds__(DT) k_dense_mixed(DenseParams P, int64_t chunk_cols,
+                                                    double *__restrict__ partial) {
+  __shared__ float4 pp[DT];
+  const int64_t i = (int64_t)blockIdx.x * DT + threadIdx.x;
+  const bool act = i < P.nr;
+  float x0 = 0.f, x1 = 0.f, x2 = 0.f;
+  if (act) {
+    x0 = (float)(P.rpos[i] - P.origin[0]);
+    if (P.dim > 1) x1 = (float)(P.rpos[P.nr + i] - P.origin[1]);
+    if (P.dim > 2) x2 = (float)(P.rpos[2 * P.nr + i] - P.origin[2]);
+  }
+  const float2 nqx = make_float2(-x0, -x0), nqy = make_float2(-x1, -x1), nqz = make_float2(-x2, -x2);
+  double acc = 0.0;
+  const int64_t c0 = (int64_t)blockIdx.y * chunk_cols;
+  const int64_t c1 = c0 + chunk_cols < P.nc ? c0 + chunk_cols : P.nc;
+  for (int64_t t = c0; t < c1; t += DT) {
+    const int64_t j = t + threadIdx.x;
+    float x = 1e4f, y = 1e4f, z = 1e4f, w = 0.f;
+    if (j < c1) {
+      x = (float)(P.cpos[j] - P.origin[0]);
+      y = P.dim > 1 ? (float)(P.cpos[P.nc + j] - P.origin[1]) : 0.f;
+      z = P.dim > 2 ? (float)(P.cpos[2 * P.nc + j] - P.origin[2]) : 0.f;
+      w = (float)P.b[j];
+    }
+    float *pf = reinterpret_cast<float *>(&pp[2 * (threadIdx.x >> 1)]);
+    const int o = threadIdx.x & 1;
+    pf[o] = x;
+    pf[2 + o] = y;
+    pf[4 + o] = z;
+    pf[6 + o] = w;
+    __syncthreads();
+    const int nt = (int)((c1 - t) < DT ? (c1 - t) : DT);
+    const int npair = (nt + 1) >> 1;
+    float2 a2 = make_float2(0.f, 0.f);
+#pragma unroll 4
+    for (int h = 0; h < npair; ++h) {
+      const float4 A = pp[2 * h], B = pp[2 * h + 1];
+      const float2 dx = __fadd2_rn(make_float2(A.x, A.y), nqx);
+      const float2 dy = __fadd2_rn(make_float2(A.z, A.w), nqy);
+      const float2 dz = __fadd2_rn(make_float2(B.x, B.y), nqz);
+      float2 dd = __fmul2_rn(dx, dx);
+      dd = __ffma2_rn(dy, dy, dd);
+      dd = __ffma2_rn(dz, dz, dd);
+      a2 = __ffma2_rn(dk32x2<KIND>(dd, P.p0f, P.c_exp2), make_float2(B.z, B.w), a2);
+    }
+    acc += (double)(a2.x + a2.y);
+    __syncthreads();
+  }
+  if (act) {
+    if (partial) partial[(int64_t)blockIdx.y * P.nr + i] = acc;
+    else P.c[i] = acc;
+  }
+}
+
+__global__ void k_dense_reduce(const double *__restrict__ partial, int64_t nr, int chunks,
+                               double *__restrict__ c) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nr) return;
+  double s = 0.0;
+  for (int k = 0; k < chunks; ++k) s += partial[(int64_t)k * nr + i];
+  c[i] = s;
+}
+
+template <int KIND>
+int launch_dense(abx_context *ctx, const DenseParams &P, bool mixed, abx_operator *op) {
   const unsigned blocks = ceil_div(P.nr, DT);
-  if (mixed && KIND != ABX_K_SCALAR_SUM)
-    k_dense_mixed<KIND><<<blocks, DT, 0, ctx->stream>>>(P);
-  else
+  if (mixed && KIND != ABX_K_SCALAR_SUM) {
+    // about 32 CTAs per SM in all: split the columns when the rows alone
+    // give fewer
+    const int64_t tiles = (P.nc + DT - 1) / DT;
+    const int64_t want = (32 * (int64_t)std::max(ctx->num_sms, 1) + blocks - 1) / blocks;
+    const int chunks = (int)std::max<int64_t>(1, std::min<int64_t>(want, std::min<int64_t>(tiles, 65535)));
+    // no columns: one chunk that writes zeros
+    const int64_t chunk_cols = tiles > 0 ? ((tiles + chunks - 1) / chunks) * DT : DT;
+    const int used = tiles > 0 ? (int)((P.nc + chunk_cols - 1) / chunk_cols) : 1;
+    double *partial = nullptr;
+    if (used > 1) {
+      ABX_TRY(op->partial.reserve((size_t)used * P.nr));
+      partial = op->partial.ptr;
+    }
+    k_dense_mixed<KIND><<<dim3(blocks, std::max(used, 1)), DT, 0, ctx->stream>>>(P, chunk_cols,
+                                                                               partial);
+    if (partial)
+      k_dense_reduce<<<ceil_div(P.nr, 256), 256, 0, ctx->stream>>>(partial, P.nr, used, P.c);
+  } else
     k_dense_fp64<KIND><<<blocks, DT, 0, ctx->stream>>>(P);
   ABX_CHECK_CUDA(cudaGetLastError());
   return ABX_OK;
@@ -172,13 +254,13 @@ int dense_matvec_device(abx_operator *op, const double *b, double *c) {
   if (P.nr == 0) return ABX_OK;
   const bool mixed = op->precision == ABX_PREC_MIXED;
   switch (P.kind) {
-  case ABX_K_CONST: return launch_dense<ABX_K_CONST>(ctx, P, mixed);
-  case ABX_K_GAUSSIAN: return launch_dense<ABX_K_GAUSSIAN>(ctx, P, mixed);
-  case ABX_K_WENDLAND_C2: return launch_dense<ABX_K_WENDLAND_C2>(ctx, P, mixed);
-  case ABX_K_COMPACT_GAUSSIAN: return launch_dense<ABX_K_COMPACT_GAUSSIAN>(ctx, P, mixed);
-  case ABX_K_LAPLACE: return launch_dense<ABX_K_LAPLACE>(ctx, P, mixed);
-  case ABX_K_MULTIQUADRIC: return launch_dense<ABX_K_MULTIQUADRIC>(ctx, P, mixed);
-  case ABX_K_SCALAR_SUM: return launch_dense<ABX_K_SCALAR_SUM>(ctx, P, false);
+  case ABX_K_CONST: return launch_dense<ABX_K_CONST>(ctx, P, mixed, op);
+  case ABX_K_GAUSSIAN: return launch_dense<ABX_K_GAUSSIAN>(ctx, P, mixed, op);
+  case ABX_K_WENDLAND_C2: return launch_dense<ABX_K_WENDLAND_C2>(ctx, P, mixed, op);
+  case ABX_K_COMPACT_GAUSSIAN: return launch_dense<ABX_K_COMPACT_GAUSSIAN>(ctx, P, mixed, op);
+  case ABX_K_LAPLACE: return launch_dense<ABX_K_LAPLACE>(ctx, P, mixed, op);
+  case ABX_K_MULTIQUADRIC: return launch_dense<ABX_K_MULTIQUADRIC>(ctx, P, mixed, op);
+  case ABX_K_SCALAR_SUM: return launch_dense<ABX_K_SCALAR_SUM>(ctx, P, false, op);
   }
   set_error("unknown kernel kind %d", P.kind);
   return ABX_ERR_INVALID;

@@ -312,6 +312,7 @@ def run_ours(args):
     if not args.matvec_only:
         del K
         out["cfg1"] = cfg1_section(ctx)
+        out["dense"] = dense_section(ctx)
         out["rbf_as_specified"] = cfg4_as_specified(ctx)
         models = ROOT / "aboria_gb300" / "models"
         out["rbf_solve"] = rbf_section(ctx, models / "spai_mlp_2d.bin")
@@ -485,6 +486,43 @@ def _event_ms(fn, stream, reps):
         torch.cuda.synchronize()
         ts.append(e0.elapsed_time(e1))
     return float(np.median(ts))
+
+
+def dense_section(ctx, n=65536, reps=5):
+    """Dense operator (create_dense_operator, every pair): N uniform points in
+    the unit cube, Gaussian exp(-|dx|^2 / 0.1^2), b U[0,1].  K*b in FP64 and
+    mixed precision (CUDA events, medians), pairs per second, the FP32 compute
+    roofline of the mixed kernel (FP32 FLOP per pair: dx 3, d2 5, exponent 1,
+    accumulate 2, plus one exp2 on the special-function unit), and the mixed
+    error against FP64."""
+    import torch
+    import aboria_gb300 as ab
+    import workloads
+    stream = torch.cuda.current_stream()
+    pos = workloads.uniform(n, 3, seed=1101)
+    p = ab.Particles(3, ctx).set(pos)
+    kern = ab.Kernel.make(ab.K_GAUSSIAN, 1.0 / 0.1 ** 2)
+    b = torch.from_numpy(np.random.default_rng(1102).uniform(0, 1, n)).cuda()
+    c = torch.empty_like(b)
+    out = {"workload": f"3-D N={n} uniform, dense Gaussian exp(-|dx|^2/0.1^2), {n * n:.3e} pairs"}
+    res = {}
+    peaks, _ = measured_peaks()
+    sm_max = peaks.get("sm_max_mhz", 2070.0)
+    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    for prec, name in ((ab.PREC_FP64, "fp64"), (ab.PREC_MIXED, "mixed")):
+        K = ab.create_dense_operator(p, p, kern, prec)
+        K.matvec(b, out=c)
+        ms = _event_ms(lambda: K.matvec(b, out=c, sync=False), stream, reps)
+        out[f"{name}_matvec_ms"] = ms
+        out[f"{name}_gpairs_per_s"] = n * n / (ms / 1e3) / 1e9
+        res[name] = c.cpu().numpy()
+        del K
+    tflops = n * n * 11 / (out["mixed_matvec_ms"] / 1e3) / 1e12
+    out["mixed_compute_roofline"] = {"achieved_tflops": tflops, "peak_tflops": fp32_peak,
+                                     "frac": tflops / fp32_peak, "flop_per_pair": 11}
+    out["mixed_vs_fp64_rel_l2"] = float(np.linalg.norm(res["mixed"] - res["fp64"])
+                                        / np.linalg.norm(res["fp64"]))
+    return out
 
 
 def cfg1_section(ctx):

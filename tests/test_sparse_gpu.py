@@ -140,20 +140,24 @@ def test_device_vectors_and_linearity():
     assert rel(lhs, rhs) < 1e-13
 
 
-def test_dense_vs_oracle():
-    pos = workloads.uniform(3000, 3, seed=33)
-    a = ab.Particles(3).set(pos)
+@pytest.mark.parametrize("dim,n", [(3, 3000), (2, 1001)])
+def test_dense_vs_oracle(dim, n):
+    """FP64 mode bit-for-bit in the reference's column order (1e-14); mixed
+    mode (packed FP32x2 pairs, an odd tile tail padded with a zero-weight
+    column) to 1e-5."""
+    pos = workloads.uniform(n, dim, seed=33)
+    a = ab.Particles(dim).set(pos)
     rng = np.random.default_rng(34)
-    b = rng.standard_normal(3000)
+    b = rng.standard_normal(n)
     for kind, params in ((ab.K_GAUSSIAN, [30.0]), (ab.K_MULTIQUADRIC, [0.01]),
-                         (ab.K_LAPLACE, [1e-12])):
+                         (ab.K_LAPLACE, [1e-12]), (ab.K_WENDLAND_C2, [5.0])):
         A = ab.create_dense_operator(a, a, ab.Kernel.make(kind, *params))
         ref = oracle.dense_matvec(pos, pos, kind, params, b)
         c = A * b
         # FP64 mode walks the columns in the reference's order
-        assert rel(c, ref) < 1e-14
+        assert rel(c, ref) < 1e-14, kind
         A.set_precision(ab.PREC_MIXED)
-        assert rel(A * b, ref) < 1e-5
+        assert rel(A * b, ref) < 1e-5, kind
 
 
 def test_empty_operator():
@@ -161,3 +165,20 @@ def test_empty_operator():
     p.init_neighbour_search([0] * 3, [1] * 3, [False] * 3)
     K = ab.create_sparse_operator(p, p, 0.1, ab.Kernel.make(ab.K_CONST, 1.0))
     assert (K * np.zeros(0)).shape == (0,)
+
+
+def test_dense_chunked_and_empty_columns():
+    """Few rows against many columns: the mixed kernel splits the columns into
+    chunks (79 here) whose row sums are added in order; no columns: zeros."""
+    rows = workloads.uniform(300, 3, seed=35)
+    cols = workloads.uniform(20000, 3, seed=36)
+    b = np.random.default_rng(37).standard_normal(20000)
+    r, c = ab.Particles(3).set(rows), ab.Particles(3).set(cols)
+    A = ab.create_dense_operator(r, c, ab.Kernel.make(ab.K_GAUSSIAN, 30.0), ab.PREC_MIXED)
+    ref = oracle.dense_matvec(rows, cols, ab.K_GAUSSIAN, [30.0], b)
+    assert rel(A * b, ref) < 1e-5
+    assert np.array_equal(A * b, A * b)  # deterministic
+    e = ab.Particles(3).set(np.zeros((0, 3)))
+    for prec in (ab.PREC_MIXED, ab.PREC_FP64):
+        E = ab.create_dense_operator(r, e, ab.Kernel.make(ab.K_GAUSSIAN, 30.0), prec)
+        assert np.array_equal(E * np.zeros(0), np.zeros(300))
