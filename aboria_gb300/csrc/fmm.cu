@@ -1005,9 +1005,8 @@ constexpr int PW = 4;   // target leaves (warps) per CTA
 template <int KIND>
 __global__ void __launch_bounds__(PT * PW) k_l2p_p2p32(
     int D, int n, int ncheb, int nleaves, const int *__restrict__ leaves, const int *__restrict__ nb,
-    const int *__restrict__ ne, const double *__restrict__ box, const double *__restrict__ pos,
-    int64_t npos, const float4 *__restrict__ posf, const float *__restrict__ b32,
-    const double *__restrict__ b, const int *__restrict__ mi, const double *__restrict__ G,
+    const int *__restrict__ ne, const double *__restrict__ box, const float4 *__restrict__ posf,
+    const float *__restrict__ b32, const double *__restrict__ b, const double *__restrict__ G,
     const int *__restrict__ rp, const int *__restrict__ src, double p0, const ChebTab32 tab,
     double *__restrict__ c) {
   __shared__ float sg_all[PW][MAXC];
@@ -1416,9 +1415,8 @@ int launch_l2p_p2p(FmmPlan *P, cudaStream_t s, const double *pos, int64_t npos, 
     // P->b32 holds this matvec's FP32 weights (converted before the P2M)
     k_l2p_p2p32<KIND><<<ceil_div((size_t)P->nleaves, PW), PT * PW, 0, s>>>(
         P->D, P->n, P->ncheb, P->nleaves, P->leaf_ids.ptr, P->node_begin.ptr, P->node_end.ptr,
-        P->box.ptr, pos,
-        npos, P->posf.ptr, P->b32.ptr, b, P->mi_d.ptr, P->G.ptr, P->p2p_rowptr.ptr,
-        P->p2p_src.ptr, P->p0, P->tab32, c);
+        P->box.ptr, P->posf.ptr, P->b32.ptr, b, P->G.ptr, P->p2p_rowptr.ptr, P->p2p_src.ptr,
+        P->p0, P->tab32, c);
   } else
     k_l2p_p2p<KIND, false><<<P->nleaves, FT, 0, s>>>(
         P->D, P->n, P->ncheb, P->leaf_ids.ptr, P->node_begin.ptr, P->node_end.ptr, P->box.ptr, pos,
