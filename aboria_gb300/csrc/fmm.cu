@@ -826,10 +826,15 @@ __global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int nkb, int ldk, in
     }
   } else {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
+    // per warp a 16 x 32 transpose tile in the (now idle) first stage: lane
+    // = row on the way in, (pair, 4 consecutive rows) on the way out, so that
+    // G receives 16-byte vector reductions (ldg and the row groups are
+    // multiples of 4; groups at or beyond ncheb are skipped)
+    float *tt = reinterpret_cast<float *>(sm) + warp * (16 * 32);
+#pragma unroll 1
     for (int rb = 0; rb < NRB; ++rb) {
-      const int i = rb * 128 + 32 * warp + lane;
-#pragma unroll
+      const int i0 = rb * 128 + 32 * warp;
+#pragma unroll 1
       for (int c0 = 0; c0 < T5_N; c0 += 16) {
         uint32_t v[16];
         asm volatile(
@@ -840,13 +845,22 @@ __global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int nkb, int ldk, in
               "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
             : "r"(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(rb * T5_N + c0)));
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (i < ncheb) {
 #pragma unroll
-          for (int q = 0; q < 16; ++q) {
-            const int tgt = sTgt[c0 + q];
-            if (tgt >= 0) atomicAdd(&G32[(size_t)tgt * ldg + i], __uint_as_float(v[q]));
+        for (int q = 0; q < 16; ++q) tt[q * 32 + lane] = __uint_as_float(v[q]);
+        __syncwarp();
+#pragma unroll
+        for (int it = 0; it < 4; ++it) {
+          const int q = it * 4 + (lane >> 3), g = (lane & 7) * 4;
+          const int tgt = sTgt[c0 + q];
+          if (tgt >= 0 && i0 + g < ncheb) {
+            const float4 a = *reinterpret_cast<const float4 *>(&tt[q * 32 + g]);
+            float *dst = G32 + (size_t)tgt * ldg + i0 + g;
+            asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst), "f"(a.x),
+                         "f"(a.y), "f"(a.z), "f"(a.w)
+                         : "memory");
           }
         }
+        __syncwarp();
       }
     }
   }
