@@ -45,3 +45,11 @@ def test_two_gloo_ranks_take_the_slowest_time():
 def test_single_rank_is_identity():
     assert bench.slowest_rank([1.5, 2.5], 1) == [1.5, 2.5]
     assert bench.replica_throughput(1, 10, 2.0) == 5.0
+
+
+def test_bench_reads_the_committed_profile_traffic():
+    """The bench's roofline `traffic` comes from the committed ncu summary of
+    the pair kernel; it must parse to a per-launch byte count no smaller than
+    the compulsory bytes of the workload (N x 40 B)."""
+    t = bench.profile_traffic()
+    assert t is not None and t >= bench.N_PARTICLES * 40
