@@ -92,6 +92,22 @@ inline double norm2(const double *dx, int D) {
   return accum;
 }
 
+// distance_helper<N> (src/detail/Distance.h:46-137) for the norms of
+// euclidean_search (N = 2), manhatten_search (N = 1) and chebyshev_search
+// (N = -1, src/Search.h:797-845): the accumulated value (sum of dx^2, sum of
+// |dx|, max of |dx|) and its threshold get_value_to_accumulate(r)
+// (src/Search.h:184-186): r^2 for N = 2, |r| otherwise.
+inline double norm_acc(const double *dx, int D, int lnorm) {
+  if (lnorm == 2) return norm2(dx, D);
+  double accum = 0;
+  for (int i = 0; i < D; ++i) {
+    const double a = std::abs(dx[i]);
+    accum = lnorm == -1 ? (a > accum ? a : accum) : accum + a;
+  }
+  return accum;
+}
+inline double norm_threshold(double r, int lnorm) { return lnorm == 2 ? r * r : std::abs(r); }
+
 // Built-in kernel functors (the closures the reference's tests and the
 // benchmark workloads pass to create_sparse_operator / create_dense_operator).
 enum {
@@ -150,12 +166,13 @@ struct CellList {
 // x bucket quadrants (lattice_iterator_within_distance,
 // src/NeighbourSearchBase.h:1720-2009) x bucket storage order
 // (CellListOrderedQuery::get_bucket_particles, src/CellListOrdered.h:472-491),
-// with check_candidate's FP64 test (src/Search.h:438-465).
+// with check_candidate's FP64 test (src/Search.h:438-465), in the norm lnorm
+// (2, 1 or -1; the domain, bucket and pair tests all use it).
 template <class Visit>
-void search_walk(const CellList &cl, const double *x, double r, Visit &&visit) {
+void search_walk(const CellList &cl, const double *x, double r, Visit &&visit, int lnorm = 2) {
   const Grid &g = cl.g;
   const int D = g.D;
-  const double r2 = r * r;  // get_value_to_accumulate: pow(r, 2)
+  const double r2 = norm_threshold(r, lnorm);  // get_value_to_accumulate(r)
   double L[3], half_side[3];
   for (int d = 0; d < D; ++d) {
     L[d] = g.hi[d] - g.lo[d];
@@ -179,7 +196,7 @@ void search_walk(const CellList &cl, const double *x, double r, Visit &&visit) {
         const double hd = 0.5 * (g.hi[d] - g.lo[d]);
         dx[d] = std::max(std::abs(c) - hd, 0.0);
       }
-      outside = norm2(dx, D) > r2;
+      outside = norm_acc(dx, D, lnorm) > r2;
     }
     if (!outside) {
       auto min_dist = [&](const int *b) {
@@ -188,7 +205,7 @@ void search_walk(const CellList &cl, const double *x, double r, Visit &&visit) {
           const double centre = (b[d] + 0.5) * g.side[d] + g.lo[d];
           dx[d] = std::max(std::abs(centre - p[d]) - half_side[d], 0.0);
         }
-        return norm2(dx, D);
+        return norm_acc(dx, D, lnorm);
       };
       for (int quadrant = 0; quadrant < (1 << D); ++quadrant) {
         int mn[3], idx[3];
@@ -221,7 +238,7 @@ void search_walk(const CellList &cl, const double *x, double r, Visit &&visit) {
             const double *pj = cl.pos + (int64_t)k * D;
             double dx[3];
             for (int d = 0; d < D; ++d) dx[d] = pj[d] - p[d];
-            if (!(norm2(dx, D) > r2)) visit((int64_t)k, dx);
+            if (!(norm_acc(dx, D, lnorm) > r2)) visit((int64_t)k, dx);
           }
           // increment, NeighbourSearchBase.h:1960-2008
           bool valid = false;
@@ -393,12 +410,13 @@ int64_t orc_celllist_build(int D, int64_t n, double *pos_io, const double *lo,
 }
 
 // Neighbour counts of nq query points against a built cell list
-// (euclidean_search, src/Search.h:839-845), OpenMP over queries.
+// (euclidean_search / manhatten_search / chebyshev_search by lnorm = 2 / 1 /
+// -1, src/Search.h:797-845), OpenMP over queries.
 void orc_radius_count(int D, const uint32_t *size, const double *lo,
                       const double *hi, const int *periodic, const double *side,
                       int64_t n, const double *pos_sorted, const uint32_t *bbegin,
                       const uint32_t *bend, int64_t nq, const double *q, double r,
-                      int32_t *counts) {
+                      int lnorm, int32_t *counts) {
   CellList cl;
   Grid &g = cl.g;
   g.D = D;
@@ -419,17 +437,18 @@ void orc_radius_count(int D, const uint32_t *size, const double *lo,
 #pragma omp parallel for schedule(dynamic, 64)
   for (int64_t i = 0; i < nq; ++i) {
     int32_t c = 0;
-    search_walk(cl, q + i * D, r, [&](int64_t, const double *) { ++c; });
+    search_walk(cl, q + i * D, r, [&](int64_t, const double *) { ++c; }, lnorm);
     counts[i] = c;
   }
 }
 
-// Neighbour lists in the reference's visiting order, CSR (rowptr from counts).
+// Neighbour lists in the reference's visiting order, CSR (rowptr from counts),
+// in the norm lnorm as for orc_radius_count.
 void orc_radius_lists(int D, const uint32_t *size, const double *lo,
                       const double *hi, const int *periodic, const double *side,
                       int64_t n, const double *pos_sorted, const uint32_t *bbegin,
                       const uint32_t *bend, int64_t nq, const double *q, double r,
-                      const int64_t *rowptr, int64_t *cols, double *dx_out) {
+                      int lnorm, const int64_t *rowptr, int64_t *cols, double *dx_out) {
   CellList cl;
   Grid &g = cl.g;
   g.D = D;
@@ -453,7 +472,7 @@ void orc_radius_lists(int D, const uint32_t *size, const double *lo,
       if (dx_out)
         for (int d = 0; d < D; ++d) dx_out[o * D + d] = dx[d];
       ++o;
-    });
+    }, lnorm);
   }
 }
 

@@ -154,21 +154,24 @@ def _grid_args(cl: CellList):
     return size, side
 
 
-def radius_count(cl: CellList, q, r):
+def radius_count(cl: CellList, q, r, lnorm=2):
+    """Neighbour counts; lnorm 2 / 1 / -1 = euclidean_search / manhatten_search
+    / chebyshev_search (src/Search.h:797-845)."""
     q = np.ascontiguousarray(q, np.float64).reshape(-1, cl.dim)
     size, side = _grid_args(cl)
     out = np.zeros(q.shape[0], np.int32)
     lib().orc_radius_count(C.c_int(cl.dim), _p(size), _p(cl.lo), _p(cl.hi), _p(cl.periodic),
                            _p(side), C.c_int64(cl.n), _p(np.ascontiguousarray(cl.pos)),
                            _p(cl.begin), _p(cl.end), C.c_int64(q.shape[0]), _p(q), C.c_double(r),
-                           _p(out))
+                           C.c_int(lnorm), _p(out))
     return out
 
 
-def radius_lists(cl: CellList, q, r, with_dx=False):
-    """Neighbour lists in the reference's visiting order (CSR)."""
+def radius_lists(cl: CellList, q, r, with_dx=False, lnorm=2):
+    """Neighbour lists in the reference's visiting order (CSR), norm as for
+    radius_count."""
     q = np.ascontiguousarray(q, np.float64).reshape(-1, cl.dim)
-    counts = radius_count(cl, q, r)
+    counts = radius_count(cl, q, r, lnorm)
     rowptr = np.zeros(q.shape[0] + 1, np.int64)
     np.cumsum(counts, out=rowptr[1:])
     nnz = int(rowptr[-1])
@@ -178,7 +181,7 @@ def radius_lists(cl: CellList, q, r, with_dx=False):
     lib().orc_radius_lists(C.c_int(cl.dim), _p(size), _p(cl.lo), _p(cl.hi), _p(cl.periodic),
                            _p(side), C.c_int64(cl.n), _p(np.ascontiguousarray(cl.pos)),
                            _p(cl.begin), _p(cl.end), C.c_int64(q.shape[0]), _p(q), C.c_double(r),
-                           _p(rowptr), _p(cols), _p(dx))
+                           C.c_int(lnorm), _p(rowptr), _p(cols), _p(dx))
     return rowptr, cols[:nnz], (dx[:nnz] if with_dx else None)
 
 

@@ -73,6 +73,48 @@ def test_regular_lattice_counts(case):
     assert np.all(counts == gauss_circle(case["r"]))
 
 
+@pytest.mark.parametrize("case", KATS["regular_lattice_linf"]["cases"])
+def test_regular_lattice_box_counts(case):
+    """The reference's box search (chebyshev norm) on the periodic lattice:
+    (2 floor(r) + 1)^D neighbours for every point."""
+    d, n = case["dim"], case["n"]
+    pos = workloads.lattice(n, d)
+    cl = oracle.celllist_build(pos, [0.0] * d, [float(n)] * d, [True] * d, case["n_leaf"])
+    counts = oracle.radius_count(cl, cl.pos, case["r"], lnorm=-1)
+    assert np.all(counts == (2 * int(np.floor(case["r"])) + 1) ** d)
+
+
+def _brute_norm_counts(pos, L, periodic, r, lnorm):
+    """Independent numpy restatement: minimum-image offsets (exact while r <
+    L/2), then sum dx^2 <= r^2, sum |dx| <= r or max |dx| <= r."""
+    out = np.zeros(len(pos), np.int64)
+    for s in range(0, len(pos), 256):
+        dx = pos[None, :, :] - pos[s:s + 256, None, :]
+        if periodic:
+            dx -= L * np.round(dx / L)
+        a = np.abs(dx)
+        if lnorm == 2:
+            ok = (dx * dx).sum(-1) <= r * r
+        elif lnorm == 1:
+            ok = a.sum(-1) <= r
+        else:
+            ok = a.max(-1) <= r
+        out[s:s + 256] = ok.sum(1)
+    return out
+
+
+@pytest.mark.parametrize("lnorm", [2, 1, -1])
+@pytest.mark.parametrize("periodic", [False, True])
+def test_norm_searches_vs_brute_force(lnorm, periodic):
+    """manhatten_search / chebyshev_search / euclidean_search counts
+    (src/Search.h:797-845) against a brute force, 3-D, r below half the box."""
+    pos = workloads.uniform(3000, 3, seed=4100)
+    cl = oracle.celllist_build(pos, [0.0] * 3, [1.0] * 3, [periodic] * 3, 10.0)
+    r = 0.12
+    counts = oracle.radius_count(cl, cl.pos, r, lnorm=lnorm)
+    assert np.array_equal(counts, _brute_norm_counts(cl.pos, 1.0, periodic, r, lnorm))
+
+
 @pytest.mark.parametrize("case", KATS["random_brute_force"]["cases"])
 def test_random_counts_vs_brute_force(case):
     d = case["dim"]
