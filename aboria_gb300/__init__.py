@@ -29,6 +29,7 @@ __all__ = [
     "K_MULTIQUADRIC", "K_SCALAR_SUM", "default_context", "Preconditioner",
     "schwarz_preconditioner", "spai_preconditioner", "gmres", "knn", "spai_exact_rows", "MLP",
     "spai_features", "learned_preconditioner", "spai_local_inverse_rows", "create_fmm_operator", "fmm_stats", "spai_rows", "gmres_with_fallback",
+    "fp32_peak_tflops", "fmm_set_wait_limit",
 ]
 
 PREC_FP64, PREC_MIXED = 0, 1
@@ -200,28 +201,39 @@ class Particles:
         return bb, be, keys
 
 
-def radius_count(p: Particles, q, r: float, out=None):
-    """Neighbour counts of ``euclidean_search(p.get_query(), q_i, r)``."""
+def radius_count(p: Particles, q, r: float, out=None, lnorm: int = 2):
+    """Neighbour counts of ``euclidean_search(p.get_query(), q_i, r)``;
+    lnorm 1 / -1 give ``manhatten_search`` / ``chebyshev_search``."""
     nq = int(q.shape[0])
     if isinstance(q, np.ndarray):
         q = np.ascontiguousarray(q, dtype=np.float64)
     if out is None:
         out = np.empty(nq, dtype=np.int32)
-    _check(lib().abx_radius_count(p._h, nq, _ptr(q), float(r), _ptr(out)), "abx_radius_count")
+    _check(lib().abx_radius_count_lnorm(p._h, nq, _ptr(q), float(r), int(lnorm), _ptr(out)),
+           "abx_radius_count")
     return out
 
 
-def radius_query_csr(p: Particles, q, r: float):
-    """Neighbour lists (storage indices) as CSR ``(rowptr, cols)``."""
+def radius_query_csr(p: Particles, q, r: float, lnorm: int = 2, with_dx: bool = False):
+    """Neighbour lists (storage indices) as CSR ``(rowptr, cols)``; lnorm as
+    for radius_count.  with_dx (euclidean only) also returns dx[nnz, dim],
+    x_j - (x + image*L) for the periodic image the search accepted."""
     nq = int(q.shape[0])
     q = np.ascontiguousarray(q, dtype=np.float64)
     rowptr = np.empty(nq + 1, dtype=np.int64)
-    _check(lib().abx_radius_query_csr(p._h, nq, _ptr(q), float(r), _ptr(rowptr), None, 0),
-           "abx_radius_query_csr")
+    _check(lib().abx_radius_query_csr_lnorm(p._h, nq, _ptr(q), float(r), int(lnorm), _ptr(rowptr),
+                                            None, 0), "abx_radius_query_csr")
     nnz = int(rowptr[-1])
     cols = np.empty(max(nnz, 1), dtype=np.int32)
-    _check(lib().abx_radius_query_csr(p._h, nq, _ptr(q), float(r), _ptr(rowptr), _ptr(cols), nnz),
-           "abx_radius_query_csr")
+    if with_dx:
+        if lnorm != 2:
+            raise ValueError("dx is returned by the euclidean search only")
+        dx = np.empty((max(nnz, 1), p.dim), dtype=np.float64)
+        _check(lib().abx_radius_query_csr_dx(p._h, nq, _ptr(q), float(r), _ptr(rowptr), _ptr(cols),
+                                             _ptr(dx), nnz), "abx_radius_query_csr_dx")
+        return rowptr, cols[:nnz], dx[:nnz]
+    _check(lib().abx_radius_query_csr_lnorm(p._h, nq, _ptr(q), float(r), int(lnorm), _ptr(rowptr),
+                                            _ptr(cols), nnz), "abx_radius_query_csr")
     return rowptr, cols[:nnz]
 
 
@@ -550,8 +562,26 @@ def create_fmm_operator(p: Particles, kernel: Kernel, order: int = 3,
     return Operator(h, p, p).set_precision(precision)
 
 
+def fmm_set_wait_limit(op: Operator, seconds: float = 1.0, drop_one_arrive: bool = False):
+    """Limit of the tensor-core M2L's device-side waits (``abx_fmm_set_wait_limit``);
+    drop_one_arrive is the tests' fault injection (a barrier nothing arrives
+    on), after which the matvec raises ABXError with status ABX_ERR_TIMEOUT."""
+    _check(lib().abx_fmm_set_wait_limit(op._h, float(seconds), 1 if drop_one_arrive else 0),
+           "abx_fmm_set_wait_limit")
+
+
 def fmm_stats(op: Operator):
     a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
     t = C.c_double()
     _check(lib().abx_fmm_stats(op._h, C.byref(a), C.byref(b), C.byref(c), C.byref(t)), "fmm_stats")
     return {"m2l_pairs": a.value, "matrices": b.value, "leaves": c.value, "plan_s": t.value}
+
+
+def fp32_peak_tflops(ctx: Context | None = None, packed: bool = True, iters: int = 4096) -> float:
+    """Measured FP32 FMA throughput of the context's GPU in TFLOP/s
+    (``abx_probe_fp32_peak``): the compute roofline's denominator."""
+    ctx = ctx or default_context()
+    out = C.c_double()
+    _check(lib().abx_probe_fp32_peak(ctx._h, 1 if packed else 0, iters, C.byref(out)),
+           "abx_probe_fp32_peak")
+    return float(out.value)

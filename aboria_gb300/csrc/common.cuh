@@ -124,6 +124,10 @@ void ctx_release(abx_context *ctx);
 // Returns 1 if p is device-accessible memory (device or managed), 0 if it is
 // host memory (pageable or pinned).
 int is_device_ptr(const void *p);
+// 1 if p is memory that kernels on `device` may use directly (device memory
+// of that GPU, or managed memory), 0 if it is host memory, -1 if it is
+// device memory of another GPU.
+int device_ptr_usable(const void *p, int device);
 
 // A vector argument that may live on the host or the device.  For host
 // pointers a device copy is made (in) or written back (out) around the call.

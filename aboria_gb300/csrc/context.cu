@@ -48,8 +48,25 @@ int is_device_ptr(const void *p) {
   return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
 }
 
+int device_ptr_usable(const void *p, int device) {
+  if (!p) return 0;
+  cudaPointerAttributes attr;
+  cudaError_t e = cudaPointerGetAttributes(&attr, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  if (attr.type == cudaMemoryTypeManaged) return 1;
+  if (attr.type == cudaMemoryTypeDevice) return attr.device == device ? 1 : -1;
+  return 0;
+}
+
 int HostStage::in(abx_context *ctx, const void *user, size_t bytes, const void **dev) {
-  if (!user || bytes == 0 || is_device_ptr(user)) {
+  const int kind = (user && bytes) ? device_ptr_usable(user, ctx->device) : 1;
+  ABX_REQUIRE(kind >= 0, ABX_ERR_INVALID,
+              "a vector argument is device memory of another GPU than the context's (%d)",
+              ctx->device);
+  if (kind == 1) {
     *dev = user;
     return ABX_OK;
   }
@@ -61,7 +78,11 @@ int HostStage::in(abx_context *ctx, const void *user, size_t bytes, const void *
 
 int HostStage::out(abx_context *ctx, void *user, size_t bytes, void **dev) {
   host_ = false;
-  if (!user || bytes == 0 || is_device_ptr(user)) {
+  const int kind = (user && bytes) ? device_ptr_usable(user, ctx->device) : 1;
+  ABX_REQUIRE(kind >= 0, ABX_ERR_INVALID,
+              "a vector argument is device memory of another GPU than the context's (%d)",
+              ctx->device);
+  if (kind == 1) {
     *dev = user;
     return ABX_OK;
   }

@@ -84,6 +84,10 @@ struct FmmPlan {
   int nleaves = 0;
   double build_s = 0.0;
   double chebsetup_s = 0.0;
+  // tcgen05 M2L: limit of each mbarrier wait, and the test-only fault
+  // injection that withholds one operand-ready signal
+  double wait_limit_s = 1.0;
+  int drop_arrive = 0;
   DevBuf<float> W32, G32;
   ChebTab tab{};        // Clenshaw coefficients of the order
   ChebTab32 tab32{};    // the same in FP32 (mixed-precision P2M / L2P)
@@ -575,7 +579,7 @@ __global__ void __launch_bounds__(64 * WM) k_m2l_tc2(int ncheb, int ldk, int ldg
 // TMEM columns.
 constexpr int T5_KB = 8;
 constexpr int T5_PART = 128 * T5_KB * 4;  // bytes of one K operand part: 128 rows x 8 columns
-constexpr int T5_SPIN = 1 << 26;          // mbarrier polls before giving up (seconds at most)
+constexpr uint32_t T5_POLL_CAP = 1u << 30;  // second bound on the polls of one wait
 // Per row-block count: N pairs per tile, ring depth S, producer lag LAG and
 // TMEM columns.  Three or four row blocks use 64-pair tiles so that two CTAs
 // share an SM (their latencies overlap); one or two use 128-pair tiles.
@@ -643,8 +647,18 @@ __host__ __device__ constexpr uint32_t umma_idesc_tf32(int m, int n) {
          ((uint32_t)(m >> 4) << 24);
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (int it = 0; it < T5_SPIN; ++it) {
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wait for the given phase of an mbarrier for at most limit_ns nanoseconds
+// of the GPU's global timer (and at most T5_POLL_CAP polls); false if it ran
+// out.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint64_t limit_ns) {
+  uint64_t t0 = 0;
+  for (uint32_t it = 0; it < T5_POLL_CAP; ++it) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -653,6 +667,13 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
         : "r"(bar), "r"(parity)
         : "memory");
     if (ok) return true;
+    if ((it & 15u) == 0u) {
+      const uint64_t now = globaltimer_ns();
+      if (it == 0u)
+        t0 = now;
+      else if (now - t0 > limit_ns)
+        return false;
+    }
   }
   return false;
 }
@@ -672,7 +693,8 @@ __global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int nkb, int ldk, in
                                                  const int *__restrict__ tile_first,
                                                  const float *__restrict__ Wh,
                                                  const float *__restrict__ Wl,
-                                                 float *__restrict__ G32, int *__restrict__ status) {
+                                                 float *__restrict__ G32, int *__restrict__ status,
+                                                 uint64_t limit_ns, int drop_arrive) {
   using C = T5Cfg<NRB>;
   constexpr int S = C::S, LAG = C::LAG, T5_N = C::N;
   extern __shared__ __align__(128) unsigned char t5raw[];
@@ -722,7 +744,7 @@ __global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int nkb, int ldk, in
     int p = 0;
     for (; p < nkb; ++p) {
       const int st = p % S;
-      if (p >= S && !mbar_wait(smem_addr(&empty[st]), ((p - S) / S) & 1)) ok = false;
+      if (p >= S && !mbar_wait(smem_addr(&empty[st]), ((p - S) / S) & 1, limit_ns)) ok = false;
       if (!__all_sync(0xffffffffu, ok)) break;
       const uint32_t sb = smbase + (uint32_t)(st * C::STAGE);
       if (lane == 0) {
@@ -753,7 +775,9 @@ __global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int nkb, int ldk, in
         asm volatile("cp.async.wait_group %0;" ::"n"(LAG) : "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncwarp();
-        if (lane == 0)
+        // drop_arrive (fault injection for tests): block 0's W copies are
+        // never signalled, so the MMA issuer's wait runs out
+        if (lane == 0 && !(drop_arrive && p - LAG == 0))
           asm volatile("{\n\t.reg .b64 state;\n\tmbarrier.arrive.shared::cta.b64 state, [%0];\n\t}" ::"r"(
                            smem_addr(&fullB[(p - LAG) % S]))
                        : "memory");
@@ -765,7 +789,8 @@ __global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int nkb, int ldk, in
     __syncwarp();
     if (lane == 0) {
       for (int q = max(p - LAG, 0); q < p; ++q)
-        asm volatile("{\n\t.reg .b64 state;\n\tmbarrier.arrive.shared::cta.b64 state, [%0];\n\t}" ::"r"(
+        if (!(drop_arrive && q == 0))
+          asm volatile("{\n\t.reg .b64 state;\n\tmbarrier.arrive.shared::cta.b64 state, [%0];\n\t}" ::"r"(
                          smem_addr(&fullB[q % S]))
                      : "memory");
       sInfo[0] = p;
@@ -781,7 +806,8 @@ __global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int nkb, int ldk, in
     for (; c < nkb; ++c) {
       const int st = c % S;
       const uint32_t par = (c / S) & 1;
-      if (!mbar_wait(smem_addr(&fullA[st]), par) || !mbar_wait(smem_addr(&fullB[st]), par)) {
+      if (!mbar_wait(smem_addr(&fullA[st]), par, limit_ns) ||
+          !mbar_wait(smem_addr(&fullB[st]), par, limit_ns)) {
         ok = false;
         break;
       }
@@ -816,14 +842,19 @@ __global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int nkb, int ldk, in
     if (!ok) sInfo[3] = 0;
   }
   __syncthreads();
-  bool ok = mbar_wait(smem_addr(accb), 0);
-  ok = __syncthreads_and(ok && sInfo[2] && sInfo[3] && sInfo[1] == nkb);
+  const bool acc_ready = mbar_wait(smem_addr(accb), 0, limit_ns);
+  const bool ok = __syncthreads_and(acc_ready && sInfo[2] && sInfo[3] && sInfo[1] == nkb);
   if (!ok) {
     if (tid == 0) {
       atomicExch(status, 1);
-      // bulk copies still in flight land before the shared memory is released
-      for (int q = sInfo[1]; q < sInfo[0]; ++q) mbar_wait(smem_addr(&fullA[q % S]), (q / S) & 1);
+      // the MMAs issued so far (accb) and the bulk copies still in flight
+      // (fullA) complete before TMEM and shared memory are released; each of
+      // these waits is bounded as well
+      if (!acc_ready) mbar_wait(smem_addr(accb), 0, limit_ns);
+      for (int q = sInfo[1]; q < sInfo[0]; ++q)
+        mbar_wait(smem_addr(&fullA[q % S]), (q / S) & 1, limit_ns);
     }
+    __syncthreads();
   } else {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     // per warp a 16 x 32 transpose tile in the (now idle) first stage: lane
@@ -1537,7 +1568,8 @@ int fmm_matvec_device(abx_operator *op, const double *b, double *c) {
                                               (int)smem));
           kern<<<P->ntiles, 128, smem, s>>>(nc, nkb, ldk, ldg, P->Kp.ptr, P->m2l_by_mat.ptr,
                                             P->mat_off_d.ptr, P->tile_mat.ptr, P->tile_first.ptr,
-                                            P->W32.ptr, P->W32l.ptr, P->G32.ptr, status);
+                                            P->W32.ptr, P->W32l.ptr, P->G32.ptr, status,
+                                            (uint64_t)(P->wait_limit_s * 1e9), P->drop_arrive);
           return ABX_OK;
         };
         switch (nrb) {
@@ -1620,5 +1652,14 @@ extern "C" int abx_fmm_stats(abx_operator *op, int64_t *m2l_pairs, int64_t *matr
   if (matrices) *matrices = op->fmm->nmat;
   if (leaves) *leaves = op->fmm->nleaves;
   if (plan_seconds) *plan_seconds = op->fmm->build_s;
+  return ABX_OK;
+}
+
+extern "C" int abx_fmm_set_wait_limit(abx_operator *op, double seconds, int drop_one_arrive) {
+  ABX_REQUIRE(op && op->kind == 2 && op->fmm, ABX_ERR_INVALID, "not an FMM operator");
+  ABX_REQUIRE(seconds > 0.0 && seconds <= 60.0, ABX_ERR_INVALID,
+              "wait limit must be in (0, 60] seconds");
+  op->fmm->wait_limit_s = seconds;
+  op->fmm->drop_arrive = drop_one_arrive ? 1 : 0;
   return ABX_OK;
 }

@@ -312,6 +312,10 @@ struct KParams {
   FineGrid fg;
   double r, r2;
   double prune2;  // squared pruning distance (r plus a safety margin)
+  // radius-search norm: 2 euclidean, 1 manhattan, -1 chebyshev (the
+  // reference's distance_helper<2/1/-1>); thr = get_value_to_accumulate(r)
+  int lnorm;
+  double thr;
   const int *ext;  // [EXT_TAB*EXT_TAB]: max e2 gap (cells) for e0/e1 gaps, -1 pruned
   // kernel functor parameters
   int kind;
@@ -336,6 +340,7 @@ struct KParams {
   int32_t *counts;
   const int64_t *rowptr;  // for LIST: query kernel order -> output offset
   int32_t *cols_out;      // storage index of the column particle
+  double *dx_out;         // for LIST (optional): x_j - (x_i + image*L), D per pair
   const uint32_t *cperm;  // column kernel order -> storage index
   double *c;
 };
@@ -400,12 +405,55 @@ __device__ __forceinline__ double exact_d2(const D4 &xq, const D4 &xj, const int
   return acc;
 }
 
+// The reference's test in the manhattan and chebyshev norms
+// (distance_helper<1>, <-1>, src/detail/Distance.h:46-137): accum starts at 0
+// and takes |dx| over the real dimensions in order, summed (1) or as a running
+// maximum (-1); inside iff !(accum > |r|).
+__device__ __forceinline__ double exact_norm(const D4 &xq, const D4 &xj, const int *img,
+                                             const FineGrid &fg, int lnorm) {
+  if (lnorm == 2) return exact_d2(xq, xj, img, fg);
+  const double q[3] = {xq.x, xq.y, xq.z};
+  const double p[3] = {xj.x, xj.y, xj.z};
+  double acc = 0.0;
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    if (e < fg.eoff) continue;
+    const double cur = __dadd_rn(q[e], __dmul_rn((double)img[e], fg.L[e]));
+    const double a = fabs(__dsub_rn(p[e], cur));
+    if (lnorm == 1)
+      acc = __dadd_rn(acc, a);
+    else if (a > acc)
+      acc = a;
+  }
+  return acc;
+}
+
 __device__ __forceinline__ void unpack_seg(int z, int img[3], int &du0, int &du1) {
   img[0] = (z & 3) - 1;
   img[1] = ((z >> 2) & 3) - 1;
   img[2] = ((z >> 4) & 3) - 1;
   du0 = ((z >> 6) & 0xfff) - 2048;
   du1 = ((z >> 18) & 0xfff) - 2048;
+}
+
+// dx of an accepted pair as the reference's search iterator exposes it:
+// x_j - (x_i + image*L) over the real dimensions (src/Search.h:188-190, 443),
+// written as D doubles at pair slot `slot`.
+__device__ __forceinline__ void write_dx(const KParams &P, int64_t slot, const D4 &xq, int k,
+                                         int seg_z) {
+  const FineGrid &fg = P.fg;
+  int img[3], du0, du1;
+  unpack_seg(seg_z, img, du0, du1);
+  const D4 xj = P.cpos[k];
+  const double q[3] = {xq.x, xq.y, xq.z};
+  const double p[3] = {xj.x, xj.y, xj.z};
+  const int D = 3 - fg.eoff;
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    if (e < fg.eoff) continue;
+    const double cur = __dadd_rn(q[e], __dmul_rn((double)img[e], fg.L[e]));
+    P.dx_out[slot * D + (e - fg.eoff)] = __dsub_rn(p[e], cur);
+  }
 }
 
 // Per-warp shared state: the segment list of one batch of rows, its length
@@ -434,7 +482,11 @@ __device__ __forceinline__ int build_segments(const KParams &P, const int lo[3],
     const int g0c = max(max(lo[0] - u0, u0 - hi[0]) - 1, 0);
     const int g1c = max(max(lo[1] - u1, u1 - hi[1]) - 1, 0);
     int ext;
-    if (g0c < EXT_TAB && g1c < EXT_TAB) {
+    if (P.lnorm == -1) {
+      // the chebyshev ball is the whole stencil box: no euclidean pruning
+      ext = fg.K[2];
+    } else if (g0c < EXT_TAB && g1c < EXT_TAB) {
+      // euclidean pruning also serves the manhattan ball, which lies inside
       ext = P.ext[g0c * EXT_TAB + g1c];
     } else {
       const double g0 = g0c * fg.h[0], g1 = g1c * fg.h[1];
@@ -636,9 +688,18 @@ __device__ __forceinline__ void unit_box(const KParams &P, const int4 qc, bool a
 //   candidates.  Pairs with d2 <= r2lo are accepted in the branch-free loop;
 //   pairs in the rounding band (r2lo, r2hi] are re-decided afterwards with the
 //   exact FP64 test, which is rare enough to run divergently.
-template <int POL, int KIND>
+// FP32 distance of a staged pair in the search norm (2: squared euclidean,
+// 1: manhattan, -1: chebyshev), compared against the FP32 thresholds.
+template <int NORM> __device__ __forceinline__ float norm32(float d0, float d1, float d2) {
+  if (NORM == 1) return fabsf(d0) + fabsf(d1) + fabsf(d2);
+  if (NORM == -1) return fmaxf(fabsf(d0), fmaxf(fabsf(d1), fabsf(d2)));
+  return fmaf(d2, d2, fmaf(d1, d1, d0 * d0));
+}
+
+template <int POL, int KIND, int NORM = 2>
 __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 7)
     k_pairs_mixed(KParams P) {
+  static_assert(NORM == 2 || POL != POL_MATVEC, "matvecs use the euclidean distance");
   __shared__ WarpSeg seg_all[WARPS_PER_CTA];
   __shared__ WarpTile32 tile_all[WARPS_PER_CTA];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -682,9 +743,20 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 7)
     const double edx = (double)(span + 2) * hmax * 9.5367431640625e-07;
     const double band = 2.0 * 1.7320508075688772 * (P.r + edx) * edx + 3.0 * edx * edx +
                         4.0 * 5.960464477539063e-08 * P.r2 + 1e-300;
-    const float r2lo = __double2float_rd(fmax(P.r2 - band, 0.0));
-    const float r2hi = __double2float_ru(P.r2 + band);
+    // manhattan / chebyshev: each FP32 |d_e| is within edx of the exact one,
+    // the sum of three adds <= 2 roundings of a value below 3 r
+    const double nband = NORM == 1 ? 3.0 * edx + 6.0 * 5.960464477539063e-08 * 3.0 * P.r + 1e-300
+                                   : edx + 2.0 * 5.960464477539063e-08 * P.r + 1e-300;
+    // (when the band reaches below 0 nothing is accepted outright: two
+    // distinct points may share an FP32 offset, d = 0, yet lie outside a
+    // radius smaller than the band)
+    const double lo_thr = NORM == 2 ? P.r2 - band : P.thr - nband;
+    const float r2lo = lo_thr > 0.0 ? __double2float_rd(lo_thr) : -1.0f;
+    const float r2hi = NORM == 2 ? __double2float_ru(P.r2 + band) : __double2float_ru(P.thr + nband);
+    // box test: euclidean for norms 2 and 1 (the manhattan ball lies inside
+    // the euclidean one), a max-norm test for the chebyshev ball
     const float r2box = __double2float_ru((P.r2 + band) * (1.0 + 1e-6) + 1e-300);
+    const float rbox_inf = __double2float_ru((P.thr + nband) * (1.0 + 1e-6) + 1e-300);
     // band as |d2 - r2mid| <= r2half, widened by a few ulps so that the FP32
     // subtraction never shrinks it below (r2lo, r2hi]
     const float r2mid = (float)(0.5 * ((double)r2lo + (double)r2hi));
@@ -696,6 +768,10 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 7)
     int count = 0;
     int64_t out_off = 0;
     if (POL == POL_LIST && active) out_off = P.rowptr[qi];
+    if (POL == POL_LIST && P.dx_out) {
+      xq = P.qpos[qi];
+      have_xq = true;
+    }
 
     for (int row0 = 0; row0 < nrows; row0 += 32) {
       const int nseg = build_segments(P, lo, hi, a0, a1, R1, nrows, row0, ws, lane);
@@ -750,7 +826,8 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 7)
             const float e0 = fmaxf(fabsf(st.x - bc0) - bw0, 0.f);
             const float e1 = fmaxf(fabsf(st.y - bc1) - bw1, 0.f);
             const float e2 = fmaxf(fabsf(st.z - bc2) - bw2, 0.f);
-            keep = fmaf(e2, e2, fmaf(e1, e1, e0 * e0)) <= r2box;
+            keep = NORM == -1 ? fmaxf(e0, fmaxf(e1, e2)) <= rbox_inf
+                              : fmaf(e2, e2, fmaf(e1, e1, e0 * e0)) <= r2box;
             st.w = bws[sub];
           }
           const unsigned km = __ballot_sync(0xffffffffu, keep);
@@ -859,8 +936,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 7)
 #pragma unroll 4
         for (int j = 0; j < nt && POL != POL_MATVEC; ++j) {
           const float4 c = sm.p[j];
-          const float d0 = c.x - pq0, d1 = c.y - pq1, d2v = c.z - pq2;
-          const float dd = fmaf(d2v, d2v, fmaf(d1, d1, d0 * d0));
+          const float dd = norm32<NORM>(c.x - pq0, c.y - pq1, c.z - pq2);
           const bool in = dd <= r2lo;
           need |= (dd > r2lo) & (dd <= r2hi);
           if (POL == POL_MATVEC) {
@@ -868,7 +944,11 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 7)
             acc32 = fmaf(in ? w : 0.f, c.w, acc32);
           }
           if (POL == POL_COUNT) count += in ? 1 : 0;
-          if (POL == POL_LIST && in && active) P.cols_out[out_off++] = (int32_t)P.cperm[sm.meta[j].x];
+          if (POL == POL_LIST && in && active) {
+            const int2 mt = sm.meta[j];
+            if (P.dx_out) write_dx(P, out_off, xq, mt.x, ws.seg[mt.y].z);
+            P.cols_out[out_off++] = (int32_t)P.cperm[mt.x];
+          }
         }
         if (!WCUT && __any_sync(0xffffffffu, need)) {
           // rare: decide the band pairs with the reference's FP64 test
@@ -879,8 +959,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 7)
             }
             for (int j = 0; j < nt; ++j) {
               const float4 c = sm.p[j];
-              const float d0 = c.x - pq0, d1 = c.y - pq1, d2v = c.z - pq2;
-              const float dd = fmaf(d2v, d2v, fmaf(d1, d1, d0 * d0));
+              const float dd = norm32<NORM>(c.x - pq0, c.y - pq1, c.z - pq2);
               const bool wend = POL == POL_MATVEC && KIND == ABX_K_WENDLAND_C2;
               const bool flagged = wend ? fabsf(__fadd_rn(dd, -r2mid)) <= r2half
                                         : (dd > r2lo && dd <= r2hi);
@@ -888,7 +967,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 7)
                 const int2 mt = sm.meta[j];
                 int img[3], du0, du1;
                 unpack_seg(ws.seg[mt.y].z, img, du0, du1);
-                const bool inside = !(exact_d2(xq, P.cpos[mt.x], img, fg) > P.r2);
+                const bool inside = !(exact_norm(xq, P.cpos[mt.x], img, fg, NORM) > P.thr);
                 if (wend) {
                   // the packed loop added the clamped value: take it back out
                   // for pairs the FP64 test rejects
@@ -896,7 +975,10 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 7)
                 } else if (inside) {
                   if (POL == POL_MATVEC) acc32 = fmaf(kern32<KIND>(dd, P), c.w, acc32);
                   if (POL == POL_COUNT) ++count;
-                  if (POL == POL_LIST && active) P.cols_out[out_off++] = (int32_t)P.cperm[mt.x];
+                  if (POL == POL_LIST && active) {
+                    if (P.dx_out) write_dx(P, out_off, xq, mt.x, ws.seg[mt.y].z);
+                    P.cols_out[out_off++] = (int32_t)P.cperm[mt.x];
+                  }
                 }
               }
             }
@@ -914,22 +996,40 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 7)
   }
 }
 
+// Per-warp staging of the FP64 matvec: the candidates kept by the warp's
+// bounding-box test, as FP32 offsets (for the prefilter) and as FP64
+// positions shifted by their periodic image (x_j - image*L, for the kernel
+// value), with their weights and (column index, segment) for the exact test.
 struct WarpTile64 {
-  double x[32], y[32], z[32], b[32], s[32];
-  int idx[32];
-  int sg[32];
+  float4 pf[STAGE];
+  double ux[STAGE], uy[STAGE], uz[STAGE], b[STAGE], s[STAGE];
+  int2 meta[STAGE];
 };
 
-// FP64 pair kernel: the reference's arithmetic for every candidate pair.
+// FP64 sparse matvec: the reference's arithmetic for every accepted pair,
+// FP64 work only for accepted pairs.  Per staged tile of <= 64 candidates:
+//  (1) every lane classifies all candidates with the FP32 offsets into
+//      accepted (d2 <= r2lo), rejected (d2 > r2hi) and the rounding band,
+//      where the reference's exact FP64 test decides (rare); the result is a
+//      64-bit mask of this lane's neighbours among the candidates;
+//  (2) every lane walks its own mask and evaluates the FP64 distance, kernel
+//      and product for those pairs only.
+// The warp then pays FP64 issue for max over lanes of its neighbour count,
+// not for every (query, candidate) combination.  The distance for the kernel
+// value is |(x_j - image*L) - x_i|, which differs from the reference's
+// x_j - (x_i + image*L) by at most an ulp of the box length (the acceptance
+// decision itself is exact); the row sum order differs from the reference's.
 template <int POL, int KIND>
-__global__ void __launch_bounds__(WARPS_PER_CTA * 32, 8)
+__global__ void __launch_bounds__(WARPS_PER_CTA * 32, 6)
     k_pairs_fp64(KParams P) {
   __shared__ WarpSeg seg_all[WARPS_PER_CTA];
   __shared__ WarpTile64 tile_all[WARPS_PER_CTA];
+  static_assert(POL == POL_MATVEC, "the FP64 pair kernel computes matvecs only");
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   WarpSeg &ws = seg_all[wid];
   WarpTile64 &sm = tile_all[wid];
   const FineGrid &fg = P.fg;
+  const unsigned lt = (1u << lane) - 1u;
   for (;;) {
     int unit = 0;
     if (lane == 0) unit = atomicAdd(P.counter, 1);
@@ -939,69 +1039,133 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32, 8)
     const bool active = lane < U.y;
     const int qi = U.x + (active ? lane : 0);
     const int4 qc = P.qcell[qi];
+    const float4 ql = P.qloc[qi];
     int lo[3], hi[3], a0, a1, R1, nrows;
     unit_box(P, qc, active, lo, hi, a0, a1, R1, nrows);
+    const float pq0 = fmaf((float)(qc.x - lo[0]), fg.hf[0], ql.x);
+    const float pq1 = fmaf((float)(qc.y - lo[1]), fg.hf[1], ql.y);
+    const float pq2 = fmaf((float)(qc.z - lo[2]), fg.hf[2], ql.z);
+    const float bl0 = warp_min(pq0), bh0 = warp_max(pq0);
+    const float bl1 = warp_min(pq1), bh1 = warp_max(pq1);
+    const float bl2 = warp_min(pq2), bh2 = warp_max(pq2);
+    const float bc0 = 0.5f * (bl0 + bh0), bw0 = __fadd_ru(0.5f * (bh0 - bl0), 1e-6f * (fabsf(bl0) + fabsf(bh0)));
+    const float bc1 = 0.5f * (bl1 + bh1), bw1 = __fadd_ru(0.5f * (bh1 - bl1), 1e-6f * (fabsf(bl1) + fabsf(bh1)));
+    const float bc2 = 0.5f * (bl2 + bh2), bw2 = __fadd_ru(0.5f * (bh2 - bl2), 1e-6f * (fabsf(bl2) + fabsf(bh2)));
+    // rounding band of the FP32 d2 (the same bound as the mixed kernel's)
+    int span = 0;
+#pragma unroll
+    for (int e = 0; e < 3; ++e) span = max(span, hi[e] - lo[e] + 2 * fg.K[e] + 2);
+    const double hmax = fmax(fmax(fg.h[0] * (fg.eoff <= 0), fg.h[1] * (fg.eoff <= 1)), fg.h[2]);
+    const double edx = (double)(span + 2) * hmax * 9.5367431640625e-07;
+    const double band = 2.0 * 1.7320508075688772 * (P.r + edx) * edx + 3.0 * edx * edx +
+                        4.0 * 5.960464477539063e-08 * P.r2 + 1e-300;
+    const float r2lo = P.r2 - band > 0.0 ? __double2float_rd(P.r2 - band) : -1.0f;
+    const float r2hi = __double2float_ru(P.r2 + band);
+    const float r2box = __double2float_ru((P.r2 + band) * (1.0 + 1e-6) + 1e-300);
     const D4 xq = P.qpos[qi];
-    const double q[3] = {xq.x, xq.y, xq.z};
     const double si = (KIND == ABX_K_SCALAR_SUM) ? P.s_row[qi] : 0.0;
     double acc = 0.0;
-    int count = 0;
-    int64_t out_off = 0;
-    if (POL == POL_LIST && active) out_off = P.rowptr[qi];
+
     for (int row0 = 0; row0 < nrows; row0 += 32) {
       const int nseg = build_segments(P, lo, hi, a0, a1, R1, nrows, row0, ws, lane);
       if (nseg == 0) continue;
       const int total = ws.off[nseg];
-      for (int t0 = 0; t0 < total; t0 += 32) {
-        const int t = t0 + lane;
-        if (t < total) {
-          const int sidx = find_seg(ws, nseg, t);
-          const int k = ws.seg[sidx].x + (t - ws.off[sidx]);
-          const D4 p = P.cpos[k];
-          sm.x[lane] = p.x;
-          sm.y[lane] = p.y;
-          sm.z[lane] = p.z;
-          sm.b[lane] = (POL == POL_MATVEC) ? P.b64[k] : 0.0;
-          sm.s[lane] = (KIND == ABX_K_SCALAR_SUM) ? P.s_col[k] : 0.0;
-          sm.idx[lane] = k;
-          sm.sg[lane] = sidx;
+      int cur = 0;
+      for (int t0 = 0; t0 < total; t0 += STAGE) {
+        constexpr int NS = STAGE / 32;
+        int kk[NS], sx[NS];
+        float4 so[NS];
+#pragma unroll
+        for (int sub = 0; sub < NS; ++sub) {
+          const int t = t0 + sub * 32 + lane;
+          kk[sub] = -1;
+          sx[sub] = 0;
+          so[sub] = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (t < total) {
+            while (cur + 1 < nseg && ws.off[cur + 1] <= t) ++cur;
+            sx[sub] = cur;
+            kk[sub] = ws.seg[cur].x + (t - ws.off[cur]);
+            so[sub] = ws.segf[cur];
+          }
+        }
+        float4 cls[NS];
+#pragma unroll
+        for (int sub = 0; sub < NS; ++sub)
+          cls[sub] = kk[sub] >= 0 ? __ldg(&P.cloc[kk[sub]]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        int nt = 0;
+#pragma unroll
+        for (int sub = 0; sub < NS; ++sub) {
+          bool keep = false;
+          float4 st = make_float4(0.f, 0.f, 0.f, 0.f);
+          const int k = kk[sub];
+          if (k >= 0) {
+            const float4 cl = cls[sub];
+            st.x = fmaf(so[sub].x, fg.hf[0], cl.x);
+            st.y = fmaf(so[sub].y, fg.hf[1], cl.y);
+            st.z = fmaf(cl.w + so[sub].z, fg.hf[2], cl.z);
+            const float e0 = fmaxf(fabsf(st.x - bc0) - bw0, 0.f);
+            const float e1 = fmaxf(fabsf(st.y - bc1) - bw1, 0.f);
+            const float e2 = fmaxf(fabsf(st.z - bc2) - bw2, 0.f);
+            keep = fmaf(e2, e2, fmaf(e1, e1, e0 * e0)) <= r2box;
+          }
+          const unsigned km = __ballot_sync(0xffffffffu, keep);
+          if (keep) {
+            const int slot = nt + __popc(km & lt);
+            int img[3], du0, du1;
+            unpack_seg(ws.seg[sx[sub]].z, img, du0, du1);
+            const D4 pj = P.cpos[k];
+            sm.pf[slot] = st;
+            sm.ux[slot] = __dsub_rn(pj.x, (double)img[0] * fg.L[0]);
+            sm.uy[slot] = __dsub_rn(pj.y, (double)img[1] * fg.L[1]);
+            sm.uz[slot] = __dsub_rn(pj.z, (double)img[2] * fg.L[2]);
+            sm.b[slot] = P.b64[k];
+            if (KIND == ABX_K_SCALAR_SUM) sm.s[slot] = P.s_col[k];
+            sm.meta[slot] = make_int2(k, sx[sub]);
+          }
+          nt += __popc(km);
         }
         __syncwarp();
-        const int nt = min(32, total - t0);
-        int cur_seg = -1;
-        double cur[3] = {0.0, 0.0, 0.0};
-        for (int j = 0; j < nt; ++j) {
-          const int sj = sm.sg[j];
-          if (sj != cur_seg) {
-            // image point x + I*L of this segment (src/Search.h:188-190)
-            int img[3], du0, du1;
-            unpack_seg(ws.seg[sj].z, img, du0, du1);
-#pragma unroll
-            for (int e = 0; e < 3; ++e) cur[e] = __dadd_rn(q[e], __dmul_rn((double)img[e], fg.L[e]));
-            cur_seg = sj;
+        // (1) this lane's neighbours among the nt staged candidates
+        unsigned m0 = 0u, m1 = 0u, band0 = 0u, band1 = 0u;
+        if (active) {
+          for (int j = 0; j < nt; ++j) {
+            const float4 c = sm.pf[j];
+            const float d0 = c.x - pq0, d1 = c.y - pq1, d2v = c.z - pq2;
+            const float dd = fmaf(d2v, d2v, fmaf(d1, d1, d0 * d0));
+            const unsigned in = dd <= r2lo ? 1u : 0u;
+            const unsigned bd = (dd > r2lo && dd <= r2hi) ? 1u : 0u;
+            if (j < 32) {
+              m0 |= in << j;
+              band0 |= bd << j;
+            } else {
+              m1 |= in << (j - 32);
+              band1 |= bd << (j - 32);
+            }
           }
-          const double pj[3] = {sm.x[j], sm.y[j], sm.z[j]};
-          double a = 0.0;
-#pragma unroll
-          for (int e = 0; e < 3; ++e) {
-            if (e < fg.eoff) continue;
-            const double dx = __dsub_rn(pj[e], cur[e]);
-            a = __dadd_rn(a, __dmul_rn(dx, dx));
+        }
+        // rare: the reference's exact FP64 test for pairs in the band
+        while (band0 | band1) {
+          const int j = band0 ? __ffs(band0) - 1 : 32 + __ffs(band1) - 1;
+          if (j < 32) band0 &= band0 - 1u; else band1 &= band1 - 1u;
+          const int2 mt = sm.meta[j];
+          int img[3], du0, du1;
+          unpack_seg(ws.seg[mt.y].z, img, du0, du1);
+          if (!(exact_d2(xq, P.cpos[mt.x], img, fg) > P.r2)) {
+            if (j < 32) m0 |= 1u << j; else m1 |= 1u << (j - 32);
           }
-          if (!(a > P.r2) && active) {
-            if (POL == POL_MATVEC)
-              acc = __dadd_rn(acc, __dmul_rn(kern64<KIND>(a, P, si, sm.s[j]), sm.b[j]));
-            if (POL == POL_COUNT) ++count;
-            if (POL == POL_LIST) P.cols_out[out_off++] = (int32_t)P.cperm[sm.idx[j]];
-          }
+        }
+        // (2) FP64 distance, kernel and product for this lane's neighbours
+        while (m0 | m1) {
+          const int j = m0 ? __ffs(m0) - 1 : 32 + __ffs(m1) - 1;
+          if (j < 32) m0 &= m0 - 1u; else m1 &= m1 - 1u;
+          const double dx = sm.ux[j] - xq.x, dy = sm.uy[j] - xq.y, dz = sm.uz[j] - xq.z;
+          const double d2 = fma(dz, dz, fma(dy, dy, dx * dx));
+          acc = fma(kern64<KIND>(d2, P, si, sm.s[j]), sm.b[j], acc);
         }
         __syncwarp();
       }
     }
-    if (active) {
-      if (POL == POL_MATVEC) P.c[qi] = acc;
-      if (POL == POL_COUNT) P.counts[qi] = count;
-    }
+    if (active) P.c[qi] = acc;
   }
 }
 
@@ -1060,6 +1224,8 @@ KParams base_params(const PairLayout &L) {
   P.fg = L.fg;
   P.r = L.r;
   P.r2 = L.r * L.r;
+  P.lnorm = 2;
+  P.thr = P.r2;
   P.prune2 = prune_distance2(L);
   P.cloc = L.cols.loc.ptr;
   P.cpos = L.cols.posk.ptr;
@@ -1083,10 +1249,30 @@ int grid_blocks(abx_context *ctx, int nunits) {
 template <int POL, int KIND> int launch_pairs(abx_context *ctx, const KParams &P, bool mixed) {
   const int blocks = grid_blocks(ctx, P.nunits);
   ABX_CHECK_CUDA(cudaMemsetAsync(P.counter, 0, sizeof(int), ctx->stream));
-  if (mixed)
+  if (mixed) {
     k_pairs_mixed<POL, KIND><<<blocks, WARPS_PER_CTA * 32, 0, ctx->stream>>>(P);
+  } else {
+    if constexpr (POL == POL_MATVEC) {
+      k_pairs_fp64<POL, KIND><<<blocks, WARPS_PER_CTA * 32, 0, ctx->stream>>>(P);
+    } else {
+      set_error("the FP64 pair kernel computes matvecs only");
+      return ABX_ERR_INVALID;
+    }
+  }
+  ABX_CHECK_CUDA(cudaGetLastError());
+  return ABX_OK;
+}
+
+// The radius search (count or list) in the norm P.lnorm.
+template <int POL> int launch_search(abx_context *ctx, const KParams &P) {
+  const int blocks = grid_blocks(ctx, P.nunits);
+  ABX_CHECK_CUDA(cudaMemsetAsync(P.counter, 0, sizeof(int), ctx->stream));
+  if (P.lnorm == 1)
+    k_pairs_mixed<POL, ABX_K_CONST, 1><<<blocks, WARPS_PER_CTA * 32, 0, ctx->stream>>>(P);
+  else if (P.lnorm == -1)
+    k_pairs_mixed<POL, ABX_K_CONST, -1><<<blocks, WARPS_PER_CTA * 32, 0, ctx->stream>>>(P);
   else
-    k_pairs_fp64<POL, KIND><<<blocks, WARPS_PER_CTA * 32, 0, ctx->stream>>>(P);
+    k_pairs_mixed<POL, ABX_K_CONST, 2><<<blocks, WARPS_PER_CTA * 32, 0, ctx->stream>>>(P);
   ABX_CHECK_CUDA(cudaGetLastError());
   return ABX_OK;
 }
@@ -1232,11 +1418,14 @@ __global__ void k_rowptr_to_kernel(const int64_t *__restrict__ rowptr,
 
 // Radius queries for arbitrary points (C ABI helpers).
 int radius_query(abx_particles *p, int64_t nq, const double *q_host_or_dev, double r,
-                 int32_t *counts_user, int64_t *rowptr_user, int32_t *cols_user, int64_t cap) {
+                 int32_t *counts_user, int64_t *rowptr_user, int32_t *cols_user, int64_t cap,
+                 int lnorm, double *dx_user = nullptr) {
   abx_context *ctx = p->ctx;
   cudaStream_t s = ctx->stream;
   ABX_REQUIRE(p->searchable, ABX_ERR_STATE, "init_neighbour_search not called on this particle set");
   ABX_REQUIRE(r >= 0 && std::isfinite(r), ABX_ERR_INVALID, "invalid radius");
+  ABX_REQUIRE(lnorm == 2 || lnorm == 1 || lnorm == -1, ABX_ERR_INVALID,
+              "norm %d not supported (2 euclidean, 1 manhattan, -1 chebyshev)", lnorm);
   const int D = p->dim;
   const void *qd;
   ABX_TRY(p->stage_b.in(ctx, q_host_or_dev, (size_t)nq * D * sizeof(double), &qd));
@@ -1258,9 +1447,11 @@ int radius_query(abx_particles *p, int64_t nq, const double *q_host_or_dev, doub
   ABX_TRY(cnt_k.reserve(nq));
   KParams P = base_params(L);
   P.kind = ABX_K_CONST;
+  P.lnorm = lnorm;
+  P.thr = lnorm == 2 ? r * r : std::fabs(r);
   P.counts = cnt_k.ptr;
   ABX_CHECK_CUDA(cudaMemsetAsync(cnt_k.ptr, 0, nq * 4, s));
-  if (p->n > 0) ABX_TRY(launch_pairs<POL_COUNT, ABX_K_CONST>(ctx, P, true));
+  if (p->n > 0) ABX_TRY(launch_search<POL_COUNT>(ctx, P));
   if (counts_user) {
     DevBuf<int32_t> cnt;
     ABX_TRY(cnt.reserve(nq));
@@ -1291,16 +1482,23 @@ int radius_query(abx_particles *p, int64_t nq, const double *q_host_or_dev, doub
                   (long long)run);
       DevBuf<int64_t> rp, rpk;
       DevBuf<int32_t> colsd;
+      DevBuf<double> dxd;
       ABX_TRY(rp.reserve(nq));
       ABX_TRY(rpk.reserve(nq));
       ABX_TRY(colsd.reserve(run ? run : 1));
+      if (dx_user) {
+        ABX_TRY(dxd.reserve((size_t)(run ? run : 1) * D));
+        P.dx_out = dxd.ptr;
+      }
       ABX_CHECK_CUDA(cudaMemcpyAsync(rp.ptr, h.data(), nq * 8, cudaMemcpyHostToDevice, s));
       k_rowptr_to_kernel<<<ceil_div(nq, TPB), TPB, 0, s>>>(rp.ptr, L.rows->perm.ptr, nq, rpk.ptr);
       ABX_CHECK_CUDA(cudaGetLastError());
       P.rowptr = rpk.ptr;
       P.cols_out = colsd.ptr;
-      if (p->n > 0 && run > 0) ABX_TRY(launch_pairs<POL_LIST, ABX_K_CONST>(ctx, P, true));
+      if (p->n > 0 && run > 0) ABX_TRY(launch_search<POL_LIST>(ctx, P));
       ABX_CHECK_CUDA(cudaMemcpyAsync(cols_user, colsd.ptr, run * 4, cudaMemcpyDefault, s));
+      if (dx_user && run)
+        ABX_CHECK_CUDA(cudaMemcpyAsync(dx_user, dxd.ptr, (size_t)run * D * 8, cudaMemcpyDefault, s));
       ABX_CHECK_CUDA(cudaStreamSynchronize(s));
     }
   }
@@ -1450,16 +1648,33 @@ using namespace abx;
 extern "C" {
 
 int abx_radius_count(abx_particles *p, int64_t nq, const double *q, double r, int32_t *counts) {
-  ABX_REQUIRE(p && (q || nq == 0) && (counts || nq == 0), ABX_ERR_INVALID, "null argument");
-  ABX_TRY(ctx_activate(p->ctx));
-  return radius_query(p, nq, q, r, counts, nullptr, nullptr, 0);
+  return abx_radius_count_lnorm(p, nq, q, r, 2, counts);
 }
 
 int abx_radius_query_csr(abx_particles *p, int64_t nq, const double *q, double r, int64_t *rowptr,
                          int32_t *cols, int64_t cap) {
+  return abx_radius_query_csr_lnorm(p, nq, q, r, 2, rowptr, cols, cap);
+}
+
+int abx_radius_query_csr_dx(abx_particles *p, int64_t nq, const double *q, double r,
+                            int64_t *rowptr, int32_t *cols, double *dx, int64_t cap) {
   ABX_REQUIRE(p && (q || nq == 0) && rowptr, ABX_ERR_INVALID, "null argument");
   ABX_TRY(ctx_activate(p->ctx));
-  return radius_query(p, nq, q, r, nullptr, rowptr, cols, cap);
+  return radius_query(p, nq, q, r, nullptr, rowptr, cols, cap, 2, cols ? dx : nullptr);
+}
+
+int abx_radius_count_lnorm(abx_particles *p, int64_t nq, const double *q, double r, int lnorm,
+                           int32_t *counts) {
+  ABX_REQUIRE(p && (q || nq == 0) && (counts || nq == 0), ABX_ERR_INVALID, "null argument");
+  ABX_TRY(ctx_activate(p->ctx));
+  return radius_query(p, nq, q, r, counts, nullptr, nullptr, 0, lnorm);
+}
+
+int abx_radius_query_csr_lnorm(abx_particles *p, int64_t nq, const double *q, double r, int lnorm,
+                               int64_t *rowptr, int32_t *cols, int64_t cap) {
+  ABX_REQUIRE(p && (q || nq == 0) && rowptr, ABX_ERR_INVALID, "null argument");
+  ABX_TRY(ctx_activate(p->ctx));
+  return radius_query(p, nq, q, r, nullptr, rowptr, cols, cap, lnorm);
 }
 
 }  // extern "C"
@@ -1526,9 +1741,11 @@ extern "C" int abx_operator_matvec_noalloc(abx_operator *op, const double *b, do
               ABX_ERR_STATE,
               "abx_operator_matvec_noalloc: the particle sets changed since the operator was "
               "built; rebuild it (or call abx_operator_matvec once) before calling this");
-  ABX_REQUIRE((nc == 0 || is_device_ptr(b)) && (nr == 0 || is_device_ptr(c)), ABX_ERR_INVALID,
-              "abx_operator_matvec_noalloc: b and c must be device memory (host vectors "
-              "would need staging buffers)");
+  ABX_REQUIRE((nc == 0 || device_ptr_usable(b, ctx->device) == 1) &&
+                  (nr == 0 || device_ptr_usable(c, ctx->device) == 1),
+              ABX_ERR_INVALID,
+              "abx_operator_matvec_noalloc: b and c must be device memory of the context's "
+              "GPU (host vectors would need staging buffers)");
   if (nr == 0) return ABX_OK;
   const bool mixed = op->precision == ABX_PREC_MIXED && op->k.kind != ABX_K_SCALAR_SUM;
   const size_t need = align256((size_t)nc * (mixed ? sizeof(float) : sizeof(double))) +

@@ -663,4 +663,30 @@ int abx_particles_get_buckets(abx_particles *p, uint32_t *bb, uint32_t *be, uint
   return ABX_OK;
 }
 
+int abx_particles_get_view(abx_particles *p, abx_particles_view *out) {
+  ABX_REQUIRE(p && out, ABX_ERR_INVALID, "null argument");
+  ABX_REQUIRE(p->searchable, ABX_ERR_STATE, "init_neighbour_search not called");
+  ABX_TRY(ctx_activate(p->ctx));
+  ABX_CHECK_CUDA(cudaStreamSynchronize(p->ctx->stream));
+  std::memset(out, 0, sizeof(*out));
+  out->n = p->n;
+  out->dim = p->dim;
+  out->device = p->ctx->device;
+  out->pos = p->pos.ptr;
+  out->ids = p->ids.ptr;
+  out->search_kind = p->search_kind;
+  const bool cells = p->search_kind == 0;
+  out->bucket_begin = cells ? p->bucket_begin.ptr : nullptr;
+  out->bucket_end = cells ? p->bucket_end.ptr : nullptr;
+  out->ncells = cells ? p->grid.ncells : 0;
+  for (int d = 0; d < 3; ++d) {
+    out->size[d] = p->grid.size[d];
+    out->lo[d] = p->grid.lo[d];
+    out->hi[d] = p->grid.hi[d];
+    out->side[d] = p->grid.side[d];
+    out->periodic[d] = p->grid.periodic[d];
+  }
+  return ABX_OK;
+}
+
 }  // extern "C"

@@ -10,7 +10,8 @@ One step = one K*b over the whole particle set.
           host->device copy of b and the device->host copy of c inside the
           timed region (abx_operator_matvec stages them itself).
 --impl reference times the reference algorithm restated in C++ (the oracle,
-OpenMP on all host threads) on a bounded sample of rows of the same workload.
+FP64, OpenMP on all host threads) on the same workload: each step is one
+quarter of the rows, the quarters in turn, so four steps are one whole K*b.
 
 Multi-GPU: the path runs as independent replicas (one per rank); value is the
 sum of matvecs over ranks divided by the slowest rank's time.
@@ -111,17 +112,16 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
 
 
-PROFILE_SUMMARY = ROOT / "profiles" / "k_pairs_mixed_wendland_n4M.md"
+TRAFFIC_FILE = ROOT / "profiles" / "k_pairs_traffic.json"
 
 
 def profile_traffic():
     """Per-launch DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of
-    the pair kernel, from the committed ncu summary of one capture."""
-    import re
-    if not PROFILE_SUMMARY.exists():
+    the pair kernel from one ncu capture of the same workload, kept as data
+    next to the profile summaries."""
+    if not TRAFFIC_FILE.exists():
         return None
-    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", PROFILE_SUMMARY.read_text())
-    return float(m.group(1)) if m else None
+    return float(json.loads(TRAFFIC_FILE.read_text())["dram_bytes_per_launch"])
 
 
 def dist_setup(args):
@@ -207,15 +207,18 @@ def run_ours(args):
     c_dev = torch.empty_like(b_dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")
 
-    # correctness side-checks (outside the timed region)
+    # correctness side-checks (outside the timed region), and the FP64 mode
+    # (the reference's arithmetic for every pair) timed on the same workload
     counts = ab.radius_count(p, p.positions, RADIUS)
     pairs = int(counts.astype(np.int64).sum())
     K64 = ab.create_sparse_operator(p, p, RADIUS, kern, ab.PREC_FP64)
     c64 = K64.matvec(b_dev).cpu().numpy()
+    fp64_ms = _event_ms(lambda: K64.matvec(b_dev, out=c_dev, sync=False), stream, 3)
     del K64
     c32 = K.matvec(b_dev).cpu().numpy()
     mixed_err = float(np.linalg.norm(c32 - c64) / np.linalg.norm(c64))
     mixed_maxerr = float(np.max(np.abs(c32 - c64)) / np.max(np.abs(c64)))
+    fp32_peak = max(ab.fp32_peak_tflops(ctx, packed=True), ab.fp32_peak_tflops(ctx, packed=False))
 
     for _ in range(args.warmup):
         K.matvec(b_dev, out=c_dev)
@@ -258,8 +261,6 @@ def run_ours(args):
 
     peaks, peak_kind = measured_peaks()
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    sm_max = peaks.get("sm_max_mhz", 2070.0)
-    fp32_peak_tflops = 152 * 128 * 2 * sm_max * 1e6 / 1e12
     comp_bytes = N_PARTICLES * (24 + 8 + 8) + ncells * 8
     achieved_gbs = comp_bytes / (ms / 1e3) / 1e9
     achieved_tflops = pairs * FLOP_PER_PAIR / (ms / 1e3) / 1e12
@@ -281,7 +282,7 @@ def run_ours(args):
             "workload": WORKLOAD,
             "n": N_PARTICLES,
             "radius": RADIUS,
-            "precision": "FP32 kernel values, FP32 blocks of <=32 terms summed in FP64",
+            "precision": "FP32 kernel values, FP32 blocks of <=64 terms summed in FP64",
             "pairs_per_matvec": pairs,
             "mean_neighbours": pairs / N_PARTICLES,
             "l2": "flushed between timed steps (256 MB write outside the events)",
@@ -292,17 +293,23 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": "matvec/s",
                 "h2d_bytes_per_step": N_PARTICLES * 8, "d2h_bytes_per_step": N_PARTICLES * 8},
         "roofline": {
-            "bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-            "frac": achieved_gbs / hbm_peak, "peak_source": peak_kind,
-            "traffic": tr,
-            "note": "compulsory bytes N*(24+8+8)+ncells*8 per matvec; the pair kernel is "
-                    "FP32-issue bound, see compute_roofline",
-        },
-        "compute_roofline": {
-            "bound": "fp32", "achieved": achieved_tflops, "peak": fp32_peak_tflops,
-            "unit": "TFLOP/s", "frac": achieved_tflops / fp32_peak_tflops,
+            "bound": "fp32", "achieved": achieved_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
+            "frac": achieved_tflops / fp32_peak, "traffic": tr,
             "flop_per_pair": FLOP_PER_PAIR,
-            "peak_source": f"152 SM x 128 FP32 lanes x 2 x {sm_max:.0f} MHz (nominal)",
+            "peak_source": "measured in this run: FP32 FMA-chain probe (abx_probe_fp32_peak, "
+                           "best of scalar FFMA and packed FFMA2)",
+            "note": "achieved = accepted pairs x 20 FLOP / mean step time; traffic = DRAM "
+                    "read+write bytes per pair-kernel launch from one ncu capture "
+                    "(profiles/k_pairs_traffic.json)",
+        },
+        "hbm_roofline": {
+            "bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved_gbs / hbm_peak, "peak_source": peak_kind, "traffic": tr,
+            "note": "compulsory bytes N*(24+8+8)+ncells*8 per matvec; not the binding bound",
+        },
+        "fp64": {
+            "kernel": "k_pairs_fp64 (FP64 distance and kernel for every pair; the 1e-12 mode)",
+            "ms_per_matvec": fp64_ms, "value": 1e3 / fp64_ms, "unit": "matvec/s",
         },
         "accuracy": {"mixed_vs_fp64_rel_l2": mixed_err, "mixed_vs_fp64_rel_max": mixed_maxerr},
         "cell_build": cell_build,
@@ -323,7 +330,7 @@ def run_ours(args):
         out["fmm"] = fmm_section(ctx)
         out["fmm_16M"] = fmm_section(ctx, n=1 << 24, orders=(5,), steps=1)
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(pos, b_by_id, budget_s=args.cpu_seconds)
+        out["cpu_baseline"] = cpu_baseline(pos, b_by_id)
     if rank == 0:
         print(json.dumps(out))
     if world > 1:
@@ -431,7 +438,7 @@ def fmm_section(ctx, n=1 << 20, orders=(3, 5, 7), n_targets=10000, steps=3):
     the unit cube, octree leaves of 64, weights U[-1,1].  Per order: plan +
     M2L set-up time, matvec time (CUDA events, mean of ``steps``) in FP64 and
     mixed mode (3xTF32 tensor-core M2L, FP32 P2P), and the relative L2 error
-    of each against an FP64 direct sum (dense operator) on 10,000 seeded
+    of each against an FP64 direct sum (dense operators) on 10,000 seeded
     targets, with the self term K(0) b_i = 1e12 b_i removed from both."""
     import torch
     import aboria_gb300 as ab
@@ -443,9 +450,18 @@ def fmm_section(ctx, n=1 << 20, orders=(3, 5, 7), n_targets=10000, steps=3):
     b = np.random.default_rng(5051).uniform(-1, 1, n)
     tgt = np.sort(np.random.default_rng(5052).choice(n, n_targets, replace=False))
     kern = ab.Kernel.make(ab.K_LAPLACE, 1e-12)
+    # FP64 direct sum without the self term K(0) b_i = 1e12 b_i (summed in, it
+    # would round ~1e-4 off every later term): the sources other than the
+    # targets through a targets x all dense operator with b zeroed at the
+    # targets, plus the targets x targets sum with its diagonal taken out
     tp = ab.Particles(3, ctx).set(P[tgt])
+    bm = b.copy()
+    bm[tgt] = 0.0
     D = ab.create_dense_operator(tp, p, kern, ab.PREC_FP64)
-    direct = (D * b) - 1e12 * b[tgt]
+    direct = D * bm
+    del D
+    D = ab.create_dense_operator(tp, tp, kern, ab.PREC_FP64)
+    direct += D * b[tgt] - 1e12 * b[tgt]
     del D
     b_dev = torch.from_numpy(b).cuda()
     c_dev = torch.empty_like(b_dev)
@@ -506,9 +522,7 @@ def dense_section(ctx, n=65536, reps=5):
     c = torch.empty_like(b)
     out = {"workload": f"3-D N={n} uniform, dense Gaussian exp(-|dx|^2/0.1^2), {n * n:.3e} pairs"}
     res = {}
-    peaks, _ = measured_peaks()
-    sm_max = peaks.get("sm_max_mhz", 2070.0)
-    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    fp32_peak = max(ab.fp32_peak_tflops(ctx, packed=True), ab.fp32_peak_tflops(ctx, packed=False))
     for prec, name in ((ab.PREC_FP64, "fp64"), (ab.PREC_MIXED, "mixed")):
         K = ab.create_dense_operator(p, p, kern, prec)
         K.matvec(b, out=c)
@@ -599,58 +613,94 @@ def cfg4_as_specified(ctx, iters=100):
             "note": "numerically singular at eps*h = 0.045: the solve stalls far above 1e-8"}
 
 
-def cpu_baseline(pos, b_by_id, budget_s=15.0):
-    """The oracle (C++ restatement of the reference's OpenMP path) on a bounded
-    sample of rows; returns matvec/s extrapolated to all N rows."""
+def _oracle_workload(pos, b_by_id):
+    """The reference's cell list of the benchmark workload (oracle) and b in
+    its storage order."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
     t0 = time.perf_counter()
     cl = oracle.celllist_build(pos, [0, 0, 0], [1, 1, 1], [True] * 3, 10.0)
     build_s = time.perf_counter() - t0
-    b = np.ascontiguousarray(b_by_id[cl.perm])
-    rng = np.random.default_rng(5)
-    rows_done = 0
-    t_spent = 0.0
-    chunk = 2000
-    while t_spent < budget_s and rows_done < N_PARTICLES:
-        idx = rng.integers(0, cl.n, size=chunk)
-        t0 = time.perf_counter()
-        oracle.sparse_matvec(cl, cl.pos[idx], RADIUS, 2, [1.0 / RADIUS], b)
-        t_spent += time.perf_counter() - t0
-        rows_done += chunk
-        chunk = min(chunk * 2, 200000)
-    rate_rows = rows_done / t_spent
-    return {"value": rate_rows / cl.n, "unit": "matvec/s", "cores": oracle.num_threads(),
-            "kind": "port",
-            "sample": f"{rows_done} random rows of {cl.n} ({t_spent:.1f} s of FP64 row "
-                      f"evaluation in the reference's neighbour order), extrapolated to one "
-                      f"full matvec; cell-list build {build_s:.1f} s not included"}
+    return oracle, cl, np.ascontiguousarray(b_by_id[cl.perm]), build_s
+
+
+def _oracle_rows(oracle, cl, b, rows):
+    """Rows `rows` (a slice of the storage order) of K*b, FP64, the reference's
+    neighbour order, OpenMP over rows (src/Kernels.h:734-736)."""
+    return oracle.sparse_matvec(cl, cl.pos[rows], RADIUS, 2, [1.0 / RADIUS], b)
+
+
+def thread_sweep(oracle, cl, b, nrows=20000):
+    """Rows per second of the oracle matvec on a fixed random sample of rows
+    for 1, 2, 4, ... host threads up to all of them (the reference's own
+    scaling harness sweeps threads the same way, tests/speed_test.h:1006-1032)."""
+    full = oracle.num_threads()
+    rows = np.sort(np.random.default_rng(9).choice(cl.n, nrows, replace=False))
+    counts = []
+    t = 1
+    while t < full:
+        counts.append(t)
+        t *= 2
+    counts.append(full)
+    out = []
+    try:
+        for t in counts:
+            oracle.set_num_threads(t)
+            t0 = time.perf_counter()
+            _oracle_rows(oracle, cl, b, rows)
+            dt = time.perf_counter() - t0
+            out.append({"threads": t, "rows_per_s": nrows / dt, "matvec_per_s": nrows / dt / cl.n})
+    finally:
+        oracle.set_num_threads(full)
+    return out
+
+
+def cpu_baseline(pos, b_by_id):
+    """The oracle (the reference's OpenMP path restated in C++) timed on one
+    whole FP64 matvec of all N rows on every host thread, plus a thread sweep
+    on a 20,000-row sample."""
+    oracle, cl, b, build_s = _oracle_workload(pos, b_by_id)
+    t0 = time.perf_counter()
+    _oracle_rows(oracle, cl, b, slice(0, cl.n))
+    dt = time.perf_counter() - t0
+    return {"value": 1.0 / dt, "unit": "matvec/s", "cores": oracle.num_threads(), "kind": "port",
+            "sample": f"one whole FP64 matvec, all {cl.n} rows ({dt:.1f} s, the reference's "
+                      f"neighbour order and arithmetic, OpenMP over rows); the cell-list build "
+                      f"({build_s:.1f} s) is not included",
+            "thread_sweep": thread_sweep(oracle, cl, b)}
 
 
 def run_reference(args):
+    """The reference's CPU implementation of the path (the oracle port: the
+    reference's algorithm restated, FP64, OpenMP on all host threads) on the
+    same workload and metric.  One step = one quarter of the rows (1,048,576,
+    contiguous in storage order), the four quarters in turn, so every four
+    steps are one whole K*b; value = rows per second / N.  Warm-up steps run
+    1/16 of the rows each."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle
     pos, b_by_id = make_workload()
-    cl = oracle.celllist_build(pos, [0, 0, 0], [1, 1, 1], [True] * 3, 10.0)
-    b = np.ascontiguousarray(b_by_id[cl.perm])
-    rng = np.random.default_rng(6)
-    sample = 20000
-    idx = rng.integers(0, cl.n, size=sample)
-    for _ in range(args.warmup):
-        oracle.sparse_matvec(cl, cl.pos[idx[:2000]], RADIUS, 2, [1.0 / RADIUS], b)
-    times = []
-    for _ in range(args.steps):
+    oracle, cl, b, build_s = _oracle_workload(pos, b_by_id)
+    n = cl.n
+    q = n // 4
+    for w in range(args.warmup):
+        lo = (w * (n // 16)) % n
+        _oracle_rows(oracle, cl, b, slice(lo, min(lo + n // 16, n)))
+    times, rows_done = [], 0
+    for i in range(args.steps):
+        k = i % 4
+        rows = slice(k * q, n if k == 3 else (k + 1) * q)
         t0 = time.perf_counter()
-        oracle.sparse_matvec(cl, cl.pos[idx], RADIUS, 2, [1.0 / RADIUS], b)
+        _oracle_rows(oracle, cl, b, rows)
         times.append(time.perf_counter() - t0)
-    t = float(np.mean(times))
-    value = (sample / t) / cl.n
-    desc = (f"{sample} random rows of {cl.n} per step (FP64, reference neighbour order), "
-            f"extrapolated to one full matvec")
+        rows_done += rows.stop - rows.start
+    t = float(np.sum(times))
+    value = rows_done / t / n
+    desc = (f"{args.steps} steps of one quarter of the {n} rows each (contiguous in storage "
+            f"order, the four quarters in turn; {rows_done / n:.2f} whole matvecs timed, "
+            f"{t:.1f} s); FP64, the reference's neighbour order; warm-up steps of n/16 rows")
     out = {
         "impl": "reference",
         "metric": "kernel-op matvec/s (N=4M)",
@@ -659,15 +709,18 @@ def run_reference(args):
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": t * 1e3 * cl.n / sample,
+        "ms_per_step": t * 1e3 / args.steps,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "n": N_PARTICLES, "radius": RADIUS},
+        "config": {"workload": WORKLOAD, "n": N_PARTICLES, "radius": RADIUS,
+                   "step": "one quarter of the rows (K*b restricted to 1,048,576 rows)",
+                   "cell_build_s": build_s},
         "cpu_baseline": {"value": value, "unit": "matvec/s", "cores": oracle.num_threads(),
-                         "kind": "port", "sample": desc},
+                         "kind": "port", "sample": desc,
+                         "thread_sweep": thread_sweep(oracle, cl, b)},
         "e2e": {"value": value, "unit": "matvec/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -680,7 +733,6 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--matvec-only", action="store_true",
                     help="skip the RBF-solve and FMM sections (profiling runs)")

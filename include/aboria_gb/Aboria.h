@@ -13,13 +13,22 @@
  *   SchwartzPreconditioner and an Eigen-shaped GMRES         src/Preconditioners.h:1121-1537,
  *                                                            tests/rbf_interpolation.h:360-370
  *
+ * User variables.  ABORIA_VARIABLE(name, type, "name") declares a particle
+ * variable (src/Variable.h); Particles<std::tuple<name, ...>, D> stores one
+ * column per variable, reads and writes it with get<name>(particles)[i] or
+ * get<name>(particle) on a value_type, and reorders it with the positions.
+ *
  * Kernel functors.  The built-in closures of the reference's tests and
  * benchmarks are kernel descriptors (Aboria::kernels::*), evaluated by the
- * library's pair kernels.  An arbitrary __host__ __device__ functor
- * f(dx, i, j) -> double is accepted by create_sparse_operator when this header
- * is compiled by nvcc: its matvec runs a kernel instantiated in the caller's
- * translation unit over the FP64 neighbour lists of the radius search
- * (include/aboria_gb/functor_operator.cuh).
+ * library's pair kernels.  Under nvcc (include/aboria_gb/functor_operator.cuh)
+ * the operators also take the reference's closures as __host__ __device__
+ * functors: create_sparse_operator(rows, cols, r, f(dx, a, b)) and its
+ * variable-radius form create_sparse_operator(rows, cols, r(a), f(dx, a, b)),
+ * create_dense_operator(rows, cols, f(a, b)), where a and b are particle
+ * references read with get<position>/get<id>/get<variable> on the device;
+ * their matvecs are matrix-free kernels instantiated in the caller's
+ * translation unit over the library's cell list.  create_zero_operator and
+ * create_block_operator<NI, NJ> compose any of these (src/Operators.h:519-548).
  *
  * Errors.  The reference's CHECK prints the message and raises SIGTRAP
  * (src/Log.h:43-81); a non-zero abx status does the same here.  Define
@@ -33,6 +42,7 @@
 #ifndef ABORIA_GB_ABORIA_H_
 #define ABORIA_GB_ABORIA_H_
 
+#include <algorithm>
 #include <array>
 #include <csignal>
 #include <cstdint>
@@ -123,16 +133,71 @@ struct HyperOctree {};      // src/OctTree.h
 
 struct position {};  // get<position>(particles) / get<position>(particles)[i]
 struct id {};        // get<id>(particles)
+/* position_d<D> (src/Variable.h): the reference's position variable type,
+ * read and written like position. */
+template <unsigned int D> struct position_d {};
+
+/* ABORIA_VARIABLE(NAME, DATA_TYPE, NAME_STRING) (src/Variable.h): a particle
+ * variable NAME holding one DATA_TYPE per particle. */
+#define ABORIA_VARIABLE(NAME, DATA_TYPE, NAME_STRING)      \
+  struct NAME {                                            \
+    typedef DATA_TYPE value_type;                          \
+    static const char *name() { return NAME_STRING; }      \
+  };
+
+namespace detail {
+template <typename T> struct is_position : std::false_type {};
+template <> struct is_position<position> : std::true_type {};
+template <unsigned int D> struct is_position<position_d<D>> : std::true_type {};
+
+// index of T in the pack (sizeof...(Vs) if absent)
+template <typename T, typename... Vs> struct index_of;
+template <typename T> struct index_of<T> : std::integral_constant<size_t, 0> {};
+template <typename T, typename... Vs>
+struct index_of<T, T, Vs...> : std::integral_constant<size_t, 0> {};
+template <typename T, typename U, typename... Vs>
+struct index_of<T, U, Vs...> : std::integral_constant<size_t, 1 + index_of<T, Vs...>::value> {};
+}  // namespace detail
+
+/* One particle by value (Particles::value_type): position, id and the
+ * variables, read and written with get<...>(p). */
+template <unsigned int D, typename... Vars> struct ParticleValue {
+  Vector<double, D> pos;
+  int64_t id_ = -1;
+  std::tuple<typename Vars::value_type...> vars;
+};
 
 /* ----------------------------------------------------------- particles ---- */
-template <typename Variables, unsigned int D, typename Storage = void,
+/* A particle seen from a kernel: device pointers into the particle set's
+ * columns and the particle's storage index (the reference's
+ * Particles::const_reference, read with get<position>, get<id> and
+ * get<variable>).  Built by the user-functor operators
+ * (aboria_gb/functor_operator.cuh); valid inside their kernels. */
+template <unsigned int D, typename... Vars> struct ParticleRef {
+  const double *pos;  // SoA: pos[d * n + index]
+  int64_t n;
+  const int64_t *ids;
+  const void *vars[sizeof...(Vars) > 0 ? sizeof...(Vars) : 1];
+  int64_t index;
+};
+
+template <typename Variables, unsigned int D = 3, typename Storage = void,
           typename SearchMethod = CellListOrdered>
-class Particles {
+class Particles;
+
+template <typename... Vars, unsigned int D, typename Storage, typename SearchMethod>
+class Particles<std::tuple<Vars...>, D, Storage, SearchMethod> {
   static_assert(D >= 1 && D <= 3, "the GPU path supports 1 to 3 dimensions");
 
  public:
+  typedef void particles_tag;
   typedef Vector<double, D> double_d;
   typedef Vector<bool, D> bool_d;
+  typedef ParticleValue<D, Vars...> value_type;
+  typedef ParticleRef<D, Vars...> const_reference;
+  typedef ParticleRef<D, Vars...> reference;
+  typedef std::tuple<Vars...> variables_type;
+  typedef SearchMethod search_method;
   static const unsigned int dimension = D;
 
   explicit Particles(std::shared_ptr<detail::Context> ctx = detail::default_context())
@@ -146,29 +211,48 @@ class Particles {
       : Particles(std::move(ctx)) {
     pos_.assign(n, double_d());
     for (size_t i = 0; i < n; ++i) ids_.push_back(int64_t(i));
+    resize_vars(n);
     next_id_ = int64_t(n);
     dirty_ = true;
   }
 
   size_t size() const { return pos_.size(); }
 
-  /* push_back(position): appended with the next id; takes effect on the
-   * device at the next init_neighbour_search / update_positions. */
-  void push_back(const double_d &x) {
-    pos_.push_back(x);
+  /* push_back(particle) / push_back(position): appended with the next id;
+   * takes effect on the device at the next init_neighbour_search /
+   * update_positions. */
+  void push_back(const value_type &v) {
+    pos_.push_back(v.pos);
     ids_.push_back(next_id_++);
+    push_vars(v.vars, std::index_sequence_for<Vars...>());
     dirty_ = true;
+    ++version_;
+  }
+  void push_back(const double_d &x) {
+    value_type v;
+    v.pos = x;
+    push_back(v);
   }
 
-  std::vector<double_d> &positions() { dirty_ = true; return pos_; }
+  std::vector<double_d> &positions() { dirty_ = true; ++version_; return pos_; }
   const std::vector<double_d> &positions() const { return pos_; }
   const std::vector<int64_t> &ids() const { return ids_; }
+  /* the host column of variable V (get<V>(particles)) */
+  template <typename V> std::vector<typename V::value_type> &variable() {
+    ++version_;
+    return std::get<detail::index_of<V, Vars...>::value>(vars_);
+  }
+  template <typename V> const std::vector<typename V::value_type> &variable() const {
+    return std::get<detail::index_of<V, Vars...>::value>(vars_);
+  }
+  const std::tuple<std::vector<typename Vars::value_type>...> &variables() const { return vars_; }
 
   /* init_neighbour_search(low, high, periodic, n_particles_in_leaf)
    * (src/Particles.h:445-456): uploads the particles, builds the search
-   * structure of SearchMethod and reorders the storage. */
+   * structure of SearchMethod and reorders the storage, variables included. */
   void init_neighbour_search(const double_d &low, const double_d &high, const bool_d &periodic,
                              double n_particles_in_leaf = 10) {
+    const std::vector<int64_t> before = ids_;
     upload();
     int per[3] = {0, 0, 0};
     for (unsigned d = 0; d < D; ++d) per[d] = periodic[d] ? 1 : 0;
@@ -184,7 +268,7 @@ class Particles {
                                                         n_particles_in_leaf),
                     "init_neighbour_search");
     searched_ = true;
-    download();
+    download(before);
   }
 
   /* update_positions() (src/Particles.h:526-540) after the host positions
@@ -198,9 +282,10 @@ class Particles {
       detail::check(ABX_ERR_INVALID, "update_positions: particle count changed");
       return;
     }
+    const std::vector<int64_t> before = ids_;
     detail::check(abx_particles_set_positions(h_.get(), &pos_[0][0]), "set_positions");
     detail::check(abx_particles_update_positions(h_.get()), "update_positions");
-    download();
+    download(before);
   }
 
   abx_particles *handle() const { return h_.get(); }
@@ -209,8 +294,29 @@ class Particles {
   const double_d &get_min() const { return low_; }
   const double_d &get_max() const { return high_; }
   const bool_d &get_periodic() const { return periodic_; }
+  /* changes with every change of the host storage (the user-functor
+   * operators re-upload the variable columns when it moved) */
+  uint64_t version() const { return version_; }
+  /* device copies of the variable columns, owned here, filled by the
+   * user-functor operators */
+  std::shared_ptr<void> &device_cache() const { return device_cache_; }
 
  private:
+  template <size_t... I>
+  void push_vars(const std::tuple<typename Vars::value_type...> &v, std::index_sequence<I...>) {
+    int dummy[] = {0, (std::get<I>(vars_).push_back(std::get<I>(v)), 0)...};
+    (void)dummy;
+  }
+  void resize_vars(size_t n) {
+    apply_vars([n](auto &col) { col.resize(n); });
+  }
+  template <typename Fn> void apply_vars(Fn fn) {
+    apply_vars_impl(fn, std::index_sequence_for<Vars...>());
+  }
+  template <typename Fn, size_t... I> void apply_vars_impl(Fn fn, std::index_sequence<I...>) {
+    int dummy[] = {0, (fn(std::get<I>(vars_)), 0)...};
+    (void)dummy;
+  }
   void upload() {
     if (!dirty_) return;
     const int64_t n = int64_t(pos_.size());
@@ -219,7 +325,9 @@ class Particles {
                   "abx_particles_set");
     dirty_ = false;
   }
-  void download() {
+  /* positions and ids in the new storage order; the variables follow the
+   * particles through their ids (`before` = the ids in the previous order) */
+  void download(const std::vector<int64_t> &before) {
     const int64_t n = abx_particles_size(h_.get());
     pos_.resize(size_t(n));
     ids_.resize(size_t(n));
@@ -227,7 +335,23 @@ class Particles {
       detail::check(abx_particles_get_positions(h_.get(), &pos_[0][0]), "get_positions");
       detail::check(abx_particles_get_ids(h_.get(), ids_.data()), "get_ids");
     }
+    if (sizeof...(Vars) > 0) {
+      std::vector<std::pair<int64_t, size_t>> by_id(before.size());
+      for (size_t k = 0; k < before.size(); ++k) by_id[k] = {before[k], k};
+      std::sort(by_id.begin(), by_id.end());
+      std::vector<size_t> src(static_cast<size_t>(n));
+      for (size_t k = 0; k < size_t(n); ++k) {
+        auto it = std::lower_bound(by_id.begin(), by_id.end(), std::make_pair(ids_[k], size_t(0)));
+        src[k] = it->second;
+      }
+      apply_vars([&src](auto &col) {
+        typename std::decay<decltype(col)>::type out(src.size());
+        for (size_t k = 0; k < src.size(); ++k) out[k] = col[src[k]];
+        col.swap(out);
+      });
+    }
     dirty_ = false;
+    ++version_;
   }
 
   static_assert(sizeof(Vector<double, D>) == D * sizeof(double), "packed positions");
@@ -235,26 +359,83 @@ class Particles {
   std::shared_ptr<abx_particles> h_;
   std::vector<double_d> pos_;
   std::vector<int64_t> ids_;
+  std::tuple<std::vector<typename Vars::value_type>...> vars_;
   double_d low_, high_;
   bool_d periodic_;
   int64_t next_id_ = 0;
   bool dirty_ = true;
   bool searched_ = false;
+  uint64_t version_ = 0;
+  mutable std::shared_ptr<void> device_cache_;
 };
 
 namespace detail {
-template <typename Tag> struct getter;
-template <> struct getter<position> {
+template <typename Tag, typename Enable = void> struct getter {
+  template <typename P> static decltype(auto) get(P &p) { return p.template variable<Tag>(); }
+};
+template <typename Tag> struct getter<Tag, typename std::enable_if<is_position<Tag>::value>::type> {
   template <typename P> static decltype(auto) get(P &p) { return p.positions(); }
 };
 template <> struct getter<id> {
   template <typename P> static const std::vector<int64_t> &get(P &p) { return p.ids(); }
 };
+
+template <typename Tag, typename Enable = void> struct value_getter {
+  template <unsigned D, typename... V> static auto &get(ParticleValue<D, V...> &p) {
+    return std::get<index_of<Tag, V...>::value>(p.vars);
+  }
+  template <unsigned D, typename... V> static const auto &get(const ParticleValue<D, V...> &p) {
+    return std::get<index_of<Tag, V...>::value>(p.vars);
+  }
+};
+template <typename Tag>
+struct value_getter<Tag, typename std::enable_if<is_position<Tag>::value>::type> {
+  template <typename P> static auto &get(P &p) { return p.pos; }
+};
+template <> struct value_getter<id> {
+  template <typename P> static auto &get(P &p) { return p.id_; }
+};
+
+template <typename Tag, typename Enable = void> struct ref_getter {
+  template <unsigned D, typename... V>
+  ABORIA_GB_HD static typename Tag::value_type get(const ParticleRef<D, V...> &r) {
+    return static_cast<const typename Tag::value_type *>(r.vars[index_of<Tag, V...>::value])[r.index];
+  }
+};
+template <typename Tag>
+struct ref_getter<Tag, typename std::enable_if<is_position<Tag>::value>::type> {
+  template <unsigned D, typename... V>
+  ABORIA_GB_HD static Vector<double, D> get(const ParticleRef<D, V...> &r) {
+    Vector<double, D> x;
+    for (unsigned d = 0; d < D; ++d) x[d] = r.pos[d * r.n + r.index];
+    return x;
+  }
+};
+template <> struct ref_getter<id> {
+  template <unsigned D, typename... V>
+  ABORIA_GB_HD static int64_t get(const ParticleRef<D, V...> &r) { return r.ids[r.index]; }
+};
 }  // namespace detail
 
-/* get<position>(particles)[i] / get<id>(particles)[i] (src/Get.h). */
-template <typename Tag, typename P> decltype(auto) get(P &p) {
+/* get<position>(particles)[i] / get<id>(particles)[i] / get<var>(particles)[i]
+ * (src/Get.h): the host columns of a particle set. */
+template <typename Tag, typename P,
+          typename = typename std::decay<P>::type::particles_tag>
+decltype(auto) get(P &p) {
   return detail::getter<Tag>::get(p);
+}
+/* get<...>(value): a particle held by value (Particles::value_type). */
+template <typename Tag, unsigned int D, typename... V> auto &get(ParticleValue<D, V...> &p) {
+  return detail::value_getter<Tag>::get(p);
+}
+template <typename Tag, unsigned int D, typename... V>
+const auto &get(const ParticleValue<D, V...> &p) {
+  return detail::value_getter<Tag>::get(p);
+}
+/* get<...>(a) on a particle reference inside a user functor (device code). */
+template <typename Tag, unsigned int D, typename... V>
+ABORIA_GB_HD auto get(const ParticleRef<D, V...> &r) {
+  return detail::ref_getter<Tag>::get(r);
 }
 
 /* ----------------------------------------------------- radius search ---- */
@@ -267,8 +448,10 @@ template <unsigned int D> struct SearchResult {
 };
 
 /* euclidean_search(particles.get_query(), x, r) (src/Search.h:839-845): every
- * particle (and periodic image) with |x_j - x|^2 <= r^2 in FP64.  One query
- * per call; many queries belong in abx_radius_count / abx_radius_query_csr. */
+ * particle (and periodic image) with |x_j - x|^2 <= r^2 in FP64, with dx the
+ * separation x_j - (x + image*L) of the image the search accepted
+ * (src/Search.h:188-190, 443).  One query per call; many queries belong in
+ * abx_radius_count / abx_radius_query_csr. */
 template <typename P>
 std::vector<SearchResult<P::dimension>> euclidean_search(const P &particles,
                                                          const typename P::double_d &x,
@@ -282,26 +465,17 @@ std::vector<SearchResult<P::dimension>> euclidean_search(const P &particles,
   int64_t rowptr[2] = {0, 0};
   detail::check(abx_radius_query_csr(particles.handle(), 1, x.data(), r, rowptr, nullptr, 0),
                 "euclidean_search");
-  std::vector<int32_t> cols(static_cast<size_t>(rowptr[1]));
-  if (!cols.empty())
-    detail::check(abx_radius_query_csr(particles.handle(), 1, x.data(), r, rowptr, cols.data(),
-                                       rowptr[1]),
+  const size_t nnz = static_cast<size_t>(rowptr[1]);
+  std::vector<int32_t> cols(nnz);
+  std::vector<double> dx(nnz * D);
+  if (nnz)
+    detail::check(abx_radius_query_csr_dx(particles.handle(), 1, x.data(), r, rowptr, cols.data(),
+                                          dx.data(), rowptr[1]),
                   "euclidean_search");
-  // dx from the storage positions with the minimum periodic image, which is
-  // the image the search accepted whenever r is below half the domain width
-  const auto &pos = particles.positions();
-  for (int32_t j : cols) {
+  for (size_t k = 0; k < nnz; ++k) {
     SearchResult<D> s;
-    s.index = j;
-    for (unsigned d = 0; d < D; ++d) {
-      double dx = pos[size_t(j)][d] - x[d];
-      if (particles.get_periodic()[d]) {
-        const double w = particles.get_max()[d] - particles.get_min()[d];
-        while (dx > w / 2) dx -= w;
-        while (dx <= -w / 2) dx += w;
-      }
-      s.dx[d] = dx;
-    }
+    s.index = cols[k];
+    for (unsigned d = 0; d < D; ++d) s.dx[d] = dx[k * D + d];
     out.push_back(s);
   }
   return out;
@@ -406,6 +580,112 @@ Operator create_fmm_operator(const RowP &row_particles, const ColP &col_particle
   detail::check(abx_create_fmm_operator(row_particles.handle(), &kernel, int(N), &h),
                 "create_fmm_operator");
   return Operator(h);
+}
+
+/* create_zero_operator(rows, cols) (src/Operators.h:519-537): the rows x cols
+ * zero operator, a placeholder block of create_block_operator. */
+class ZeroOperator {
+ public:
+  ZeroOperator(int64_t r, int64_t c) : r_(r), c_(c) {}
+  int64_t rows() const { return r_; }
+  int64_t cols() const { return c_; }
+  void apply(const double *, double *c) const {
+    for (int64_t i = 0; i < r_; ++i) c[i] = 0.0;
+  }
+  template <typename Vec> Vec operator*(const Vec &b) const {
+    if (int64_t(b.size()) != c_) {
+      detail::check(ABX_ERR_INVALID, "K*b: size of b does not match the operator's columns");
+      return Vec();
+    }
+    Vec c(static_cast<size_t>(r_));
+    apply(b.data(), c.data());
+    return c;
+  }
+
+ private:
+  int64_t r_, c_;
+};
+
+template <typename RowP, typename ColP>
+ZeroOperator create_zero_operator(const RowP &row_particles, const ColP &col_particles) {
+  return ZeroOperator(int64_t(row_particles.size()), int64_t(col_particles.size()));
+}
+
+/* create_block_operator<NI, NJ>(K_00, K_01, ..., K_(NI-1)(NJ-1))
+ * (src/Operators.h:539-548, MatrixReplacement<NI, NJ, ...>): an NI x NJ
+ * matrix of operators given row by row; block (i, j) spans the rows of block
+ * (i, 0) and the columns of block (0, j) (start_row/start_col,
+ * src/Operators.h:219-234), and K * b sums K_ij b_j into each block row. */
+template <unsigned int NI, unsigned int NJ, typename... Ops> class BlockOperator {
+  static_assert(sizeof...(Ops) == NI * NJ, "create_block_operator<NI, NJ> takes NI*NJ operators");
+
+ public:
+  explicit BlockOperator(const Ops &...ops) : ops_(ops...) {}
+
+  int64_t rows() const {
+    int64_t n = 0;
+    for (unsigned i = 0; i < NI; ++i) n += block_rows(i);
+    return n;
+  }
+  int64_t cols() const {
+    int64_t n = 0;
+    for (unsigned j = 0; j < NJ; ++j) n += block_cols(j);
+    return n;
+  }
+
+  void apply(const double *b, double *c) const {
+    int64_t r0 = 0;
+    for (unsigned i = 0; i < NI; ++i) {
+      const int64_t nr = block_rows(i);
+      for (int64_t k = 0; k < nr; ++k) c[r0 + k] = 0.0;
+      std::vector<double> tmp(static_cast<size_t>(nr));
+      int64_t c0 = 0;
+      for (unsigned j = 0; j < NJ; ++j) {
+        for_block(i * NJ + j, [&](const auto &op) {
+          if (nr > 0) op.apply(b + c0, tmp.data());
+        });
+        for (int64_t k = 0; k < nr; ++k) c[r0 + k] += tmp[size_t(k)];
+        c0 += block_cols(j);
+      }
+      r0 += nr;
+    }
+  }
+
+  template <typename Vec> Vec operator*(const Vec &b) const {
+    if (int64_t(b.size()) != cols()) {
+      detail::check(ABX_ERR_INVALID, "K*b: size of b does not match the operator's columns");
+      return Vec();
+    }
+    Vec c(static_cast<size_t>(rows()));
+    apply(b.data(), c.data());
+    return c;
+  }
+
+ private:
+  template <typename Fn> void for_block(unsigned k, Fn fn) const {
+    for_block_impl(k, fn, std::index_sequence_for<Ops...>());
+  }
+  template <typename Fn, size_t... I>
+  void for_block_impl(unsigned k, Fn fn, std::index_sequence<I...>) const {
+    int dummy[] = {0, (I == k ? (fn(std::get<I>(ops_)), 0) : 0)...};
+    (void)dummy;
+  }
+  int64_t block_rows(unsigned i) const {
+    int64_t n = 0;
+    for_block(i * NJ, [&](const auto &op) { n = op.rows(); });
+    return n;
+  }
+  int64_t block_cols(unsigned j) const {
+    int64_t n = 0;
+    for_block(j, [&](const auto &op) { n = op.cols(); });
+    return n;
+  }
+  std::tuple<Ops...> ops_;
+};
+
+template <unsigned int NI, unsigned int NJ, typename... Ops>
+BlockOperator<NI, NJ, Ops...> create_block_operator(const Ops &...ops) {
+  return BlockOperator<NI, NJ, Ops...>(ops...);
 }
 
 /* -------------------------------------------------------------- solvers ---- */

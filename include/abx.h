@@ -9,7 +9,8 @@
  * (include/aboria_gb/Aboria.h) maps a non-zero status back to that behaviour.
  *
  * Vector arguments (positions, b, c, counts, ...) may be host memory
- * (pageable or pinned) or device memory; the library detects which
+ * (pageable or pinned) or device memory of the context's GPU (device memory
+ * of another GPU is rejected with ABX_ERR_INVALID); the library detects which
  * (cudaPointerGetAttributes) and stages host buffers through the device
  * around the call.  All work runs on the context's stream; calls that return
  * data to host memory synchronise that stream before returning.
@@ -122,6 +123,30 @@ ABX_API int abx_particles_get_grid(abx_particles *p, uint32_t *size, double *sid
 ABX_API int abx_particles_get_buckets(abx_particles *p, uint32_t *bucket_begin, uint32_t *bucket_end,
                               uint32_t *keys);
 
+/* Device view of a particle set, for kernels compiled in the caller's
+ * translation unit (the C++ header's user-functor operators): plain device
+ * pointers into the library's storage, valid until the set is next changed
+ * (set, init_neighbour_search, update_positions) or destroyed.  Positions are
+ * SoA (pos[d*n + i]); the bucket ranges and grid are the CellListOrdered ones
+ * (src/CellListOrdered.h:132-259; bucket key = sum_d v_d prod_{e>d} size_e,
+ * v_d the bucket coordinate), NULL for an octree (search_kind 1).  The
+ * reference's query object exposes the same data to its search iterators
+ * (CellListOrderedQuery, src/CellListOrdered.h:280-491). */
+typedef struct abx_particles_view {
+  int64_t n;
+  int dim;
+  int device;
+  const double *pos;
+  const int64_t *ids;
+  const uint32_t *bucket_begin, *bucket_end;
+  uint32_t ncells;
+  uint32_t size[3];
+  double lo[3], hi[3], side[3];
+  int periodic[3];
+  int search_kind;
+} abx_particles_view;
+ABX_API int abx_particles_get_view(abx_particles *p, abx_particles_view *out);
+
 /* -------------------------------------------------------- radius search --
  * euclidean_search(query, x, r) (src/Search.h:839-845) for nq query points:
  * every stored particle j (and periodic image) with
@@ -134,6 +159,21 @@ ABX_API int abx_radius_count(abx_particles *p, int64_t nq, const double *q, doub
  * rowptr[nq]); cap is the capacity of cols. */
 ABX_API int abx_radius_query_csr(abx_particles *p, int64_t nq, const double *q, double r,
                          int64_t *rowptr, int32_t *cols, int64_t cap);
+/* abx_radius_query_csr plus dx[nnz*dim]: for every neighbour the separation
+ * x_j - (x + image*L) of the periodic image the search accepted, in FP64 as
+ * the reference's search iterator computes it (src/Search.h:188-190, 443). */
+ABX_API int abx_radius_query_csr_dx(abx_particles *p, int64_t nq, const double *q, double r,
+                                    int64_t *rowptr, int32_t *cols, double *dx, int64_t cap);
+/* The same searches in another norm: manhatten_search (lnorm = 1) and
+ * chebyshev_search (lnorm = -1), src/Search.h:797-845, with the reference's
+ * FP64 test distance_helper<1/-1> (src/detail/Distance.h:46-137): accum = 0,
+ * then |dx_d| over the dimensions in order, summed (1) or as a running
+ * maximum (-1); a particle is a neighbour iff !(accum > |r|).  lnorm = 2 is
+ * euclidean_search (abx_radius_count / abx_radius_query_csr). */
+ABX_API int abx_radius_count_lnorm(abx_particles *p, int64_t nq, const double *q, double r,
+                                   int lnorm, int32_t *counts);
+ABX_API int abx_radius_query_csr_lnorm(abx_particles *p, int64_t nq, const double *q, double r,
+                                       int lnorm, int64_t *rowptr, int32_t *cols, int64_t cap);
 
 /* k nearest neighbours of every stored particle among the stored particles
  * (itself included, FP64 distances with periodic images, ties by storage
@@ -163,6 +203,16 @@ ABX_API int abx_create_fmm_operator(abx_particles *p, const abx_kernel *k, int o
                                     abx_operator **out);
 ABX_API int abx_fmm_stats(abx_operator *op, int64_t *m2l_pairs, int64_t *matrices,
                           int64_t *leaves, double *plan_seconds);
+/* Limit of every device-side wait of the tensor-core M2L (its pipeline's
+ * mbarriers), in seconds of the GPU's global timer (default 1 s, at most 60):
+ * a wait that runs out makes the matvec return ABX_ERR_TIMEOUT after the
+ * kernel has drained its copies and MMAs in flight and freed its tensor
+ * memory, so the context stays usable.  drop_one_arrive = 1 is fault
+ * injection for tests: the M2L producer withholds its first operand-ready
+ * signal, so the MMA issuer's wait runs out (a barrier nothing arrives on);
+ * 0 restores normal operation.  No counterpart in the reference, whose FMM
+ * runs on the host. */
+ABX_API int abx_fmm_set_wait_limit(abx_operator *op, double seconds, int drop_one_arrive);
 ABX_API int abx_operator_destroy(abx_operator *op);
 ABX_API int abx_operator_set_precision(abx_operator *op, int mode);
 ABX_API int64_t abx_operator_rows(const abx_operator *op);
@@ -178,7 +228,8 @@ ABX_API int abx_operator_matvec(abx_operator *op, const double *b, double *c);
  * cudaMalloc, cudaFree or allocating library routine: the per-call scratch
  * lives in one fixed 32 MiB device array inside the library, which every GPU
  * that loads the library holds until the process exits.
- *   - b and c must be device memory; host vectors are rejected (ABX_ERR_INVALID).
+ *   - b and c must be device memory of the context's GPU (or managed memory);
+ *     host vectors and other GPUs' memory are rejected (ABX_ERR_INVALID).
  *   - The scratch needed is 4 B (mixed precision) or 8 B (FP64) per column plus
  *     8 B per row, each rounded up to 256 B, plus 256 B; larger operators are
  *     rejected with ABX_ERR_CAPACITY (about 2.7M particles for a square mixed
@@ -311,6 +362,15 @@ ABX_API int abx_gmres_solve_fallback(abx_operator *A, abx_operator *A_check, abx
                                      int restart, int learned_max_iters, int max_iters,
                                      double tol, int *iterations, double *rel_residual,
                                      int *used_fallback);
+
+/* ------------------------------------------------------------ diagnostics --
+ * Measured FP32 throughput of this GPU (no counterpart in the reference): the
+ * denominator of the pair kernels' compute roofline.  8 CTAs x 256 threads per
+ * SM run independent FMA chains, `iters` steps of 8 chains per thread, scalar
+ * FFMA (packed = 0) or packed FP32x2 FFMA2 (packed = 1); best of three timed
+ * launches after a warm-up, CUDA events on the context's stream.  *tflops
+ * counts an FMA as 2 FLOP. */
+ABX_API int abx_probe_fp32_peak(abx_context *ctx, int packed, int iters, double *tflops);
 
 #ifdef __cplusplus
 }

@@ -358,7 +358,8 @@ int64_t orc_celllist_build(int D, int64_t n, double *pos_io, const double *lo,
                            int stable, double *pos_out, int64_t *perm_out,
                            uint32_t *keys_out, uint32_t *bucket_begin,
                            uint32_t *bucket_end, uint32_t ncells_cap,
-                           uint32_t *size_out, double *side_out) {
+                           uint32_t *size_out, double *side_out, int64_t prev_grid_n,
+                           int64_t *grid_n_out) {
   std::vector<uint8_t> alive(n, 1);
   for (int64_t i = 0; i < n; ++i) {
     double *r = pos_io + i * D;
@@ -378,8 +379,14 @@ int64_t orc_celllist_build(int D, int64_t n, double *pos_io, const double *lo,
   for (int64_t i = 0; i < n; ++i)
     if (alive[i]) alive_idx.push_back(i);
   const int64_t na = (int64_t)alive_idx.size();
+  // set_domain_impl recomputes the grid only when the alive count left
+  // [0.5, 2] x the count it was last computed with (src/CellListOrdered.h:
+  // 133-136); prev_grid_n <= 0 means no grid yet.
+  int64_t grid_n = na;
+  if (prev_grid_n > 0 && !(na < 0.5 * prev_grid_n || na > 2 * prev_grid_n)) grid_n = prev_grid_n;
+  *grid_n_out = grid_n;
   Grid g;
-  make_grid(g, D, lo, hi, periodic, n_leaf, na);
+  make_grid(g, D, lo, hi, periodic, n_leaf, grid_n);
   if (g.ncells > ncells_cap) return -1;
   for (int d = 0; d < D; ++d) {
     size_out[d] = g.size[d];
@@ -1034,14 +1041,19 @@ void orc_fmm(int D, int n_cheb, int64_t npts, const double *pos_in, const double
 }
 
 // Direct sum c_i = sum_j K(x_i, x_j) b_j for the targets listed in `targets`.
+// skip_self != 0 leaves out j == i: with the regularised Laplace kernel
+// 1/(|dx| + 1e-12) the self term 1e12 b_i would otherwise sit in the
+// accumulator and round away ~1e-4 of every later term.
 void orc_direct_sum(int D, int64_t npts, const double *pos, int kind, const double *params,
-                    const double *b, int64_t ntargets, const int64_t *targets, double *c) {
+                    const double *b, int64_t ntargets, const int64_t *targets, int skip_self,
+                    double *c) {
   KDesc k{kind, {params[0], params[1], params[2], params[3]}, nullptr, nullptr};
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(dynamic, 4)
   for (int64_t t = 0; t < ntargets; ++t) {
     const int64_t i = targets[t];
     double acc = 0.0;
     for (int64_t j = 0; j < npts; ++j) {
+      if (skip_self && j == i) continue;
       double dx[3];
       for (int d = 0; d < D; ++d) dx[d] = pos[j * D + d] - pos[i * D + d];
       acc += kernel_eval(k, dx, D, 0, 0) * b[j];

@@ -115,13 +115,16 @@ def point_to_bucket(size, lo, side, x):
     return int(idx), v
 
 
-def celllist_build(pos, lo, hi, periodic, n_leaf=10.0, stable=True) -> CellList:
+def celllist_build(pos, lo, hi, periodic, n_leaf=10.0, stable=True, prev_grid_n=0) -> CellList:
+    """Domain enforcement, grid, stable sort and bucket ranges.  prev_grid_n:
+    the alive count the existing grid was computed with (0: none); the grid
+    is kept while the new alive count stays within a factor 2 of it."""
     pos = np.array(pos, dtype=np.float64, order="C", copy=True)
     n, dim = pos.shape
     lo = np.ascontiguousarray(lo, np.float64)
     hi = np.ascontiguousarray(hi, np.float64)
     per = np.ascontiguousarray([1 if p else 0 for p in periodic], np.int32)
-    _, _, nc_cap = grid(dim, lo, hi, periodic, n_leaf, n)
+    _, _, nc_cap = grid(dim, lo, hi, periodic, n_leaf, max(n, prev_grid_n))
     # the grid of the alive count can only be smaller or equal in most cases;
     # retry with a larger capacity if not.
     cap = max(nc_cap, 1) * 8 + 64
@@ -134,10 +137,12 @@ def celllist_build(pos, lo, hi, periodic, n_leaf=10.0, stable=True) -> CellList:
         be = np.zeros(cap, np.uint32)
         size = np.zeros(3, np.uint32)
         side = np.zeros(3, np.float64)
+        gn = np.zeros(1, np.int64)
         na = lib().orc_celllist_build(C.c_int(dim), C.c_int64(n), _p(pos_io), _p(lo), _p(hi),
                                       _p(per), C.c_double(n_leaf), C.c_int(1 if stable else 0),
                                       _p(out_pos), _p(perm), _p(keys), _p(bb), _p(be),
-                                      C.c_uint32(cap), _p(size), _p(side))
+                                      C.c_uint32(cap), _p(size), _p(side),
+                                      C.c_int64(prev_grid_n), _p(gn))
         if na >= 0:
             break
         cap *= 8
@@ -288,7 +293,9 @@ def fmm(pos, lo, hi, n_leaf, order, kind, params, b):
     return c
 
 
-def direct_sum(pos, kind, params, b, targets):
+def direct_sum(pos, kind, params, b, targets, skip_self=False):
+    """FP64 direct sum c_t = sum_j K(x_j - x_i) b_j, i = targets[t], j in input
+    order; skip_self leaves out j == i."""
     pos = np.ascontiguousarray(pos, np.float64)
     npts, dim = pos.shape
     prm = np.zeros(4)
@@ -297,5 +304,5 @@ def direct_sum(pos, kind, params, b, targets):
     c = np.zeros(len(targets))
     lib().orc_direct_sum(C.c_int(dim), C.c_int64(npts), _p(pos), C.c_int(kind), _p(prm),
                          _p(np.ascontiguousarray(b, np.float64)), C.c_int64(len(targets)),
-                         _p(targets), _p(c))
+                         _p(targets), C.c_int(1 if skip_self else 0), _p(c))
     return c

@@ -28,22 +28,11 @@ template <typename T> static void write(const std::string &path, const std::vect
 }
 
 #ifdef __CUDACC__
-struct SumFunctor {  // get<scalar1>(a) + get<scalar2>(b) with constant scalars
-  double s1, s2;
-  __host__ __device__ double operator()(const vdouble3 &, int64_t, int64_t) const { return s1 + s2; }
-};
-struct BlockFunctor {  // the 2 x 1 block kernel (s1 + s2, s1 - s2)
-  double s1, s2;
-  __host__ __device__ Vector<double, 2> operator()(const vdouble3 &, int64_t, int64_t) const {
-    return Vector<double, 2>(s1 + s2, s1 - s2);
-  }
-};
-struct GaussianFunctor {
-  double inv_c2;
-  __host__ __device__ double operator()(const vdouble3 &dx, int64_t, int64_t) const {
-    return exp(-dx.squaredNorm() * inv_c2);
-  }
-};
+ABORIA_VARIABLE(scalar1, double, "scalar1")
+ABORIA_VARIABLE(scalar2, double, "scalar2")
+ABORIA_VARIABLE(search_radius, double, "search_radius")
+typedef Particles<std::tuple<scalar1, scalar2>> ParticlesType;  // D = 3, as the reference's default
+typedef Particles<std::tuple<search_radius>, 3> RadiusParticles;
 #endif
 
 static int run(const char *in, const std::string &out) {
@@ -99,20 +88,56 @@ static int run(const char *in, const std::string &out) {
   std::vector<double> kb = K * bs;
   write(out + "/kb.bin", kb);
 #ifdef __CUDACC__
-  auto Kf = create_sparse_operator(particles, particles, r, GaussianFunctor{1.0 / (c * c)});
-  std::vector<double> kf = Kf * bs;
-  write(out + "/kf.bin", kf);
+  {
+    // the Gaussian as a user closure f(dx, a, b), matrix-free over the cell
+    // list, against the built-in kernel: non-periodic and periodic
+    const double inv_c2 = 1.0 / (c * c);
+    auto gauss = [inv_c2] __host__ __device__(const vdouble3 &dx, Cells3::const_reference,
+                                               Cells3::const_reference) {
+      return exp(-dx.squaredNorm() * inv_c2);
+    };
+    auto Kf = create_sparse_operator(particles, particles, r, gauss);
+    write(out + "/kf.bin", Kf * bs);
+    Cells3 per;
+    for (int64_t i = 0; i < n; ++i) per.push_back(vdouble3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]));
+    per.init_neighbour_search(vdouble3(0, 0, 0), vdouble3(1, 1, 1), vbool3(true, true, true));
+    std::vector<double> bp(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i) bp[size_t(i)] = b[size_t(get<id>(per)[size_t(i)])];
+    auto Kp = create_sparse_operator(per, per, r, kernels::gaussian(c));
+    auto Kfp = create_sparse_operator(per, per, r, gauss);
+    write(out + "/kbp.bin", Kp * bp);
+    write(out + "/kfp.bin", Kfp * bp);
+  }
   {
     // tests/operators.h:810-963: three particles 0.09 apart, diameter 0.1,
-    // scalar1 = 1 and scalar2 = 2 on every particle; the scalar kernel
-    // s1_a + s2_b and the 2 x 1 block kernel (s1_a + s2_b, s1_a - s2_b)
-    Cells3 kat;
-    for (int q = 0; q < 3; ++q) kat.push_back(vdouble3(0.09 * q, 0, 0));
+    // scalar1 = 1 and scalar2 = 2 on every particle; the closure
+    // get<scalar1>(a) + get<scalar2>(b) and the 2 x 1 block closure
+    // (s1_a + s2_b, s1_a - s2_b)
+    ParticlesType kat;
+    const double diameter = 0.1;
+    ParticlesType::value_type p;
+    get<scalar1>(p) = 1.0;
+    get<scalar2>(p) = 2.0;
+    for (int q = 0; q < 3; ++q) {
+      get<position>(p) = vdouble3(diameter * 0.9 * q, 0, 0);
+      kat.push_back(p);
+    }
     kat.init_neighbour_search(vdouble3(-1, -1, -1), vdouble3(1, 1, 1), vbool3(false, false, false));
     std::vector<double> v(3);
-    for (int q = 0; q < 3; ++q) v[size_t(q)] = double(get<id>(kat)[size_t(q)] + 1);  // v = (1, 2, 3) by id
-    auto C = create_sparse_operator(kat, kat, 0.1, SumFunctor{1.0, 2.0});
-    auto C2 = create_sparse_operator(kat, kat, 0.1, BlockFunctor{1.0, 2.0});
+    for (int q = 0; q < 3; ++q) v[size_t(q)] = double(get<id>(kat)[size_t(q)] + 1);  // (1, 2, 3) by id
+    auto C = create_sparse_operator(
+        kat, kat, diameter,
+        [] __host__ __device__(const vdouble3 &, ParticlesType::const_reference a,
+                               ParticlesType::const_reference b) {
+          return get<scalar1>(a) + get<scalar2>(b);
+        });
+    auto C2 = create_sparse_operator(
+        kat, kat, diameter,
+        [] __host__ __device__(const vdouble3 &, ParticlesType::const_reference a,
+                               ParticlesType::const_reference b) {
+          return Vector<double, 2>(get<scalar1>(a) + get<scalar2>(b),
+                                   get<scalar1>(a) - get<scalar2>(b));
+        });
     std::vector<double> a1 = C * v, a2 = C2 * v;
     std::vector<double> res;  // by id: answer, then block answer, then nnz
     std::vector<double> r1(3), r2(6);
@@ -127,6 +152,72 @@ static int run(const char *in, const std::string &out) {
     res.push_back(double(C.nonzeros()));
     res.push_back(double(C2.nonzeros()));
     write(out + "/kat.bin", res);
+  }
+  {
+    // tests/operators.h:969-1090: dense closures over particle variables, a
+    // zero operator and the 2 x 2 block operator [A B; C 0]
+    ParticlesType particles3, augment;
+    const double diameter = 0.1;
+    ParticlesType::value_type p;
+    for (int q = 0; q < 3; ++q) {
+      get<position>(p) = vdouble3(diameter * 0.9 * q, 0, 0);
+      get<scalar1>(p) = q + 1;
+      get<scalar2>(p) = 0.1 * (q + 1);
+      particles3.push_back(p);
+    }
+    get<scalar1>(p) = 0;
+    get<scalar2>(p) = 0;
+    get<position>(p) = vdouble3(-diameter * 1.8, 0, 0);
+    augment.push_back(p);
+    particles3.init_neighbour_search(vdouble3(-1, -1, -1), vdouble3(1, 1, 1),
+                                     vbool3(false, false, false));
+    auto A = create_dense_operator(
+        particles3, particles3,
+        [] __host__ __device__(ParticlesType::const_reference a, ParticlesType::const_reference) {
+          return get<scalar1>(a);
+        });
+    auto B = create_dense_operator(
+        particles3, augment,
+        [] __host__ __device__(ParticlesType::const_reference a, ParticlesType::const_reference) {
+          return get<scalar2>(a);
+        });
+    auto Cd = create_dense_operator(
+        augment, particles3,
+        [] __host__ __device__(ParticlesType::const_reference, ParticlesType::const_reference b) {
+          return get<scalar2>(b);
+        });
+    auto Zero = create_zero_operator(augment, augment);
+    auto Full = create_block_operator<2, 2>(A, B, Cd, Zero);
+    std::vector<double> ones(4, 1.0);
+    std::vector<double> ans = Full * ones;
+    ans.push_back(double(Full.rows()));
+    ans.push_back(double(Full.cols()));
+    write(out + "/block_kat.bin", ans);
+  }
+  {
+    // create_sparse_operator(rows, cols, radius_function, f) with a per-row
+    // search radius held in a particle variable
+    RadiusParticles rp;
+    RadiusParticles::value_type p;
+    for (int64_t i = 0; i < n; ++i) {
+      get<position>(p) = vdouble3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+      get<search_radius>(p) = 0.02 + 0.06 * b[size_t(i)] * b[size_t(i)] / (1.0 + b[size_t(i)] * b[size_t(i)]);
+      rp.push_back(p);
+    }
+    rp.init_neighbour_search(vdouble3(0, 0, 0), vdouble3(1, 1, 1), vbool3(false, false, false));
+    const double inv_c2 = 1.0 / (c * c);
+    auto Kv = create_sparse_operator(
+        rp, rp,
+        [] __host__ __device__(RadiusParticles::const_reference a) { return get<search_radius>(a); },
+        [inv_c2] __host__ __device__(const vdouble3 &dx, RadiusParticles::const_reference,
+                                     RadiusParticles::const_reference) {
+          return exp(-dx.squaredNorm() * inv_c2);
+        });
+    std::vector<double> bv(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i) bv[size_t(i)] = b[size_t(get<id>(rp)[size_t(i)])];
+    write(out + "/kv.bin", Kv * bv);
+    write(out + "/kv_radius.bin", get<search_radius>(rp));
+    write(out + "/kv_ids.bin", get<id>(rp));
   }
 #endif
 

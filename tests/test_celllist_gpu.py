@@ -85,3 +85,35 @@ def test_rebuild_after_moving_particles():
     cl = oracle.celllist_build(moved, [0] * 3, [1] * 3, [True] * 3)
     assert np.array_equal(p.ids, ids_before[cl.perm])
     assert np.array_equal(p.positions, cl.pos)
+
+
+@pytest.mark.parametrize("frac_deleted,keeps_grid", [(0.3, True), (0.6, False)])
+def test_grid_hysteresis_after_deletion(frac_deleted, keeps_grid):
+    """set_domain_impl recomputes the grid only when the alive count leaves
+    [0.5, 2] x the count it was computed with (src/CellListOrdered.h:133-136):
+    deleting 30% keeps the old grid, deleting 60% recomputes it.  The rebuilt
+    order, keys and buckets must equal the oracle's with the same rule."""
+    n = 100000
+    pos = workloads.uniform(n, 3, seed=8)
+    p = ab.Particles(3).set(pos)
+    p.init_neighbour_search([0] * 3, [1] * 3, [False] * 3)
+    size0 = p.grid()[0].copy()
+    ids_before = p.ids
+    moved = p.positions
+    kill = np.random.default_rng(9).random(n) < frac_deleted
+    moved[kill] = 2.0  # outside the non-periodic domain: deleted
+    p.set_positions(moved)
+    p.update_positions()
+    cl = oracle.celllist_build(moved, [0] * 3, [1] * 3, [False] * 3, prev_grid_n=n)
+    size, side, _ = p.grid()
+    assert list(size) == list(cl.size)
+    assert np.array_equal(side, cl.side)
+    assert np.array_equal(size, size0) == keeps_grid
+    assert len(p) == cl.n == n - int(kill.sum())
+    assert np.array_equal(p.ids, ids_before[cl.perm])
+    assert np.array_equal(p.positions, cl.pos)
+    bb, be, keys = p.buckets()
+    assert np.array_equal(keys, cl.keys)
+    assert np.array_equal(bb, cl.begin) and np.array_equal(be, cl.end)
+    counts = ab.radius_count(p, p.positions, 0.05)
+    assert np.array_equal(counts, oracle.radius_count(cl, cl.pos, 0.05))

@@ -58,7 +58,8 @@ def test_cpp_api_parity(tmp_path):
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     _lib.load_library()
     exe = tmp_path / "api_test_cu"
-    subprocess.run([nvcc, "-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a",
+    subprocess.run([nvcc, "-std=c++17", "-O2", "--extended-lambda",
+                    "-gencode", "arch=compute_103a,code=sm_103a",
                     "-I", str(ROOT / "include"), str(SRC), "-L", str(LIBDIR), "-labx",
                     "-Xlinker", f"-rpath={LIBDIR}", "-o", str(exe)], check=True)
     n, nq, r, rw = 20000, 300, 0.08, 0.1
@@ -97,6 +98,30 @@ def test_cpp_api_parity(tmp_path):
     assert np.max(np.abs(kb - ref)) <= 1e-12 * np.max(np.abs(ref))
     kf = np.fromfile(out / "kf.bin", np.float64)
     assert np.max(np.abs(kf - ref)) <= 1e-12 * np.max(np.abs(ref))
+    # the closure on a periodic set (dx of the accepted image) against the
+    # built-in kernel
+    kbp = np.fromfile(out / "kbp.bin", np.float64)
+    kfp = np.fromfile(out / "kfp.bin", np.float64)
+    assert np.max(np.abs(kfp - kbp)) <= 1e-12 * np.max(np.abs(kbp))
+    # the variable-radius operator against a brute force (non-periodic)
+    kv = np.fromfile(out / "kv.bin", np.float64)
+    rad = np.fromfile(out / "kv_radius.bin", np.float64)
+    vid = np.fromfile(out / "kv_ids.bin", np.int64)
+    P, bv = pos[vid], b[vid]
+    want = np.empty(n)
+    for i in range(n):
+        dx = P - P[i]
+        d2 = (dx[:, 0] * dx[:, 0] + dx[:, 1] * dx[:, 1]) + dx[:, 2] * dx[:, 2]
+        m = ~(d2 > rad[i] * rad[i])
+        want[i] = np.sum(np.exp(-d2[m] / (r / 2) ** 2) * bv[m])
+    assert np.max(np.abs(kv - want)) <= 1e-12 * np.max(np.abs(want))
+    assert len(np.unique(np.round(rad, 6))) > 100  # the radius does vary
+    # the reference's block operator known answer (tests/operators.h:969-1090)
+    bk = np.fromfile(out / "block_kat.bin", np.float64)
+    want_block = json.loads((ROOT / "tests" / "golden" / "reference_kats.json").read_text())[
+        "block_operator"]["answer"]
+    assert np.all(np.abs(bk[:4] - want_block) <= np.finfo(float).eps), bk
+    assert bk[4] == 4 and bk[5] == 4
 
     # the reference's sparse and block operator known answers, with the
     # user-functor path (tests/operators.h:810-963)

@@ -87,3 +87,26 @@ def test_mixed_m2l_matches_fp64_for_every_row_block_count(order):
     assert ab.fmm_stats(K)["m2l_pairs"] > 0
     err = np.linalg.norm(c32 - c64) / np.linalg.norm(c64)
     assert err < 1e-5, err
+
+
+def test_m2l_wait_timeout_is_reported_and_the_context_survives():
+    """The tensor-core M2L bounds every mbarrier wait by the GPU's global
+    timer.  With one operand-ready signal withheld (a barrier nothing arrives
+    on) the MMA issuer's wait runs out: the matvec must return ABX_ERR_TIMEOUT
+    after the kernel drained its copies and freed its tensor memory, and the
+    next matvec on the same context must be correct."""
+    n = 30000
+    pos = workloads.uniform(n, 3, seed=170)
+    p = octree(pos, 64)
+    b = np.random.default_rng(171).uniform(-1, 1, n)
+    K = ab.create_fmm_operator(p, ab.Kernel.make(ab.K_LAPLACE, 1e-12), 5)
+    c64 = K * b - 1e12 * b
+    K.set_precision(ab.PREC_MIXED)
+    ab.fmm_set_wait_limit(K, 0.02, drop_one_arrive=True)
+    with pytest.raises(ab.ABXError) as exc:
+        K * b
+    assert exc.value.status == 5  # ABX_ERR_TIMEOUT
+    ab.fmm_set_wait_limit(K, 1.0, drop_one_arrive=False)
+    for _ in range(2):
+        c32 = K * b - 1e12 * b
+        assert np.linalg.norm(c32 - c64) / np.linalg.norm(c64) < 1e-5

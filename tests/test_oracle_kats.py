@@ -150,6 +150,19 @@ def test_grid_matches_reference_formula():
     assert list(size) == [74, 74, 74] and nc == 405224
 
 
+def test_grid_hysteresis_rule():
+    """The grid is kept while the alive count stays within [0.5, 2] x the count
+    it was computed with (src/CellListOrdered.h:133-136)."""
+    pos = workloads.uniform(1000, 3, seed=61)
+    fresh = oracle.celllist_build(pos, [0] * 3, [1] * 3, [False] * 3, 10.0)
+    assert list(fresh.size) == [4, 4, 4]
+    kept = oracle.celllist_build(pos, [0] * 3, [1] * 3, [False] * 3, 10.0, prev_grid_n=1900)
+    assert list(kept.size) == list(oracle.grid(3, [0] * 3, [1] * 3, [False] * 3, 10.0, 1900)[0])
+    assert list(kept.size) != list(fresh.size)
+    again = oracle.celllist_build(pos, [0] * 3, [1] * 3, [False] * 3, 10.0, prev_grid_n=2100)
+    assert list(again.size) == list(fresh.size)  # 1000 < 0.5 x 2100: recomputed
+
+
 def test_periodic_wrap_and_deletion():
     pos = np.array([[1.25, 0.5], [-0.25, 0.5], [0.5, 0.5], [0.5, np.nan]])
     cl = oracle.celllist_build(pos, [0, 0], [1, 1], [True, True], 1.0)

@@ -48,8 +48,8 @@ def test_single_rank_is_identity():
 
 
 def test_bench_reads_the_committed_profile_traffic():
-    """The bench's roofline `traffic` comes from the committed ncu summary of
-    the pair kernel; it must parse to a per-launch byte count no smaller than
-    the compulsory bytes of the workload (N x 40 B)."""
+    """The bench's roofline `traffic` comes from the committed data file of one
+    ncu capture of the pair kernel; it must parse to a per-launch byte count no
+    smaller than the compulsory bytes of the workload (N x 40 B)."""
     t = bench.profile_traffic()
     assert t is not None and t >= bench.N_PARTICLES * 40

@@ -116,3 +116,22 @@ def test_empty_queries_and_zero_radius():
     assert ab.radius_count(p, np.zeros((0, 3)), 0.1).shape == (0,)
     counts = ab.radius_count(p, p.positions, 0.0)
     assert np.all(counts == 1)
+
+
+@pytest.mark.parametrize("dim,r", [(3, 0.07), (2, 0.45)])
+def test_dx_of_the_accepted_image(dim, r):
+    """dx = x_j - (x + image*L) for the periodic image the search accepted,
+    bit-exact against the oracle's search iterator (src/Search.h:188-190,
+    443); at r = 0.45 in 2-D a particle is often reached through two images,
+    each with its own dx."""
+    pos = workloads.uniform(4000 if dim == 3 else 600, dim, seed=18)
+    p, cl = build(pos, [0] * dim, [1] * dim, [True] * dim, 5.0)
+    q = workloads.uniform(300, dim, lo=-0.1, hi=1.1, seed=19)
+    rowptr, cols, dx = ab.radius_query_csr(p, q, r, with_dx=True)
+    orp, ocols, odx = oracle.radius_lists(cl, q, r, with_dx=True)
+    assert np.array_equal(rowptr, orp)
+    for i in range(len(q)):
+        s = slice(rowptr[i], rowptr[i + 1])
+        a = sorted(zip(cols[s].tolist(), map(tuple, dx[s].tolist())))
+        b = sorted(zip(ocols[s].tolist(), map(tuple, odx[s].tolist())))
+        assert a == b, i

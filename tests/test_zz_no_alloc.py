@@ -18,7 +18,7 @@ import workloads
 pytestmark = pytest.mark.gpu
 FP64_TOL = 1e-12
 MIXED_TOL = 2e-6
-ABX_ERR_INVALID, ABX_ERR_CAPACITY = 1, 6
+ABX_ERR_INVALID, ABX_ERR_STATE, ABX_ERR_CAPACITY = 1, 4, 6
 
 
 def _noalloc(K, b_dev, c_dev):
@@ -66,7 +66,7 @@ def test_noalloc_rejects_host_vectors_and_oversize():
                                                 C.c_void_p(ch.ctypes.data))
     assert st == ABX_ERR_INVALID
     assert b"device memory" in _lib.lib().abx_last_error()
-    # 3M particles need 36 MB of scratch in FP64 mode (> 32 MiB)
+    # 3M particles need 8 + 8 B each, 48 MB of scratch, in FP64 mode (> 32 MiB)
     big = ab.Particles(3).set(workloads.uniform(3_000_000, 3, seed=44))
     big.init_neighbour_search([0] * 3, [1] * 3, [False] * 3)
     Kb = ab.create_sparse_operator(big, big, 0.005, ab.Kernel.make(ab.K_CONST, 1.0))
@@ -74,3 +74,22 @@ def test_noalloc_rejects_host_vectors_and_oversize():
     cb = torch.empty_like(bb)
     assert _noalloc(Kb, bb, cb) == ABX_ERR_CAPACITY
     assert b"scratch" in _lib.lib().abx_last_error()
+
+
+def test_noalloc_refuses_a_stale_layout_until_rebuilt():
+    """After the particle set is searched again the operator's layout is stale;
+    rebuilding it would allocate, so the entry point refuses (ABX_ERR_STATE)
+    until a regular matvec has rebuilt it."""
+    torch, p, b = _setup(n=60000, seed=45)
+    r = 0.04
+    K = ab.create_sparse_operator(p, p, r, ab.Kernel.make(ab.K_WENDLAND_C2, 1 / r), ab.PREC_FP64)
+    ref = K.matvec(b).cpu().numpy()
+    c = torch.empty_like(b)
+    assert _noalloc(K, b, c) == 0
+    p.init_neighbour_search([0] * 3, [1] * 3, [True] * 3)
+    assert _noalloc(K, b, c) == ABX_ERR_STATE
+    assert b"changed" in _lib.lib().abx_last_error()
+    K.matvec(b)
+    assert _noalloc(K, b, c) == 0
+    K.rows.ctx.synchronize()
+    assert np.linalg.norm(c.cpu().numpy() - ref) / np.linalg.norm(ref) < FP64_TOL
