@@ -66,6 +66,14 @@ struct abx_particles {
   abx::OctTree tree;
   uint64_t version = 0;  // bumped by every rebuild; operators check it
   abx::HostStage stage_a, stage_b;
+  // cell-list build (celllist.cu): per-dimension cell boundaries of the
+  // grid they were computed for, look-back status words, pass epoch
+  abx::DevBuf<uint64_t> cl_bnd;
+  size_t cl_bnd_off[3] = {0, 0, 0};
+  abx::GridDesc cl_bnd_grid{};
+  bool cl_bnd_valid = false;
+  abx::DevBuf<unsigned long long> cl_status;
+  uint32_t cl_epoch = 0;
 };
 
 namespace abx {
@@ -109,6 +117,8 @@ namespace abx {
 void particles_retain(abx_particles *p);
 void particles_release(abx_particles *p);
 int particles_grid_desc(const abx_particles *p, GridDesc *g);
+// celllist.cu: the CellListOrdered build of the alive particles (n > 0)
+int celllist_build(abx_particles *p);
 // pairs.cu
 int pair_layout_build(abx_operator *op);
 void pair_layout_free(PairLayout *L);

@@ -173,12 +173,16 @@ __global__ void k_iota64(int64_t *ids, int64_t n, int64_t start) {
   if (i < n) ids[i] = start + i;
 }
 
-// set_domain_impl (src/CellListOrdered.h:132-186), host side.  Returns true if
-// the grid was recomputed.
-bool set_domain_impl(abx_particles *p, size_t n) {
-  GridDesc &g = p->grid;
-  if (!(n < 0.5 * p->size_calculated_with_n || n > 2 * p->size_calculated_with_n)) return false;
-  p->size_calculated_with_n = n;
+}  // namespace
+
+// set_domain_impl (src/CellListOrdered.h:132-186) as a function: the grid
+// that alive count n leaves (recomputed only when n left [0.5, 2] x the count
+// the current grid was computed with) and the count it then records.
+GridDesc grid_for_count(const abx_particles *p, size_t n, size_t *calc_n) {
+  GridDesc g = p->grid;
+  *calc_n = p->size_calculated_with_n;
+  if (!(n < 0.5 * p->size_calculated_with_n || n > 2 * p->size_calculated_with_n)) return g;
+  *calc_n = n;
   const int D = p->dim;
   if (p->n_leaf > (double)n) {
     for (int d = 0; d < D; ++d) g.size[d] = 1;
@@ -206,7 +210,20 @@ bool set_domain_impl(abx_particles *p, size_t n) {
     g.inv_side[d] = 1.0;
     g.periodic[d] = 0;
   }
-  return true;
+  return g;
+}
+
+namespace {
+
+// set_domain_impl applied to the particle set.  Returns true if the grid was
+// recomputed.
+bool set_domain_impl(abx_particles *p, size_t n) {
+  const size_t before = p->size_calculated_with_n;
+  const bool recompute = n < 0.5 * before || n > 2 * before;
+  size_t calc = 0;
+  p->grid = grid_for_count(p, n, &calc);
+  p->size_calculated_with_n = calc;
+  return recompute;
 }
 
 // HyperOctree::build_tree (src/OctTree.h:328-475) on the sorted tags.
@@ -272,6 +289,12 @@ int update_positions(abx_particles *p) {
   }
   ABX_REQUIRE(n < (int64_t)0xFFFFFFFFll, ABX_ERR_INVALID, "too many particles (%lld)",
               (long long)n);
+  if (p->search_kind == 0) {
+    ABX_TRY(celllist_build(p));
+    p->searchable = true;
+    return ABX_OK;
+  }
+  // HyperOctree:
   // scratch: alive(n) scan(n) idx(n) keys(n) vals(n) keys_alt(n) vals_alt(n) temp
   size_t off = 0;
   carve_size<uint32_t>(off, n);
