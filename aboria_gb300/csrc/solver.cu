@@ -629,6 +629,13 @@ int gmres_solve(abx_operator *A, abx_operator *Acheck, abx_precond *M, const dou
   std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), hcol(m + 2), h2(m + 2), y(m);
   int total = 0, restarts = 0;
   double rel = 1.0;
+  // refinement (a less accurate Krylov operator than A_check): the inner
+  // cycle's target relative to the current true residual.  It starts at 1e-5;
+  // after each cycle it follows half the contraction that cycle achieved on
+  // the checked residual -- iterating the inner system far below what the
+  // operator difference lets the outer residual gain is wasted work.
+  const bool refining = Acheck != A && Acheck->precision != A->precision;
+  double inner_ratio = 1e-5, prev_beta = -1.0;
   for (;;) {
     // true residual with the checking operator
     ABX_TRY(sparse_or_dense_matvec(Acheck, x, W.tmp.ptr));
@@ -641,16 +648,18 @@ int gmres_solve(abx_operator *A, abx_operator *Acheck, abx_precond *M, const dou
       return ABX_ERR_NUMERIC;
     }
     if (rel <= tol || total >= max_iters) break;
+    if (refining && prev_beta > 0.0)
+      inner_ratio = std::min(0.5, std::max(1e-5, 0.5 * beta / prev_beta));
+    prev_beta = beta;
     k_scale<<<nb, TPB, 0, s>>>(n, 1.0 / beta, W.r.ptr, W.V.ptr);
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
     int j = 0;
     // inner tolerance: when the Krylov operator is less accurate than the
-    // checking operator (mixed precision), its Arnoldi estimate cannot go far
-    // below that accuracy, so each cycle only reduces the residual by 1e-5 and
-    // the restart (a refinement step against A_check) does the rest.
-    const bool refining = Acheck != A && Acheck->precision != A->precision;
-    const double target = std::max(tol * bnorm, refining ? 1e-5 * beta : 0.0);
+    // checking operator (mixed precision), each cycle only reduces the
+    // residual by inner_ratio and the restart (a refinement step against
+    // A_check) does the rest.
+    const double target = std::max(tol * bnorm, refining ? inner_ratio * beta : 0.0);
     for (; j < m && total < max_iters; ++j, ++total) {
       double *vj = W.V.ptr + (size_t)j * n;
       double *zj = W.Z.ptr + (size_t)j * n;
