@@ -42,9 +42,13 @@ namespace abx {
 namespace {
 
 constexpr int CL_TPB = 256;
-constexpr int CL_WARPS = CL_TPB / 32;
 constexpr int CL_ITEMS = 16;
-constexpr int CL_TILE = CL_TPB * CL_ITEMS;  // 4096 particles per tile
+constexpr int CL_TILE = 16384;                         // keys per sort tile
+constexpr int SW_TPB = 512;                            // sort-pass threads per block
+constexpr int SW_WARPS = SW_TPB / 32;
+constexpr int SW_ROUNDS = CL_TILE / (SW_TPB * CL_ITEMS);  // rounds of 16 keys per thread
+constexpr int CL_BND_SMEM = 4096;  // boundary entries staged in shared memory (32 KB)
+constexpr int CL_KEYS_TILE = 4096;                     // particles per keys-kernel step
 constexpr int CL_RB = 10;
 constexpr int CL_RADIX = 1 << CL_RB;
 constexpr int CL_MAX_PASSES = 4;
@@ -52,11 +56,17 @@ constexpr uint32_t CL_SPIN_CAP = 1u << 26;   // look-back polls before giving up
 constexpr int CL_WRAP_CAP = 1 << 20;         // periodic wrap steps before giving up
 constexpr uint64_t ST_AGG = 1ull << 32, ST_INCL = 2ull << 32;
 
+constexpr int CL_HIST_COPIES = 32;  // spread of the keys kernel's histogram atomics
+
 struct ClHeader {
   uint32_t hist[CL_MAX_PASSES][CL_RADIX];
   uint32_t tile_counter[CL_MAX_PASSES];
   uint32_t dead;
   uint32_t error;  // 1: a look-back wait gave up; 2: a periodic wrap did not end
+  uint32_t blocks_done;
+  // per-block histograms land in one of CL_HIST_COPIES copies (few blocks
+  // share a counter), the last block to finish sums them into hist
+  uint32_t part[CL_HIST_COPIES][CL_MAX_PASSES][CL_RADIX];
 };
 
 struct ClParams {
@@ -65,8 +75,11 @@ struct ClParams {
   double lo[3], hi[3], inv[3];
   int periodic[3];
   uint64_t olo[3], ohi[3];  // order-preserving bit patterns of lo, hi
-  float lo_f[3], inv_f[3];  // FP32 estimate of the bucket coordinate
+  float inv_f[3], c_f[3];   // FP32 estimate of the bucket coordinate: x * inv_f + c_f
+  float lo_fast[3], hi_fast[3], delta_f[3];  // FP32 fast-path bounds
   const uint64_t *bnd[3];   // size+2 boundaries per dimension (ordered bits)
+  const uint64_t *bnd_all;  // all of them, dimension after dimension
+  int bnd_off[3], bnd_total;
   uint32_t dead_key;
 };
 
@@ -93,94 +106,140 @@ __device__ __forceinline__ float approx_f32(uint64_t u) {
 
 // Bucket coordinate of an in-domain coordinate: FP32 estimate, then the exact
 // boundary comparisons (bnd[0] = 0, bnd[v] = ord(b_v), bnd[size+1] = max).
-__device__ __forceinline__ uint32_t cell_coord(uint64_t u, int d, const ClParams &P) {
+__device__ __forceinline__ uint32_t cell_coord(uint64_t u, int d, const ClParams &P,
+                                               const uint64_t *b) {
   const uint64_t o = ord_bits(u);
   const int sz = (int)P.size[d];
-  float t = floorf((approx_f32(u) - P.lo_f[d]) * P.inv_f[d]);
+  float t = floorf(fmaf(approx_f32(u), P.inv_f[d], P.c_f[d]));
   int v = t < 0.f ? 0 : (t > (float)sz ? sz : (int)t);
-  const uint64_t *b = P.bnd[d];
-  for (int it = 0; it <= sz && v < sz && o >= __ldg(&b[v + 1]); ++it) ++v;
-  for (int it = 0; it <= sz && v > 0 && o < __ldg(&b[v]); ++it) --v;
+  for (int it = 0; it <= sz && v < sz && o >= b[v + 1]; ++it) ++v;
+  for (int it = 0; it <= sz && v > 0 && o < b[v]; ++it) --v;
   return (uint32_t)v;
 }
 
+template <int DIM>
 __global__ void __launch_bounds__(CL_TPB) k_cl_keys(double *__restrict__ pos, int64_t n, ClParams P,
                                                     uint32_t *__restrict__ keys,
                                                     uint32_t *__restrict__ vals,
                                                     ClHeader *__restrict__ H) {
   __shared__ uint32_t h[CL_MAX_PASSES][CL_RADIX];
   __shared__ uint32_t sdead;
+  extern __shared__ uint64_t sbnd[];  // the boundary tables when they fit
   for (int i = threadIdx.x; i < P.npasses * CL_RADIX; i += CL_TPB) (&h[0][0])[i] = 0;
   if (threadIdx.x == 0) sdead = 0;
+  const bool shared_tab = P.bnd_total <= CL_BND_SMEM;
+  if (shared_tab)
+    for (int i = threadIdx.x; i < P.bnd_total; i += CL_TPB) sbnd[i] = P.bnd_all[i];
   __syncthreads();
+  const uint64_t *tab = shared_tab ? sbnd : P.bnd_all;
   uint32_t dead = 0, err = 0;
-  const int64_t base = (int64_t)blockIdx.x * CL_TILE;
-#pragma unroll 4
-  for (int it = 0; it < CL_ITEMS; ++it) {
-    const int64_t i = base + (int64_t)it * CL_TPB + threadIdx.x;
-    if (i >= n) break;
-    bool alive = true;
-    uint32_t v[3] = {0, 0, 0};
-    for (int d = 0; d < P.dim; ++d) {
-      double r = pos[(int64_t)d * n + i];
-      uint64_t u = (uint64_t)__double_as_longlong(r);
-      if (((u >> 52) & 0x7ff) == 0x7ff) {  // !isfinite
-        alive = false;
-        continue;
-      }
-      uint64_t o = ord_bits(u);
-      if (P.periodic[d]) {
-        if (o < P.olo[d] || o >= P.ohi[d]) {
-          // the reference's wrap loops (rare)
-          const double w = __dsub_rn(P.hi[d], P.lo[d]);
-          int k = 0;
-          while (r < P.lo[d] && k < CL_WRAP_CAP) { r = __dadd_rn(r, w); ++k; }
-          while (r >= P.hi[d] && k < CL_WRAP_CAP) { r = __dsub_rn(r, w); ++k; }
-          if (k >= CL_WRAP_CAP) {
-            err = 2;
+  for (int64_t base = (int64_t)blockIdx.x * CL_KEYS_TILE; base < n;
+       base += (int64_t)gridDim.x * CL_KEYS_TILE) {
+#pragma unroll 2
+    for (int it = 0; it < CL_KEYS_TILE / CL_TPB; ++it) {
+      const int64_t i = base + (int64_t)it * CL_TPB + threadIdx.x;
+      if (i < n) {
+        double r[DIM];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) r[d] = pos[(int64_t)d * n + i];
+        bool alive = true;
+        uint32_t key = 0, mult = 1;
+#pragma unroll
+        for (int d = DIM - 1; d >= 0; --d) {
+          uint64_t u = (uint64_t)__double_as_longlong(r[d]);
+          uint32_t v = 0;
+          const uint32_t hw = (uint32_t)(u >> 32);
+          const uint32_t ex = (hw >> 20) & 0x7ffu;
+          // fast path: the FP32 value shows the coordinate inside the domain
+          // and the FP32 bucket estimate away from a cell boundary by more
+          // than its error bound, so both decisions are the FP64 ones
+          bool fast = false;
+          if (ex - 897u < 254u) {  // a normal FP32 exponent
+            const float xf = __uint_as_float((hw & 0x80000000u) |
+                                             (((hw & 0x7fffffffu) - (896u << 20)) << 3) |
+                                             ((uint32_t)u >> 29));
+            if (xf >= P.lo_fast[d] && xf <= P.hi_fast[d]) {
+              const float t = fmaf(xf, P.inv_f[d], P.c_f[d]);
+              const float vf = floorf(t);
+              const float fr = t - vf;
+              if (fr >= P.delta_f[d] && fr <= 1.0f - P.delta_f[d]) {
+                v = (uint32_t)(int)vf;
+                fast = true;
+              }
+            }
+          }
+          if (fast) {
+          } else if (ex == 0x7ffu) {  // !isfinite
             alive = false;
+          } else {
+            uint64_t o = ord_bits(u);
+            bool exact = false;
+            if (o < P.olo[d] || o >= P.ohi[d]) {
+              if (P.periodic[d]) {
+                // the reference's wrap loops (rare)
+                double x = r[d];
+                const double w = __dsub_rn(P.hi[d], P.lo[d]);
+                int k = 0;
+                while (x < P.lo[d] && k < CL_WRAP_CAP) { x = __dadd_rn(x, w); ++k; }
+                while (x >= P.hi[d] && k < CL_WRAP_CAP) { x = __dsub_rn(x, w); ++k; }
+                if (k >= CL_WRAP_CAP) {
+                  err = 2;
+                  alive = false;
+                }
+                pos[(int64_t)d * n + i] = x;
+                u = (uint64_t)__double_as_longlong(x);
+                o = ord_bits(u);
+                if (o < P.olo[d] || o >= P.ohi[d]) {
+                  // the wrap rounded outside [lo, hi): the reference's formula as is
+                  v = (uint32_t)(int)floor(__dmul_rn(__dsub_rn(x, P.lo[d]), P.inv[d]));
+                  exact = true;
+                }
+              } else {
+                alive = false;
+              }
+            }
+            if (alive && !exact) v = cell_coord(u, d, P, tab + P.bnd_off[d]);
           }
-          pos[(int64_t)d * n + i] = r;
-          u = (uint64_t)__double_as_longlong(r);
-          o = ord_bits(u);
-          if (alive && (o < P.olo[d] || o >= P.ohi[d])) {
-            // the wrap rounded outside [lo, hi): the reference's formula as is
-            v[d] = (uint32_t)(int)floor(__dmul_rn(__dsub_rn(r, P.lo[d]), P.inv[d]));
-            continue;
-          }
+          // collapse_index_vector (src/detail/SpatialUtil.h:49-59): last
+          // dimension fastest, unsigned 32-bit arithmetic
+          if (d != DIM - 1) mult *= P.size[d + 1];
+          key += mult * v;
         }
-      } else if (o < P.olo[d] || o >= P.ohi[d]) {
-        alive = false;
+        if (!alive) {
+          key = P.dead_key;
+          ++dead;
+        }
+        keys[i] = key;
+        vals[i] = (uint32_t)i;
+        atomicAdd(&h[0][key & (CL_RADIX - 1)], 1u);
+        for (int p = 1; p < P.npasses; ++p) atomicAdd(&h[p][(key >> (CL_RB * p)) & (CL_RADIX - 1)], 1u);
       }
-      if (alive) v[d] = cell_coord(u, d, P);
     }
-    uint32_t key = P.dead_key;
-    if (alive) {
-      // collapse_index_vector (src/detail/SpatialUtil.h:49-59): last
-      // dimension fastest, unsigned 32-bit arithmetic
-      key = 0;
-      uint32_t mult = 1;
-      for (int d = P.dim - 1; d >= 0; --d) {
-        if (d != P.dim - 1) mult *= P.size[d + 1];
-        key += mult * v[d];
-      }
-    } else {
-      ++dead;
-    }
-    keys[i] = key;
-    vals[i] = (uint32_t)i;
-    for (int p = 0; p < P.npasses; ++p) atomicAdd(&h[p][(key >> (CL_RB * p)) & (CL_RADIX - 1)], 1u);
   }
   if (err) atomicMax(&H->error, err);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) dead += __shfl_xor_sync(0xffffffffu, dead, o);
   if ((threadIdx.x & 31) == 0 && dead) atomicAdd(&sdead, dead);
   __syncthreads();
+  uint32_t *part = &H->part[blockIdx.x % CL_HIST_COPIES][0][0];
   for (int i = threadIdx.x; i < P.npasses * CL_RADIX; i += CL_TPB) {
     const uint32_t c = (&h[0][0])[i];
-    if (c) atomicAdd(&(&H->hist[0][0])[i], c);
+    if (c) atomicAdd(&part[i], c);
   }
   if (threadIdx.x == 0 && sdead) atomicAdd(&H->dead, sdead);
+  // the last block to finish sums the copies into the pass histograms
+  __threadfence();
+  __shared__ uint32_t ticket;
+  __syncthreads();
+  if (threadIdx.x == 0) ticket = atomicAdd(&H->blocks_done, 1u);
+  __syncthreads();
+  if (ticket != gridDim.x - 1) return;
+  __threadfence();
+  for (int i = threadIdx.x; i < P.npasses * CL_RADIX; i += CL_TPB) {
+    uint32_t t = 0;
+    for (int c = 0; c < CL_HIST_COPIES; ++c) t += ((volatile uint32_t *)&H->part[c][0][0])[i];
+    (&H->hist[0][0])[i] = t;
+  }
 }
 
 __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long *p) {
@@ -192,28 +251,46 @@ __device__ __forceinline__ void st_release(unsigned long long *p, unsigned long 
   asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-// One stable LSD pass over the digit (key >> shift) & (CL_RADIX - 1).
+// Dynamic shared memory of the sort pass: the tile's keys, values and
+// within-warp ranks, the per-warp digit counts and the digit bases.
+struct SweepSmem {
+  uint32_t key[CL_TILE];
+  uint32_t val[CL_TILE];
+  uint16_t rank[CL_TILE];
+  uint16_t wcount[SW_WARPS][CL_RADIX + 2];  // counts, then offsets, per warp (<= 16384)
+  uint32_t dbase[CL_RADIX];
+  uint32_t wsum[SW_WARPS + 1];
+  uint32_t tile, fail;
+};
+
+// One stable LSD pass over the digit (key >> 10 pass) & (CL_RADIX - 1).
+// A tile is 16384 keys: warp w of 16 ranks its own 1024 consecutive keys in
+// two rounds of 512 (lane l holding keys l, l+32, ... of a round, so the slots
+// visit them in input order; __match_any_sync gives the stable rank within
+// the warp), staging keys, values and ranks in shared memory.  The tile's
+// digit counts are published and prefixed by decoupled look-back over the
+// preceding tiles (tiles are claimed in order, so every tile waited on is
+// already running), then every key is written to its place.
 // Status word of (tile, digit): epoch << 34 | flag << 32 | count.
-__global__ void __launch_bounds__(CL_TPB) k_cl_onesweep(
+__global__ void __launch_bounds__(SW_TPB) k_cl_onesweep(
     const uint32_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
     uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, uint32_t n, int pass,
     unsigned long long *__restrict__ status, uint32_t epoch, ClHeader *__restrict__ H) {
-  __shared__ uint32_t wcount[CL_WARPS][CL_RADIX + 1];
-  __shared__ uint32_t dbase[CL_RADIX];
-  __shared__ uint32_t wsum[CL_WARPS + 1];
-  __shared__ uint32_t stile, sfail;
+  extern __shared__ __align__(16) unsigned char sweep_raw[];
+  SweepSmem &S = *reinterpret_cast<SweepSmem *>(sweep_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int shift = CL_RB * pass;
   if (tid == 0) {
-    stile = atomicAdd(&H->tile_counter[pass], 1u);
-    sfail = 0;
+    S.tile = atomicAdd(&H->tile_counter[pass], 1u);
+    S.fail = 0;
   }
-  for (int i = tid; i < CL_WARPS * (CL_RADIX + 1); i += CL_TPB) (&wcount[0][0])[i] = 0;
-  // global digit bases: exclusive scan of the pass histogram (4 digits per thread)
-  uint32_t g[4], gs = 0;
+  for (int i = tid; i < SW_WARPS * (CL_RADIX + 2); i += SW_TPB) (&S.wcount[0][0])[i] = 0;
+  // global digit bases: exclusive scan of the pass histogram
+  constexpr int DPT = CL_RADIX / SW_TPB;  // digits per thread
+  uint32_t g[DPT], gs = 0;
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    g[q] = H->hist[pass][tid * 4 + q];
+  for (int q = 0; q < DPT; ++q) {
+    g[q] = H->hist[pass][tid * DPT + q];
     gs += g[q];
   }
   uint32_t incl = gs;
@@ -222,72 +299,75 @@ __global__ void __launch_bounds__(CL_TPB) k_cl_onesweep(
     const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
     if (lane >= o) incl += t;
   }
-  if (lane == 31) wsum[warp] = incl;
+  if (lane == 31) S.wsum[warp] = incl;
   __syncthreads();
   if (tid == 0) {
     uint32_t run = 0;
-    for (int w = 0; w < CL_WARPS; ++w) {
-      const uint32_t c = wsum[w];
-      wsum[w] = run;
+    for (int w = 0; w < SW_WARPS; ++w) {
+      const uint32_t c = S.wsum[w];
+      S.wsum[w] = run;
       run += c;
     }
   }
   __syncthreads();
   {
-    uint32_t run = wsum[warp] + incl - gs;
+    uint32_t run = S.wsum[warp] + incl - gs;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      dbase[tid * 4 + q] = run;
+    for (int q = 0; q < DPT; ++q) {
+      S.dbase[tid * DPT + q] = run;
       run += g[q];
     }
   }
-  const uint32_t tile = stile;
-  // load and rank (warp w owns 512 consecutive items; lane l holds items
-  // l, l+32, ... so the slots visit the warp's items in input order)
-  const size_t base = (size_t)tile * CL_TILE + (size_t)warp * (32 * CL_ITEMS);
-  uint32_t key[CL_ITEMS], val[CL_ITEMS], rank[CL_ITEMS];
-  int dig[CL_ITEMS];
+  const uint32_t tile = S.tile;
   const uint32_t lt_mask = (1u << lane) - 1u;
+  constexpr int WCHUNK = CL_TILE / SW_WARPS;  // 1024 keys per warp
+  for (int round = 0; round < SW_ROUNDS; ++round) {
+    const int lbase = warp * WCHUNK + round * (32 * CL_ITEMS);  // within the tile
+    const size_t gbase = (size_t)tile * CL_TILE + lbase;
+    uint32_t key[CL_ITEMS], val[CL_ITEMS];
+    int dig[CL_ITEMS];
 #pragma unroll
-  for (int i = 0; i < CL_ITEMS; ++i) {
-    const size_t gi = base + (size_t)i * 32 + lane;
-    if (gi < n) {
-      key[i] = keys_in[gi];
-      val[i] = vals_in[gi];
-      dig[i] = (key[i] >> shift) & (CL_RADIX - 1);
-    } else {
-      key[i] = 0;
-      val[i] = 0;
-      dig[i] = CL_RADIX;  // sentinel, never written out
+    for (int i = 0; i < CL_ITEMS; ++i) {
+      const size_t gi = gbase + (size_t)i * 32 + lane;
+      if (gi < n) {
+        key[i] = keys_in[gi];
+        val[i] = vals_in[gi];
+        dig[i] = (key[i] >> shift) & (CL_RADIX - 1);
+      } else {
+        key[i] = 0;
+        val[i] = 0;
+        dig[i] = CL_RADIX;  // sentinel, never written out
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < CL_ITEMS; ++i) {
+      const uint32_t peers = __match_any_sync(0xffffffffu, dig[i]);
+      const int leader = 31 - __clz(peers);
+      const uint32_t before = __popc(peers & lt_mask);
+      const uint32_t cnt = S.wcount[warp][dig[i]];  // the sentinel column CL_RADIX included
+      const int li = lbase + i * 32 + lane;
+      S.key[li] = key[i];
+      S.val[li] = val[i];
+      S.rank[li] = (uint16_t)(cnt + before);
+      __syncwarp();
+      if (lane == leader) S.wcount[warp][dig[i]] = (uint16_t)(cnt + __popc(peers));
+      __syncwarp();
     }
   }
   __syncthreads();
-#pragma unroll
-  for (int i = 0; i < CL_ITEMS; ++i) {
-    const uint32_t peers = __match_any_sync(0xffffffffu, dig[i]);
-    const int leader = 31 - __clz(peers);
-    const uint32_t before = __popc(peers & lt_mask);
-    const uint32_t cnt = wcount[warp][dig[i]];
-    rank[i] = cnt + before;
-    __syncwarp();
-    if (lane == leader) wcount[warp][dig[i]] = cnt + __popc(peers);
-    __syncwarp();
-  }
-  __syncthreads();
-  // per digit (4 per thread): warp prefixes and the tile's count, published
-  // for every digit first; then the decoupled look-back over the preceding
-  // tiles and the inclusive publication
-  constexpr int DPT = CL_RADIX / CL_TPB;
+  // per digit: warp prefixes and the tile's count, published for every digit
+  // first; then the decoupled look-back over the preceding tiles and the
+  // inclusive publication
   const unsigned long long ep = (unsigned long long)epoch << 34;
   uint32_t tcount[DPT];
 #pragma unroll
   for (int q = 0; q < DPT; ++q) {
-    const int d = tid + q * CL_TPB;
+    const int d = tid + q * SW_TPB;
     uint32_t run = 0;
 #pragma unroll
-    for (int w = 0; w < CL_WARPS; ++w) {
-      const uint32_t c = wcount[w][d];
-      wcount[w][d] = run;
+    for (int w = 0; w < SW_WARPS; ++w) {
+      const uint32_t c = S.wcount[w][d];
+      S.wcount[w][d] = (uint16_t)run;
       run += c;
     }
     tcount[q] = run;
@@ -296,7 +376,7 @@ __global__ void __launch_bounds__(CL_TPB) k_cl_onesweep(
   if (tile > 0) {
 #pragma unroll
     for (int q = 0; q < DPT; ++q) {
-      const int d = tid + q * CL_TPB;
+      const int d = tid + q * SW_TPB;
       uint32_t prefix = 0;
       for (int64_t t = (int64_t)tile - 1; t >= 0; --t) {
         const unsigned long long *pp = status + (size_t)t * CL_RADIX + d;
@@ -320,7 +400,7 @@ __global__ void __launch_bounds__(CL_TPB) k_cl_onesweep(
           st = ld_acquire(pp);
         }
         if (gave_up) {
-          atomicExch(&sfail, 1u);
+          atomicExch(&S.fail, 1u);
           atomicMax(&H->error, 1u);
           break;
         }
@@ -328,21 +408,21 @@ __global__ void __launch_bounds__(CL_TPB) k_cl_onesweep(
         if (((st >> 32) & 3ull) == 2ull) break;
       }
       st_release(status + (size_t)tile * CL_RADIX + d, ep | ST_INCL | (uint32_t)(prefix + tcount[q]));
-      dbase[d] += prefix;
+      S.dbase[d] += prefix;
     }
   }
   __syncthreads();
-  if (sfail) {
-    if (tid == 0) atomicMax(&H->error, 1u);
-    return;
-  }
-#pragma unroll
-  for (int i = 0; i < CL_ITEMS; ++i) {
-    if (dig[i] < CL_RADIX) {
-      const uint32_t dst = dbase[dig[i]] + wcount[warp][dig[i]] + rank[i];
-      keys_out[dst] = key[i];
-      vals_out[dst] = val[i];
-    }
+  if (S.fail) return;
+  const int nvalid = (int)min((size_t)CL_TILE, (size_t)n - (size_t)tile * CL_TILE);
+  // staged key li came from position tile * CL_TILE + li and was ranked by
+  // warp li / WCHUNK; keys past n were never staged
+  for (int li = tid; li < nvalid; li += SW_TPB) {
+    const int w = li / WCHUNK;
+    const uint32_t k = S.key[li];
+    const int d = (k >> shift) & (CL_RADIX - 1);
+    const uint32_t dst = S.dbase[d] + S.wcount[w][d] + S.rank[li];
+    keys_out[dst] = k;
+    vals_out[dst] = S.val[li];
   }
 }
 
@@ -451,10 +531,31 @@ int run_build(abx_particles *p, const GridDesc &g, uint32_t *dead_out) {
     P.periodic[d] = g.periodic[d];
     P.olo[d] = ord_host(g.lo[d]);
     P.ohi[d] = ord_host(g.hi[d]);
-    P.lo_f[d] = (float)g.lo[d];
     P.inv_f[d] = (float)g.inv_side[d];
+    P.c_f[d] = (float)(-g.lo[d] * g.inv_side[d]);
+    // with M = max |bound|: the FP32 value xf of an in-range x (mantissa
+    // truncated) is within M 2^-23 of x, so xf in [lo_fast, hi_fast] (lo + m
+    // and hi - m rounded inwards, m = M 2^-21) puts x inside [lo, hi); the
+    // FP32 estimate of (x - lo) inv is then within M inv 2^-21 + (size+1)
+    // 2^-23 of the FP64 one, delta_f doubles that
+    const double M = std::max(std::fabs(g.lo[d]), std::fabs(g.hi[d]));
+    const double m = std::ldexp(M, -21);
+    P.lo_fast[d] = std::nextafter((float)(g.lo[d] + m), HUGE_VALF);
+    P.hi_fast[d] = std::nextafter((float)(g.hi[d] - m), -HUGE_VALF);
+    P.delta_f[d] = (float)(std::ldexp(M * g.inv_side[d], -20) +
+                           std::ldexp((double)g.size[d] + 2.0, -22) + 1e-7);
+    if (!(P.delta_f[d] < 0.25f) || !(P.lo_fast[d] < P.hi_fast[d])) {
+      // cells too fine for the FP32 estimate: every coordinate takes the exact path
+      P.lo_fast[d] = HUGE_VALF;
+      P.hi_fast[d] = -HUGE_VALF;
+    }
     P.bnd[d] = p->cl_bnd.ptr + p->cl_bnd_off[d];
+    P.bnd_off[d] = (int)p->cl_bnd_off[d];
   }
+  P.bnd_all = p->cl_bnd.ptr;
+  P.bnd_total = 0;
+  for (int d = 0; d < D; ++d) P.bnd_total += (int)g.size[d] + 2;
+  const size_t keys_smem = P.bnd_total <= CL_BND_SMEM ? (size_t)P.bnd_total * 8 : 0;
   const int ntiles = (int)((n + CL_TILE - 1) / CL_TILE);
   // scratch: header, vals, keys_alt, vals_alt
   size_t o = 0;
@@ -476,14 +577,23 @@ int run_build(abx_particles *p, const GridDesc &g, uint32_t *dead_out) {
     ABX_CHECK_CUDA(cudaMemsetAsync(p->cl_status.ptr, 0, nstatus * 8, s));
   }
   ABX_CHECK_CUDA(cudaMemsetAsync(H, 0, sizeof(ClHeader), s));
-  k_cl_keys<<<ntiles, CL_TPB, 0, s>>>(p->pos.ptr, n, P, p->keys.ptr, vals, H);
+  ABX_CHECK_CUDA(cudaFuncSetAttribute(k_cl_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sizeof(SweepSmem)));
+  const int kblocks = (int)std::min<int64_t>((n + CL_KEYS_TILE - 1) / CL_KEYS_TILE,
+                                             (int64_t)ctx->num_sms * 4);
+  if (D == 1)
+    k_cl_keys<1><<<kblocks, CL_TPB, keys_smem, s>>>(p->pos.ptr, n, P, p->keys.ptr, vals, H);
+  else if (D == 2)
+    k_cl_keys<2><<<kblocks, CL_TPB, keys_smem, s>>>(p->pos.ptr, n, P, p->keys.ptr, vals, H);
+  else
+    k_cl_keys<3><<<kblocks, CL_TPB, keys_smem, s>>>(p->pos.ptr, n, P, p->keys.ptr, vals, H);
   ABX_CHECK_CUDA(cudaGetLastError());
   uint32_t *ki = p->keys.ptr, *vi = vals, *ko = keys_alt, *vo = vals_alt;
   for (int pass = 0; pass < P.npasses; ++pass) {
     p->cl_epoch = (p->cl_epoch + 1) & 0x3fffffffu;
     if (p->cl_epoch == 0) p->cl_epoch = 1;
-    k_cl_onesweep<<<ntiles, CL_TPB, 0, s>>>(ki, vi, ko, vo, (uint32_t)n, pass, p->cl_status.ptr,
-                                            p->cl_epoch, H);
+    k_cl_onesweep<<<ntiles, SW_TPB, sizeof(SweepSmem), s>>>(ki, vi, ko, vo, (uint32_t)n, pass,
+                                                            p->cl_status.ptr, p->cl_epoch, H);
     ABX_CHECK_CUDA(cudaGetLastError());
     std::swap(ki, ko);
     std::swap(vi, vo);
