@@ -165,6 +165,29 @@ class Particles:
     def update_positions(self):
         _check(lib().abx_particles_update_positions(self._h), "abx_particles_update_positions")
 
+    def push_back(self, pos):
+        """Append particles (``Particles::push_back``); returns their ids.  A
+        searchable set is re-searched at once, as the reference does."""
+        pos = np.ascontiguousarray(np.atleast_2d(pos), dtype=np.float64).reshape(-1, self.dim)
+        ids = np.empty(len(pos), dtype=np.int64)
+        _check(lib().abx_particles_push_back(self._h, len(pos), _ptr(pos), _ptr(ids)),
+               "abx_particles_push_back")
+        return ids
+
+    def erase(self, first: int, last: int | None = None):
+        """``Particles::erase``: drop the particles at storage positions
+        [first, last) (last defaults to first + 1)."""
+        last = first + 1 if last is None else last
+        _check(lib().abx_particles_erase(self._h, int(first), int(last)), "abx_particles_erase")
+
+    def find_ids(self, ids):
+        """Storage index of every id (-1 where absent): find-by-id."""
+        ids = np.ascontiguousarray(ids, dtype=np.int64)
+        out = np.empty(len(ids), dtype=np.int64)
+        _check(lib().abx_particles_find_ids(self._h, len(ids), _ptr(ids), _ptr(out)),
+               "abx_particles_find_ids")
+        return out
+
     @property
     def positions(self) -> np.ndarray:
         out = np.empty((len(self), self.dim), dtype=np.float64)

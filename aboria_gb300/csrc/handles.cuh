@@ -74,6 +74,11 @@ struct abx_particles {
   bool cl_bnd_valid = false;
   abx::DevBuf<unsigned long long> cl_status;
   uint32_t cl_epoch = 0;
+  // find-by-id map (NeighbourSearchBase::find_id_map): ids sorted, with the
+  // storage index of each; rebuilt when the storage version moved
+  abx::DevBuf<int64_t> idmap_key;
+  abx::DevBuf<uint32_t> idmap_val;
+  uint64_t idmap_version = ~uint64_t(0);
 };
 
 namespace abx {

@@ -154,6 +154,56 @@ __global__ void k_gather(const T *__restrict__ src, const uint32_t *__restrict__
   dst[k] = src[perm[k]];
 }
 
+// new particles (AoS) into rows [n0, n) of SoA columns of stride n
+__global__ void k_append_aos(const double *__restrict__ aos, int64_t n_new, int dim, int64_t n0,
+                             int64_t n, double *__restrict__ soa) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_new) return;
+  for (int d = 0; d < dim; ++d) soa[(int64_t)d * n + n0 + i] = aos[i * dim + d];
+}
+
+__global__ void k_mark_dead(double *__restrict__ pos, int64_t first, int64_t last) {
+  int64_t i = first + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < last) pos[i] = __longlong_as_double(0x7ff8000000000000ll);  // NaN
+}
+
+// one 32-bit half of each id (as unsigned 64-bit), in the order `order`
+// (null: storage order); vals get the storage index
+__global__ void k_id_half(const int64_t *__restrict__ ids, const uint32_t *__restrict__ order,
+                          int64_t n, int high, uint32_t *__restrict__ keys,
+                          uint32_t *__restrict__ vals) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint32_t i = order ? order[k] : (uint32_t)k;
+  const uint64_t id = (uint64_t)ids[i];
+  keys[k] = high ? (uint32_t)(id >> 32) : (uint32_t)id;
+  vals[k] = i;
+}
+
+__global__ void k_idmap_fill(const int64_t *__restrict__ ids, const uint32_t *__restrict__ perm,
+                             int64_t n, int64_t *__restrict__ key, uint32_t *__restrict__ val) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  key[k] = ids[perm[k]];
+  val[k] = perm[k];
+}
+
+// find_id_map (src/NeighbourSearchBase.h:276-281): lower_bound of the id in
+// the sorted keys; storage index, or -1 when the id is not in the set
+__global__ void k_find_ids(const int64_t *__restrict__ key, const uint32_t *__restrict__ val,
+                           int64_t n, const int64_t *__restrict__ q, int64_t nq,
+                           int64_t *__restrict__ out) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nq) return;
+  const uint64_t id = (uint64_t)q[t];
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if ((uint64_t)key[mid] < id) lo = mid + 1; else hi = mid;
+  }
+  out[t] = (lo < n && (uint64_t)key[lo] == id) ? (int64_t)val[lo] : -1;
+}
+
 __global__ void k_aos_to_soa(const double *__restrict__ aos, int64_t n, int dim,
                              double *__restrict__ soa) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -659,6 +709,160 @@ int abx_particles_update_positions(abx_particles *p) {
   ABX_REQUIRE(p->domain_set, ABX_ERR_STATE, "init_neighbour_search not called");
   ABX_TRY(ctx_activate(p->ctx));
   return update_positions(p);
+}
+
+int abx_particles_push_back(abx_particles *p, int64_t n_new, const double *pos, int64_t *ids_out) {
+  ABX_REQUIRE(p && (pos || n_new == 0), ABX_ERR_INVALID, "null argument");
+  ABX_REQUIRE(n_new >= 0, ABX_ERR_INVALID, "negative particle count");
+  ABX_TRY(ctx_activate(p->ctx));
+  if (n_new == 0) return ABX_OK;
+  cudaStream_t s = p->ctx->stream;
+  const int D = p->dim;
+  const int64_t n0 = p->n, n = n0 + n_new;
+  const void *dpos;
+  ABX_TRY(p->stage_a.in(p->ctx, pos, (size_t)n_new * D * sizeof(double), &dpos));
+  // grow the SoA columns into the alternate buffers, then swap
+  ABX_TRY(p->pos_alt.reserve((size_t)D * n));
+  ABX_TRY(p->ids_alt.reserve(n));
+  for (int d = 0; d < D; ++d)
+    if (n0)
+      ABX_CHECK_CUDA(cudaMemcpyAsync(p->pos_alt.ptr + (size_t)d * n, p->pos.ptr + (size_t)d * n0,
+                                     n0 * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  k_append_aos<<<ceil_div(n_new, TPB), TPB, 0, s>>>((const double *)dpos, n_new, D, n0, n,
+                                                   p->pos_alt.ptr);
+  if (n0)
+    ABX_CHECK_CUDA(cudaMemcpyAsync(p->ids_alt.ptr, p->ids.ptr, n0 * sizeof(int64_t),
+                                   cudaMemcpyDeviceToDevice, s));
+  k_iota64<<<ceil_div(n_new, TPB), TPB, 0, s>>>(p->ids_alt.ptr + n0, n_new, p->next_id);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  if (p->has_scalar) {
+    ABX_TRY(p->scalar_alt.reserve(n));
+    if (n0)
+      ABX_CHECK_CUDA(cudaMemcpyAsync(p->scalar_alt.ptr, p->scalar.ptr, n0 * sizeof(double),
+                                     cudaMemcpyDeviceToDevice, s));
+    ABX_CHECK_CUDA(cudaMemsetAsync(p->scalar_alt.ptr + n0, 0, n_new * sizeof(double), s));
+    std::swap(p->scalar.ptr, p->scalar_alt.ptr);
+    std::swap(p->scalar.cap, p->scalar_alt.cap);
+  }
+  std::swap(p->pos.ptr, p->pos_alt.ptr);
+  std::swap(p->pos.cap, p->pos_alt.cap);
+  std::swap(p->ids.ptr, p->ids_alt.ptr);
+  std::swap(p->ids.cap, p->ids_alt.cap);
+  if (ids_out)
+    for (int64_t k = 0; k < n_new; ++k) ids_out[k] = p->next_id + k;
+  p->next_id += n_new;
+  p->n = n;
+  ++p->version;
+  ABX_CHECK_CUDA(cudaStreamSynchronize(s));
+  // Particles::push_back on a searchable, ordered set updates the whole
+  // search structure (src/Particles.h:264-283)
+  if (p->searchable) return update_positions(p);
+  return ABX_OK;
+}
+
+int abx_particles_erase(abx_particles *p, int64_t first, int64_t last) {
+  ABX_REQUIRE(p, ABX_ERR_INVALID, "null particles");
+  ABX_REQUIRE(first >= 0 && first <= last && last <= p->n, ABX_ERR_INVALID,
+              "erase range [%lld, %lld) outside [0, %lld)", (long long)first, (long long)last,
+              (long long)p->n);
+  ABX_TRY(ctx_activate(p->ctx));
+  if (first == last) return ABX_OK;
+  // Particles::erase sets alive = false and updates the search structure,
+  // which drops the dead (src/Particles.h:361-389); a non-finite position is
+  // dead in the same update
+  k_mark_dead<<<ceil_div(last - first, TPB), TPB, 0, p->ctx->stream>>>(p->pos.ptr, first, last);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  ++p->version;
+  if (p->domain_set) return update_positions(p);
+  // no search structure yet: compact on the host side of the columns
+  const int64_t n = p->n, k = last - first, D = p->dim;
+  cudaStream_t s = p->ctx->stream;
+  ABX_TRY(p->pos_alt.reserve((size_t)D * (n - k) + 1));
+  ABX_TRY(p->ids_alt.reserve(n - k + 1));
+  for (int d = 0; d < D; ++d) {
+    if (first)
+      ABX_CHECK_CUDA(cudaMemcpyAsync(p->pos_alt.ptr + (size_t)d * (n - k), p->pos.ptr + (size_t)d * n,
+                                     first * 8, cudaMemcpyDeviceToDevice, s));
+    if (n - last)
+      ABX_CHECK_CUDA(cudaMemcpyAsync(p->pos_alt.ptr + (size_t)d * (n - k) + first,
+                                     p->pos.ptr + (size_t)d * n + last, (n - last) * 8,
+                                     cudaMemcpyDeviceToDevice, s));
+  }
+  if (first)
+    ABX_CHECK_CUDA(cudaMemcpyAsync(p->ids_alt.ptr, p->ids.ptr, first * 8, cudaMemcpyDeviceToDevice, s));
+  if (n - last)
+    ABX_CHECK_CUDA(cudaMemcpyAsync(p->ids_alt.ptr + first, p->ids.ptr + last, (n - last) * 8,
+                                   cudaMemcpyDeviceToDevice, s));
+  if (p->has_scalar) {
+    ABX_TRY(p->scalar_alt.reserve(n - k + 1));
+    if (first)
+      ABX_CHECK_CUDA(cudaMemcpyAsync(p->scalar_alt.ptr, p->scalar.ptr, first * 8,
+                                     cudaMemcpyDeviceToDevice, s));
+    if (n - last)
+      ABX_CHECK_CUDA(cudaMemcpyAsync(p->scalar_alt.ptr + first, p->scalar.ptr + last,
+                                     (n - last) * 8, cudaMemcpyDeviceToDevice, s));
+    std::swap(p->scalar.ptr, p->scalar_alt.ptr);
+    std::swap(p->scalar.cap, p->scalar_alt.cap);
+  }
+  std::swap(p->pos.ptr, p->pos_alt.ptr);
+  std::swap(p->pos.cap, p->pos_alt.cap);
+  std::swap(p->ids.ptr, p->ids_alt.ptr);
+  std::swap(p->ids.cap, p->ids_alt.cap);
+  p->n = n - k;
+  ABX_CHECK_CUDA(cudaStreamSynchronize(s));
+  return ABX_OK;
+}
+
+int abx_particles_find_ids(abx_particles *p, int64_t nq, const int64_t *ids, int64_t *index_out) {
+  ABX_REQUIRE(p && ((ids && index_out) || nq == 0), ABX_ERR_INVALID, "null argument");
+  ABX_TRY(ctx_activate(p->ctx));
+  if (nq == 0) return ABX_OK;
+  cudaStream_t s = p->ctx->stream;
+  const int64_t n = p->n;
+  ABX_REQUIRE(n < (int64_t)0xFFFFFFFFll, ABX_ERR_INVALID, "too many particles");
+  if (p->idmap_version != p->version) {
+    // (id, storage index) sorted by id: stable LSD radix sort of the id's
+    // two 32-bit halves (low half first), ids as unsigned 64-bit keys
+    ABX_TRY(p->idmap_key.reserve(n ? n : 1));
+    ABX_TRY(p->idmap_val.reserve(n ? n : 1));
+    if (n) {
+      size_t off = 0;
+      carve_size<uint32_t>(off, n);
+      carve_size<uint32_t>(off, n);
+      carve_size<uint32_t>(off, n);
+      carve_size<uint32_t>(off, n);
+      carve_size<uint32_t>(off, n);
+      carve_size<uint32_t>(off, radix_temp_u32(n));
+      ABX_TRY(p->ctx->scratch.reserve(off + 256));
+      unsigned char *base = p->ctx->scratch.ptr;
+      off = 0;
+      uint32_t *k = carve<uint32_t>(base, off, n);
+      uint32_t *v = carve<uint32_t>(base, off, n);
+      uint32_t *ka = carve<uint32_t>(base, off, n);
+      uint32_t *va = carve<uint32_t>(base, off, n);
+      uint32_t *perm = carve<uint32_t>(base, off, n);
+      uint32_t *tmp = carve<uint32_t>(base, off, radix_temp_u32(n));
+      k_id_half<<<ceil_div(n, TPB), TPB, 0, s>>>(p->ids.ptr, nullptr, n, 0, k, v);
+      ABX_TRY(radix_sort_pairs(k, v, n, 32, ka, va, tmp, s));
+      k_id_half<<<ceil_div(n, TPB), TPB, 0, s>>>(p->ids.ptr, v, n, 1, k, perm);
+      ABX_TRY(radix_sort_pairs(k, perm, n, 32, ka, va, tmp, s));
+      k_idmap_fill<<<ceil_div(n, TPB), TPB, 0, s>>>(p->ids.ptr, perm, n, p->idmap_key.ptr,
+                                                     p->idmap_val.ptr);
+      ABX_CHECK_CUDA(cudaGetLastError());
+    }
+    p->idmap_version = p->version;
+  }
+  const void *dq;
+  void *dout;
+  HostStage out;
+  ABX_TRY(p->stage_b.in(p->ctx, ids, nq * sizeof(int64_t), &dq));
+  ABX_TRY(out.out(p->ctx, index_out, nq * sizeof(int64_t), &dout));
+  k_find_ids<<<ceil_div(nq, TPB), TPB, 0, s>>>(p->idmap_key.ptr, p->idmap_val.ptr, n,
+                                               (const int64_t *)dq, nq, (int64_t *)dout);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  ABX_TRY(out.finish(p->ctx, index_out, nq * sizeof(int64_t)));
+  ABX_CHECK_CUDA(cudaStreamSynchronize(s));
+  return ABX_OK;
 }
 
 int abx_particles_get_grid(abx_particles *p, uint32_t *size, double *side, uint32_t *ncells) {

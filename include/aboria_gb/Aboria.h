@@ -222,11 +222,53 @@ class Particles<std::tuple<Vars...>, D, Storage, SearchMethod> {
    * takes effect on the device at the next init_neighbour_search /
    * update_positions. */
   void push_back(const value_type &v) {
+    if (searched_ && !dirty_) {
+      // a searchable set is updated at once (src/Particles.h:264-283)
+      const std::vector<int64_t> before = ids_;
+      int64_t nid = 0;
+      detail::check(abx_particles_push_back(h_.get(), 1, v.pos.data(), &nid), "push_back");
+      ids_.push_back(nid);
+      next_id_ = nid + 1;
+      push_vars(v.vars, std::index_sequence_for<Vars...>());
+      std::vector<int64_t> with_new = before;
+      with_new.push_back(nid);
+      download(with_new);
+      return;
+    }
     pos_.push_back(v.pos);
     ids_.push_back(next_id_++);
     push_vars(v.vars, std::index_sequence_for<Vars...>());
     dirty_ = true;
     ++version_;
+  }
+
+  /* erase(i) / erase(first, last) (src/Particles.h:361-389): the particles at
+   * storage positions [first, last) are dropped; a searchable set is updated
+   * at once. */
+  void erase(size_t first, size_t last) {
+    if (first >= last) return;
+    if (searched_ && !dirty_) {
+      std::vector<int64_t> before = ids_;
+      detail::check(abx_particles_erase(h_.get(), int64_t(first), int64_t(last)), "erase");
+      download(before);
+      return;
+    }
+    pos_.erase(pos_.begin() + first, pos_.begin() + last);
+    ids_.erase(ids_.begin() + first, ids_.begin() + last);
+    apply_vars([&](auto &col) { col.erase(col.begin() + first, col.begin() + last); });
+    dirty_ = true;
+    ++version_;
+  }
+  void erase(size_t i) { erase(i, i + 1); }
+
+  /* Find-by-id (src/NeighbourSearchBase.h:276-321): the storage position of
+   * the particle with this id, or size() when there is none (the reference
+   * returns end()). */
+  size_t find(int64_t particle_id) {
+    upload();
+    int64_t idx = -1;
+    detail::check(abx_particles_find_ids(h_.get(), 1, &particle_id, &idx), "find");
+    return idx < 0 ? size() : size_t(idx);
   }
   void push_back(const double_d &x) {
     value_type v;

@@ -103,6 +103,24 @@ ABX_API int abx_particles_init_neighbour_search(abx_particles *p, const double *
  * replaced with abx_particles_set_positions (same n, current storage order). */
 ABX_API int abx_particles_set_positions(abx_particles *p, const double *pos);
 ABX_API int abx_particles_update_positions(abx_particles *p);
+/* Particles::push_back (src/Particles.h:264-311): append n_new particles (AoS
+ * positions) with the next ids (written to ids_out when not NULL); on a
+ * searchable set the search structure is updated at once (the reference
+ * updates an ordered search after every push_back). */
+ABX_API int abx_particles_push_back(abx_particles *p, int64_t n_new, const double *pos,
+                                    int64_t *ids_out);
+/* Particles::erase(first, last) (src/Particles.h:361-389): the particles at
+ * storage positions [first, last) are marked dead and the search structure is
+ * updated, which drops them (without a search structure they are removed and
+ * the rest keep their order). */
+ABX_API int abx_particles_erase(abx_particles *p, int64_t first, int64_t last);
+/* Find-by-id (NeighbourSearchBase::find_id_map and find,
+ * src/NeighbourSearchBase.h:276-321, 720): the storage index of every id in
+ * ids[nq] (host or device memory), -1 for an id not in the set.  The id map
+ * (ids sorted, with their storage index) is built on the device on first use
+ * after the particles changed. */
+ABX_API int abx_particles_find_ids(abx_particles *p, int64_t nq, const int64_t *ids,
+                                   int64_t *index_out);
 /* Particles<..., HyperOctree>::init_neighbour_search (src/OctTree.h:168-226):
  * domain enforcement as above, then storage reordered by octree tag
  * (src/detail/SpatialUtil.h:255-286, stable) and the tree built level by level

@@ -80,6 +80,27 @@ static int run(const char *in, const std::string &out) {
   write(out + "/counts.bin", counts);
   write(out + "/lists.bin", lists);
 
+  {
+    // push_back / find-by-id / erase on the searchable set (src/Particles.h:
+    // 264-389, src/NeighbourSearchBase.h:276-321); the copy keeps the set
+    // used below unchanged
+    Cells3 edit;
+    for (int64_t i = 0; i < n; ++i)
+      edit.push_back(vdouble3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]));
+    edit.init_neighbour_search(vdouble3(0, 0, 0), vdouble3(1, 1, 1), vbool3(false, false, false));
+    edit.push_back(vdouble3(0.123, 0.456, 0.789));
+    const int64_t new_id = n;  // ids run 0..n-1 for the first n particles
+    const size_t at = edit.find(new_id);
+    const auto &xp = get<position>(edit)[at];
+    std::vector<double> res = {double(edit.size()), double(at < edit.size()),
+                               xp[0], xp[1], xp[2]};
+    edit.erase(at);
+    res.push_back(double(edit.size()));
+    res.push_back(double(edit.find(new_id) == edit.size()));
+    res.push_back(double(edit.find(7) < edit.size() && get<id>(edit)[edit.find(7)] == 7));
+    write(out + "/edit.bin", res);
+  }
+
   // tests/operators.h pattern: K = create_sparse_operator(...); c = K * b
   std::vector<double> bs(static_cast<size_t>(n));
   for (int64_t i = 0; i < n; ++i) bs[size_t(i)] = b[size_t(ids[size_t(i)])];

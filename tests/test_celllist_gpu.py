@@ -117,3 +117,50 @@ def test_grid_hysteresis_after_deletion(frac_deleted, keeps_grid):
     assert np.array_equal(bb, cl.begin) and np.array_equal(be, cl.end)
     counts = ab.radius_count(p, p.positions, 0.05)
     assert np.array_equal(counts, oracle.radius_count(cl, cl.pos, 0.05))
+
+
+def test_push_back_erase_and_find_by_id():
+    """push_back / erase on a searchable set update the search structure at
+    once (src/Particles.h:264-311, 361-389): the new order equals the oracle's
+    build over the storage order before the update plus the new particles,
+    with the grid kept within the 2x band (src/CellListOrdered.h:133-136).
+    find-by-id (src/NeighbourSearchBase.h:276-321) maps ids to storage
+    positions, -1 for erased ids."""
+    n = 60000
+    rng = np.random.default_rng(20)
+    p = ab.Particles(3).set(workloads.uniform(n, 3, seed=21))
+    p.init_neighbour_search([0] * 3, [1] * 3, [True] * 3)
+    before_pos, before_ids = p.positions, p.ids
+    extra = rng.uniform(-0.2, 1.2, size=(5000, 3))  # outside coordinates wrap
+    new_ids = p.push_back(extra)
+    assert np.array_equal(new_ids, np.arange(n, n + 5000))
+    allpos = np.concatenate([before_pos, extra])
+    allids = np.concatenate([before_ids, new_ids])
+    cl = oracle.celllist_build(allpos, [0] * 3, [1] * 3, [True] * 3, prev_grid_n=n)
+    assert np.array_equal(p.ids, allids[cl.perm])
+    assert np.array_equal(p.positions, cl.pos)
+    bb, be, keys = p.buckets()
+    assert np.array_equal(keys, cl.keys) and np.array_equal(bb, cl.begin)
+    # erase a storage range
+    pos2, ids2 = p.positions, p.ids
+    p.erase(1000, 4000)
+    keep = np.r_[0:1000, 4000:len(ids2)]
+    cl2 = oracle.celllist_build(pos2[keep], [0] * 3, [1] * 3, [True] * 3, prev_grid_n=n)
+    assert np.array_equal(p.ids, ids2[keep][cl2.perm])
+    assert np.array_equal(p.positions, cl2.pos)
+    # find by id: present ids map to their storage index, erased ones to -1
+    q = np.concatenate([rng.choice(p.ids, 3000), ids2[1000:1100], [-5, 10 ** 12]])
+    idx = p.find_ids(q)
+    ids_now = p.ids
+    assert np.all(ids_now[idx[:3000]] == q[:3000])
+    assert np.all(idx[3000:] == -1)
+    counts = ab.radius_count(p, p.positions, 0.05)
+    assert np.array_equal(counts, oracle.radius_count(cl2, cl2.pos, 0.05))
+
+
+def test_erase_without_search_keeps_order():
+    p = ab.Particles(2).set(workloads.uniform(100, 2, seed=22))
+    ids = p.ids
+    p.erase(10, 20)
+    assert np.array_equal(p.ids, np.r_[ids[:10], ids[20:]])
+    assert np.array_equal(p.find_ids(ids[:30]), np.r_[np.arange(10), [-1] * 10, np.arange(10, 20)])

@@ -92,6 +92,11 @@ def test_cpp_api_parity(tmp_path):
         assert np.array_equal(np.sort(lists[off[k]:off[k + 1]]),
                               np.sort(cols[rowptr[k]:rowptr[k + 1]]))
 
+    edit = np.fromfile(out / "edit.bin", np.float64)
+    assert edit[0] == n + 1 and edit[1] == 1
+    assert np.array_equal(edit[2:5], [0.123, 0.456, 0.789])
+    assert edit[5] == n and edit[6] == 1 and edit[7] == 1
+
     bs = b[cl.perm]
     ref = oracle.sparse_matvec(cl, cl.pos, r, 1, [1.0 / (r / 2) ** 2], bs)
     kb = np.fromfile(out / "kb.bin", np.float64)
