@@ -29,7 +29,7 @@ __all__ = [
     "K_MULTIQUADRIC", "K_SCALAR_SUM", "default_context", "Preconditioner",
     "schwarz_preconditioner", "spai_preconditioner", "gmres", "knn", "spai_exact_rows", "MLP",
     "spai_features", "learned_preconditioner", "spai_local_inverse_rows", "create_fmm_operator", "fmm_stats", "spai_rows", "gmres_with_fallback",
-    "fp32_peak_tflops", "fmm_set_wait_limit",
+    "fp32_peak_tflops", "fmm_set_wait_limit", "create_h2_operator",
 ]
 
 PREC_FP64, PREC_MIXED = 0, 1
@@ -582,6 +582,16 @@ def create_fmm_operator(p: Particles, kernel: Kernel, order: int = 3,
     h = C.c_void_p()
     _check(lib().abx_create_fmm_operator(p._h, C.byref(kernel), int(order), C.byref(h)),
            "abx_create_fmm_operator")
+    return Operator(h, p, p).set_precision(precision)
+
+
+def create_h2_operator(p: Particles, kernel: Kernel, order: int = 3, eta: float = 1.0,
+                       precision: int = PREC_FP64) -> Operator:
+    """``create_h2_operator`` on an octree particle set: the black-box H2
+    operator with runtime Chebyshev order and admissibility parameter eta."""
+    h = C.c_void_p()
+    _check(lib().abx_create_h2_operator(p._h, C.byref(kernel), int(order), float(eta),
+                                        C.byref(h)), "abx_create_h2_operator")
     return Operator(h, p, p).set_precision(precision)
 
 

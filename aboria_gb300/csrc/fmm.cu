@@ -1177,7 +1177,10 @@ __global__ void k_m2l_mats(int D, int n, int ncheb, const double *__restrict__ m
 }  // namespace
 
 // ----------------------------------------------------------- plan build ---
-int fmm_plan_build(abx_operator *op, int order, FmmPlan *&out) {
+// eta scales the admissibility of a box pair: it is near (P2P or further
+// refinement) iff (max diameter)^2 > eta^2 (box distance)^2; eta = 1 is the
+// reference FMM's theta_condition (src/detail/FastMultipoleMethod.h:1249-1279).
+int fmm_plan_build(abx_operator *op, int order, FmmPlan *&out, double eta = 1.0) {
   abx_particles *p = op->rows;
   abx_context *ctx = p->ctx;
   cudaStream_t s = ctx->stream;
@@ -1218,6 +1221,7 @@ int fmm_plan_build(abx_operator *op, int order, FmmPlan *&out) {
     }
   }
   // ---- traversal (host): M2L pairs and P2P connectivity
+  const double eta2 = eta * eta;
   auto near = [&](int t, int sdx) {
     double maxd = std::numeric_limits<double>::min();
     for (int d = 0; d < D; ++d) maxd = std::max(maxd, boxes[t * 6 + 3 + d] - boxes[t * 6 + d]);
@@ -1231,7 +1235,7 @@ int fmm_plan_build(abx_operator *op, int order, FmmPlan *&out) {
       maxd = std::max(maxd, shi - slo);
       dist2 += dd * dd;
     }
-    return maxd * maxd > dist2;
+    return maxd * maxd > eta2 * dist2;
   };
   std::vector<std::array<int, 2>> m2l;
   std::vector<std::vector<int>> p2p_of(NN);
@@ -1634,6 +1638,33 @@ extern "C" int abx_create_fmm_operator(abx_particles *p, const abx_kernel *k, in
   op->k = *k;
   FmmPlan *P = nullptr;
   const int st = fmm_plan_build(op, order, P);
+  if (st != ABX_OK) {
+    delete op;
+    return st;
+  }
+  op->fmm = P;
+  particles_retain(p);
+  particles_retain(p);
+  *out = op;
+  return ABX_OK;
+}
+
+extern "C" int abx_create_h2_operator(abx_particles *p, const abx_kernel *k, int order,
+                                      double eta, abx_operator **out) {
+  ABX_REQUIRE(p && k && out, ABX_ERR_INVALID, "null argument");
+  ABX_REQUIRE(eta > 0.0 && std::isfinite(eta), ABX_ERR_INVALID, "eta must be positive");
+  ABX_REQUIRE(k->kind == ABX_K_LAPLACE || k->kind == ABX_K_GAUSSIAN ||
+                  k->kind == ABX_K_COMPACT_GAUSSIAN || k->kind == ABX_K_MULTIQUADRIC ||
+                  k->kind == ABX_K_CONST,
+              ABX_ERR_INVALID, "H2: kernel kind %d not supported", k->kind);
+  ABX_TRY(ctx_activate(p->ctx));
+  abx_operator *op = new abx_operator();
+  op->kind = 2;
+  op->rows = p;
+  op->cols = p;
+  op->k = *k;
+  FmmPlan *P = nullptr;
+  const int st = fmm_plan_build(op, order, P, eta);
   if (st != ABX_OK) {
     delete op;
     return st;

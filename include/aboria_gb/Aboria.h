@@ -730,6 +730,22 @@ BlockOperator<NI, NJ, Ops...> create_block_operator(const Ops &...ops) {
   return BlockOperator<NI, NJ, Ops...>(ops...);
 }
 
+/* create_h2_operator(rows, cols, order, kernel, eta) (src/Operators.h:440-447):
+ * the black-box H2 operator with a runtime Chebyshev order and the
+ * admissibility parameter eta on the HyperOctree of one particle set. */
+template <typename RowP, typename ColP>
+Operator create_h2_operator(const RowP &row_particles, const ColP &col_particles, int order,
+                            const abx_kernel &kernel, double eta = 1.0) {
+  if (row_particles.handle() != col_particles.handle()) {
+    detail::check(ABX_ERR_INVALID, "create_h2_operator: rows and cols must be one particle set");
+    return Operator();
+  }
+  abx_operator *h = nullptr;
+  detail::check(abx_create_h2_operator(row_particles.handle(), &kernel, order, eta, &h),
+                "create_h2_operator");
+  return Operator(h);
+}
+
 /* -------------------------------------------------------------- solvers ---- */
 /* SchwartzPreconditioner<Solver> (src/Preconditioners.h:1121-1537): domains
  * are the octree leaves of the operator's particle set; blocks are factorised

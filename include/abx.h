@@ -219,6 +219,18 @@ ABX_API int abx_create_dense_operator(abx_particles *rows, abx_particles *cols, 
  * P2P in FP32. */
 ABX_API int abx_create_fmm_operator(abx_particles *p, const abx_kernel *k, int order,
                                     abx_operator **out);
+/* create_h2_operator(particles, particles, order, kernel, eta)
+ * (src/Operators.h:440-447; H2Matrix / make_h2_matrix, src/H2Matrix.h:46-110,
+ * src/ParH2Matrix.h:564-570): the black-box Chebyshev H2 operator with a
+ * runtime order and the admissibility parameter eta -- a box pair is far
+ * (M2L) unless (max diameter)^2 > eta^2 (distance)^2, eta = 1 being the FMM's
+ * rule.  The plan (tree traversal, M2L and child interpolation matrices, the
+ * split-TF32 M2L images) is built once and reused by every K*b; the leaf
+ * expansions and the near-field blocks are evaluated on the fly, which on the
+ * GPU is cheaper than reading stored blocks from memory.  Matvec precision
+ * and kernels as for abx_create_fmm_operator. */
+ABX_API int abx_create_h2_operator(abx_particles *p, const abx_kernel *k, int order, double eta,
+                                   abx_operator **out);
 ABX_API int abx_fmm_stats(abx_operator *op, int64_t *m2l_pairs, int64_t *matrices,
                           int64_t *leaves, double *plan_seconds);
 /* Limit of every device-side wait of the tensor-core M2L (its pipeline's
