@@ -1220,138 +1220,79 @@ int fmm_plan_build(abx_operator *op, int order, FmmPlan *&out, double eta = 1.0)
       boxes[nd * 6 + 3 + d] = d < D ? hi[d] : 1.0;
     }
   }
-  // ---- traversal (host): M2L pairs and P2P connectivity
-  const double eta2 = eta * eta;
-  auto near = [&](int t, int sdx) {
-    double maxd = std::numeric_limits<double>::min();
-    for (int d = 0; d < D; ++d) maxd = std::max(maxd, boxes[t * 6 + 3 + d] - boxes[t * 6 + d]);
-    double dist2 = 0.0;
-    for (int d = 0; d < D; ++d) {
-      double dd = 0.0;
-      const double tlo = boxes[t * 6 + d], thi = boxes[t * 6 + 3 + d];
-      const double slo = boxes[sdx * 6 + d], shi = boxes[sdx * 6 + 3 + d];
-      if (thi < slo) dd = slo - thi;
-      else if (shi < tlo) dd = tlo - shi;
-      maxd = std::max(maxd, shi - slo);
-      dist2 += dd * dd;
+  // ---- traversal on the device: M2L pairs grouped by matrix key, P2P lists
+  DevBuf<double> boxes_d;
+  if (int e = boxes_d.reserve(boxes.size() + 1)) {
+    delete P;
+    return e;
+  }
+  if (!boxes.empty())
+    cudaMemcpyAsync(boxes_d.ptr, boxes.data(), boxes.size() * 8, cudaMemcpyHostToDevice, s);
+  FmmLists lists;
+  if (NN > 1) {
+    const int e = fmm_traverse_device(p, boxes_d.ptr, eta, lists);
+    if (e != ABX_OK) {
+      delete P;
+      return e;
     }
-    return maxd * maxd > eta2 * dist2;
-  };
-  std::vector<std::array<int, 2>> m2l;
-  std::vector<std::vector<int>> p2p_of(NN);
+  } else {
+    lists.mat_off.assign(1, 0);
+  }
+  // ---- links by level, octant-major (M2M bottom-up uses deepest first)
   std::vector<std::array<int, 3>> links;  // parent, child, octant
-  std::function<void(int, std::vector<int> &)> leaves_of = [&](int nd, std::vector<int> &o) {
-    if (T.kind[nd] == 1) { o.push_back(nd); return; }
-    if (T.kind[nd] == 0) return;
-    for (int c = 0; c < P->nchild; ++c) leaves_of(T.first_child[nd] + c, o);
-  };
-  std::function<void(int, const std::vector<int> &, int)> down = [&](int t, const std::vector<int> &cp,
-                                                                    int parent) {
-    std::vector<int> conn;
-    if (parent < 0) {
-      for (int c = 0; c < P->nchild; ++c) {
-        const int sdx = T.first_child[0] + c;
-        if (T.kind[sdx] == 0) continue;
-        if (near(t, sdx)) conn.push_back(sdx); else m2l.push_back({t, sdx});
-      }
-    } else {
-      for (int sdx : cp) {
-        if (T.kind[sdx] == 1) { conn.push_back(sdx); continue; }
-        for (int c = 0; c < P->nchild; ++c) {
-          const int ch = T.first_child[sdx] + c;
-          if (T.kind[ch] == 0) continue;
-          if (near(t, ch)) conn.push_back(ch); else m2l.push_back({t, ch});
-        }
-      }
-    }
-    if (T.kind[t] == 2) {
-      for (int c = 0; c < P->nchild; ++c) {
-        const int ch = T.first_child[t] + c;
-        if (T.kind[ch] == 0) continue;
-        links.push_back({t, ch, c});
-        down(ch, conn, t);
-      }
-    } else {
-      for (int sdx : conn) leaves_of(sdx, p2p_of[t]);
-    }
-  };
-  std::vector<int> none;
-  if (NN > 1)
-    for (int c = 0; c < P->nchild; ++c) {
-      const int t = T.first_child[0] + c;
-      if (T.kind[t] != 0) down(t, none, -1);
-    }
-  // ---- links by level (M2M bottom-up uses deepest first)
   int maxlev = 0;
-  for (auto &l : links) maxlev = std::max(maxlev, T.level[l[1]]);
+  {
+    const OctDev &O = p->oct;
+    for (size_t L = 1; L < O.lvl_base.size(); ++L)
+      for (int c = 0; c < O.lvl_count[L]; ++c) {
+        const int t = O.lvl_base[L] + c;
+        if (T.kind[t] == 0) continue;
+        links.push_back({T.parent[t], t, c % P->nchild});
+        maxlev = std::max(maxlev, (int)L);
+      }
+  }
   std::vector<int> flat;
   std::vector<int2> batches;
   P->batch_off.assign(maxlev + 2, 0);
   P->batch_cnt.assign(maxlev + 2, 0);
-  for (int lev = 1; lev <= maxlev; ++lev) {
-    P->batch_off[lev] = (int)batches.size();
-    // octant-major within the level: batches of <= NBL links share a matrix
-    for (int o = 0; o < P->nchild; ++o) {
-      int run = 0;
-      for (auto &l : links)
-        if (T.level[l[1]] == lev && l[2] == o) {
+  {
+    std::vector<std::vector<std::vector<int>>> by(maxlev + 1,
+                                                  std::vector<std::vector<int>>(P->nchild));
+    for (size_t q = 0; q < links.size(); ++q)
+      by[T.level[links[q][1]]][links[q][2]].push_back((int)q);
+    for (int lev = 1; lev <= maxlev; ++lev) {
+      P->batch_off[lev] = (int)batches.size();
+      // octant-major within the level: batches of <= NBL links share a matrix
+      for (int o = 0; o < P->nchild; ++o) {
+        int run = 0;
+        for (int q : by[lev][o]) {
           const int idx = (int)(flat.size() / 3);
           if (run == 0) batches.push_back(make_int2(idx, 0));
           ++batches.back().y;
           run = (run + 1) % NBL;
-          flat.push_back(l[0]);
-          flat.push_back(l[1]);
-          flat.push_back(l[2]);
+          flat.push_back(links[q][0]);
+          flat.push_back(links[q][1]);
+          flat.push_back(links[q][2]);
         }
+      }
+      P->batch_cnt[lev] = (int)batches.size() - P->batch_off[lev];
     }
-    P->batch_cnt[lev] = (int)batches.size() - P->batch_off[lev];
   }
-  // ---- M2L matrices keyed by (level, offset)
-  std::map<std::array<long long, 4>, int> matid;
+  // ---- M2L matrices: (level, offset) keys from the traversal, the box size
+  // of a representative target
   std::vector<double> mdesc;
-  std::vector<int> trip;
-  for (auto &pr : m2l) {
-    const int t = pr[0], sdx = pr[1];
-    std::array<long long, 4> key{T.level[t], 0, 0, 0};
-    double hbox[3] = {1, 1, 1}, off[3] = {0, 0, 0};
-    for (int d = 0; d < D; ++d) {
-      hbox[d] = boxes[t * 6 + 3 + d] - boxes[t * 6 + d];
-      off[d] = boxes[sdx * 6 + d] - boxes[t * 6 + d];
-      key[1 + d] = std::llround(off[d] / hbox[d]);
-    }
-    auto it = matid.find(key);
-    int id;
-    if (it == matid.end()) {
-      id = (int)matid.size();
-      matid[key] = id;
-      for (int d = 0; d < 3; ++d) mdesc.push_back(hbox[d]);
-      for (int d = 0; d < 3; ++d) mdesc.push_back(d < D ? key[1 + d] * hbox[d] : 0.0);
-    } else {
-      id = it->second;
-    }
-    trip.push_back(t);
-    trip.push_back(sdx);
-    trip.push_back(id);
-  }
-  P->nmat = (int)matid.size();
-  P->n_m2l = (int)m2l.size();
-  // grouped by matrix for the tensor-core path
-  std::vector<std::vector<int2>> bym(P->nmat);
-  for (size_t q = 0; q < m2l.size(); ++q) bym[trip[3 * q + 2]].push_back(make_int2(trip[3 * q], trip[3 * q + 1]));
-  std::vector<int2> bymat;
-  P->mat_off.assign(P->nmat + 1, 0);
+  P->nmat = (int)lists.mat_key.size();
+  P->n_m2l = (int)lists.n_m2l;
   for (int m = 0; m < P->nmat; ++m) {
-    P->mat_off[m] = (int)bymat.size();
-    bymat.insert(bymat.end(), bym[m].begin(), bym[m].end());
+    const int t = lists.mat_rep[m];
+    double hbox[3] = {1, 1, 1};
+    for (int d = 0; d < D; ++d) hbox[d] = boxes[t * 6 + 3 + d] - boxes[t * 6 + d];
+    for (int d = 0; d < 3; ++d) mdesc.push_back(hbox[d]);
+    for (int d = 0; d < 3; ++d)
+      mdesc.push_back(d < D ? (double)lists.mat_key[m][1 + d] * hbox[d] : 0.0);
   }
-  P->mat_off[P->nmat] = (int)bymat.size();
-  // ---- P2P CSR over leaves
+  P->mat_off = lists.mat_off;
   std::vector<int> leaves = T.leaves;
-  std::vector<int> rp(1, 0), srcs;
-  for (int lf : leaves) {
-    for (int sl : p2p_of[lf]) srcs.push_back(sl);
-    rp.push_back((int)srcs.size());
-  }
   P->nleaves = (int)leaves.size();
   // ---- child interpolation matrices Tc[o][i][j] = R_i(node j of child o; parent box)
   std::vector<double> Tc((size_t)P->nchild * nc * nc);
@@ -1386,17 +1327,30 @@ int fmm_plan_build(abx_operator *op, int order, FmmPlan *&out, double eta = 1.0)
       (st = P->leaf_ids.reserve(leaves.size() + 1)) || (st = P->node_begin.reserve(NN)) ||
       (st = P->node_end.reserve(NN)) || (st = P->links.reserve(flat.size() + 1)) ||
       (st = P->batches.reserve(batches.size() + 1)) || (st = P->TcT.reserve(Tc.size())) ||
-      (st = P->m2l.reserve(trip.size() + 1)) ||
       (st = P->Km.reserve((size_t)std::max(1, P->nmat) * nc * nc)) ||
-      (st = P->p2p_rowptr.reserve(rp.size())) || (st = P->p2p_src.reserve(srcs.size() + 1)) ||
-      (st = P->m2l_by_mat.reserve(bymat.size() + 1)) || (st = P->mat_off_d.reserve(P->nmat + 1)))
+      (st = P->mat_off_d.reserve(P->nmat + 1)))
     return fail(st);
+  // the traversal's device lists move into the plan
+  auto take = [](auto &dst, auto &src) {
+    std::swap(dst.ptr, src.ptr);
+    std::swap(dst.cap, src.cap);
+  };
+  take(P->m2l, lists.m2l_trip);
+  take(P->m2l_by_mat, lists.m2l_by_mat);
+  take(P->p2p_rowptr, lists.p2p_rowptr);
+  take(P->p2p_src, lists.p2p_src);
+  if ((st = P->m2l.reserve(1)) || (st = P->m2l_by_mat.reserve(1)) ||
+      (st = P->p2p_rowptr.reserve(1)) || (st = P->p2p_src.reserve(1)))
+    return fail(st);
+  if (NN <= 1) {
+    const int zero = 0;
+    cudaMemcpyAsync(P->p2p_rowptr.ptr, &zero, 4, cudaMemcpyHostToDevice, s);
+  }
   DevBuf<double> md_d;
   if ((st = P->mi_d.reserve(P->mi.size())) || (st = md_d.reserve(mdesc.size() + 1))) return fail(st);
-  // tensor-core M2L tiles: 64 pairs of one matrix each
-  std::vector<int> tmat, tfirst;
   // tensor-core M2L tiles: 64 pairs for the mma.sync kernel (<= 64 nodes),
-  // t5_pairs pairs for the tcgen05 kernel
+  // t5_pairs pairs for the tcgen05 kernel, of one matrix each
+  std::vector<int> tmat, tfirst;
   const int tile_pairs = nc <= 64 ? TC_PAIRS : t5_pairs((nc + 127) / 128);
   for (int m = 0; m < P->nmat; ++m)
     for (int q = P->mat_off[m]; q < P->mat_off[m + 1]; q += tile_pairs) {
@@ -1419,10 +1373,6 @@ int fmm_plan_build(abx_operator *op, int order, FmmPlan *&out, double eta = 1.0)
   up(P->node_end.ptr, ne.data(), ne.size() * 4);
   up(P->links.ptr, flat.data(), flat.size() * 4);
   up(P->batches.ptr, batches.data(), batches.size() * sizeof(int2));
-  up(P->m2l.ptr, trip.data(), trip.size() * 4);
-  up(P->p2p_rowptr.ptr, rp.data(), rp.size() * 4);
-  up(P->p2p_src.ptr, srcs.data(), srcs.size() * 4);
-  up(P->m2l_by_mat.ptr, bymat.data(), bymat.size() * sizeof(int2));
   up(P->mat_off_d.ptr, P->mat_off.data(), P->mat_off.size() * 4);
   up(P->mi_d.ptr, P->mi.data(), P->mi.size() * 4);
   up(P->tile_mat.ptr, tmat.data(), tmat.size() * 4);

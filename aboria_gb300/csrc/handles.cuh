@@ -2,6 +2,8 @@
 // operators with their pair layout.
 #pragma once
 
+#include <array>
+
 #include "common.cuh"
 
 namespace abx {
@@ -40,6 +42,33 @@ struct OctTree {
   void box(const GridDesc &g, int node, double *lo, double *hi) const;
 };
 
+// The octree's node arrays on the device (octree.cu), levels as node-id
+// ranges: level L holds nodes [lvl_base[L], lvl_base[L] + lvl_count[L]).
+struct OctDev {
+  DevBuf<int> tag, level, begin, end, kind, first_child, parent, leaves;
+  int cap = 0, nnodes = 0, nleaves = 0, max_level = 0;
+  std::vector<int> lvl_base, lvl_count;
+  void reset() {
+    DevBuf<int> *a[8] = {&tag, &level, &begin, &end, &kind, &first_child, &parent, &leaves};
+    for (DevBuf<int> *b : a) b->release();
+    cap = nnodes = nleaves = max_level = 0;
+    lvl_base.clear();
+    lvl_count.clear();
+  }
+};
+
+// The FMM plan's lists built on the device (octree.cu): M2L pairs grouped by
+// matrix key (level, integer box offset), and the leaves' P2P sources.
+struct FmmLists {
+  DevBuf<int2> m2l_by_mat;          // (target, source), grouped by matrix
+  DevBuf<int> m2l_trip;             // (target, source, matrix) in the same order
+  DevBuf<int> p2p_rowptr, p2p_src;  // CSR over the leaves (creation order)
+  std::vector<int> mat_off;         // nmat + 1
+  std::vector<std::array<int, 4>> mat_key;  // level, offset (in boxes) per dimension
+  std::vector<int> mat_rep;         // a target node of each matrix
+  int64_t n_m2l = 0;
+};
+
 }  // namespace abx
 
 struct abx_particles {
@@ -76,6 +105,7 @@ struct abx_particles {
   uint32_t cl_epoch = 0;
   // find-by-id map (NeighbourSearchBase::find_id_map): ids sorted, with the
   // storage index of each; rebuilt when the storage version moved
+  abx::OctDev oct;  // the octree on the device (search_kind 1)
   abx::DevBuf<int64_t> idmap_key;
   abx::DevBuf<uint32_t> idmap_val;
   uint64_t idmap_version = ~uint64_t(0);
@@ -124,6 +154,10 @@ void particles_release(abx_particles *p);
 int particles_grid_desc(const abx_particles *p, GridDesc *g);
 // celllist.cu: the CellListOrdered build of the alive particles (n > 0)
 int celllist_build(abx_particles *p);
+// octree.cu: the HyperOctree from the sorted tags (device and host copies),
+// and the FMM traversal lists
+int octree_build_device(abx_particles *p, const uint32_t *tags, int64_t na);
+int fmm_traverse_device(abx_particles *p, const double *boxes, double eta, FmmLists &out);
 // pairs.cu
 int pair_layout_build(abx_operator *op);
 void pair_layout_free(PairLayout *L);

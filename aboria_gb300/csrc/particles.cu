@@ -327,7 +327,10 @@ int update_positions(abx_particles *p) {
   p->searchable = false;
   ++p->version;
   if (n == 0) {
-    if (p->search_kind == 1) build_octree(p, std::vector<int>());
+    if (p->search_kind == 1) {
+      p->oct.reset();
+      build_octree(p, std::vector<int>());
+    }
     set_domain_impl(p, 0);
     p->n_alive_prev = 0;
     ABX_TRY(p->bucket_begin.reserve(p->grid.ncells));
@@ -392,11 +395,12 @@ int update_positions(abx_particles *p) {
       ABX_CHECK_CUDA(cudaGetLastError());
       ABX_TRY(radix_sort_pairs(keys, vals, na, max_level * D, keys_alt, vals_alt, rtmp, s));
     }
-    std::vector<int> tags(na);
-    if (na > 0)
-      ABX_CHECK_CUDA(cudaMemcpyAsync(tags.data(), keys, na * 4, cudaMemcpyDeviceToHost, s));
-    ABX_CHECK_CUDA(cudaStreamSynchronize(s));
-    build_octree(p, tags);
+    if (na > 0) {
+      ABX_TRY(octree_build_device(p, keys, na));
+    } else {
+      p->oct.reset();
+      build_octree(p, std::vector<int>());
+    }
   } else {
   set_domain_impl(p, (size_t)na);
   g = p->grid;
