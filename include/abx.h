@@ -223,8 +223,8 @@ ABX_API int abx_create_fmm_operator(abx_particles *p, const abx_kernel *k, int o
  * (src/Operators.h:440-447; H2Matrix / make_h2_matrix, src/H2Matrix.h:46-110,
  * src/ParH2Matrix.h:564-570): the black-box Chebyshev H2 operator with a
  * runtime order and the admissibility parameter eta -- a box pair is far
- * (M2L) unless (max diameter)^2 > eta^2 (distance)^2, eta = 1 being the FMM's
- * rule.  The plan (tree traversal, M2L and child interpolation matrices, the
+ * (M2L) when its gap is at least (max diameter) / eta, eta = 1 being the
+ * FMM's rule; a smaller eta keeps more pairs near and is more accurate.  The plan (tree traversal, M2L and child interpolation matrices, the
  * split-TF32 M2L images) is built once and reused by every K*b; the leaf
  * expansions and the near-field blocks are evaluated on the fly, which on the
  * GPU is cheaper than reading stored blocks from memory.  Matvec precision
