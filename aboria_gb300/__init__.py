@@ -365,8 +365,12 @@ class Preconditioner:
         t = C.c_double()
         _check(lib().abx_precond_stats(self._h, C.byref(nd), C.byref(ms), C.byref(el), C.byref(t)),
                "abx_precond_stats")
+        ph = [C.c_double() for _ in range(4)]
+        _check(lib().abx_precond_setup_phases(self._h, *[C.byref(x) for x in ph]),
+               "abx_precond_setup_phases")
         return {"domains": nd.value, "max_size": ms.value, "elements": el.value,
-                "setup_s": t.value}
+                "setup_s": t.value, "knn_s": ph[0].value, "features_s": ph[1].value,
+                "infer_s": ph[2].value, "exact_rows_s": ph[3].value}
 
 
 def schwarz_preconditioner(op: Operator, precision: int = PREC_FP64) -> Preconditioner:

@@ -145,6 +145,9 @@ struct abx_precond {
   int64_t n = 0;
   int64_t exact_rows = 0;  // learned approximate inverse: rows solved exactly
   double setup_s = 0.0;    // approximate inverses: set-up time
+  // learned approximate inverse: device time of the set-up phases (k-NN,
+  // features, inference, exact rows), from CUDA events on the build stream
+  double phase_s[4] = {0.0, 0.0, 0.0, 0.0};
   abx::HostStage stage_b, stage_x;
 };
 

@@ -768,6 +768,15 @@ int abx_precond_apply(abx_precond *pc, const double *b, double *x) {
   return ABX_OK;
 }
 
+int abx_precond_setup_phases(abx_precond *pc, double *knn_s, double *features_s, double *infer_s,
+                             double *exact_s) {
+  ABX_REQUIRE(pc, ABX_ERR_INVALID, "null preconditioner");
+  double *out[4] = {knn_s, features_s, infer_s, exact_s};
+  for (int i = 0; i < 4; ++i)
+    if (out[i]) *out[i] = pc->phase_s[i];
+  return ABX_OK;
+}
+
 int abx_precond_stats(abx_precond *pc, int64_t *ndomains, int64_t *max_size, int64_t *elements,
                       double *setup_seconds) {
   ABX_REQUIRE(pc, ABX_ERR_INVALID, "null preconditioner");

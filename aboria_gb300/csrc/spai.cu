@@ -333,6 +333,35 @@ int self_csr_device(abx_particles *p, double r, DevBuf<int64_t> &rowptr, DevBuf<
                     int64_t &nnz);
 int knn_device(abx_particles *p, int k, int32_t *idx, double *d2);
 
+namespace {
+// Events at the boundaries of the learned preconditioner's set-up phases.
+// Timing is best effort: if an event cannot be created the phases read 0.
+struct PhaseEvents {
+  cudaStream_t s;
+  cudaEvent_t e[5] = {};
+  bool ok = true;
+  explicit PhaseEvents(cudaStream_t st) : s(st) {
+    for (auto &x : e) ok = ok && cudaEventCreate(&x) == cudaSuccess;
+  }
+  ~PhaseEvents() {
+    for (auto &x : e)
+      if (x) cudaEventDestroy(x);
+  }
+  void mark(int i) {
+    if (ok) ok = cudaEventRecord(e[i], s) == cudaSuccess;
+  }
+  // after the stream has been synchronised past mark(4)
+  void elapsed(double out[4]) {
+    for (int i = 0; i < 4; ++i) {
+      float ms = 0.0f;
+      const bool got = ok && cudaEventElapsedTime(&ms, e[i], e[i + 1]) == cudaSuccess;
+      if (ok && !got) cudaGetLastError();  // the timing's own error, not the caller's
+      out[i] = got ? 1e-3 * ms : 0.0;
+    }
+  }
+};
+}  // namespace
+
 // subset (device, nsub rows) restricts the solve to those rows; knn_given
 // says cols_out already holds the k-nearest-neighbour supports.
 int spai_exact_rows(abx_operator *op, int k, int32_t *cols_out, double *vals_out, int local,
@@ -494,6 +523,7 @@ __global__ void k_f2d_masked(const float *__restrict__ y, const int32_t *__restr
 
 int knn_device(abx_particles *p, int k, int32_t *idx, double *d2);
 
+
 int spai_features_device(abx_particles *p, const int32_t *knn, int k, double eps, float *feats) {
   const int64_t n = p->n;
   if (n == 0) return ABX_OK;
@@ -544,15 +574,16 @@ extern "C" int abx_precond_create_learned(abx_operator *op, abx_mlp *mlp, double
   const auto t0 = std::chrono::steady_clock::now();
   DevBuf<float> feats, y;
   DevBuf<double> d2;
+  PhaseEvents ev(p->ctx->stream);
   if ((st = S->cols.reserve((size_t)n * k + 1)) || (st = S->vals.reserve((size_t)n * k + 1)) ||
       (st = feats.reserve((size_t)n * k * p->dim + 1)) || (st = y.reserve((size_t)n * k + 1)) ||
       (st = d2.reserve((size_t)n * k + 1)) ||
-      (n > 0 && ((st = knn_device(p, k, S->cols.ptr, d2.ptr)) ||
-                 (st = spai_features_device(p, S->cols.ptr, k, eps, feats.ptr)) ||
+      (n > 0 && ((ev.mark(0), st = knn_device(p, k, S->cols.ptr, d2.ptr)) ||
+                 (ev.mark(1), st = spai_features_device(p, S->cols.ptr, k, eps, feats.ptr)) ||
                  // the model may live on another context (stream) of the same
                  // device: order its inference after the features and the
                  // weights' use after the inference
-                 (st = stream_order(p->ctx->stream, mlp_context(mlp)->stream)) ||
+                 (ev.mark(2), st = stream_order(p->ctx->stream, mlp_context(mlp)->stream)) ||
                  (st = precision == ABX_PREC_FP64
                            ? mlp_infer_fp32(mlp, feats.ptr, n, y.ptr)
                            : mlp_infer_bf16(mlp, feats.ptr, n, y.ptr)) ||
@@ -561,6 +592,7 @@ extern "C" int abx_precond_create_learned(abx_operator *op, abx_mlp *mlp, double
     delete pc;
     return st;
   }
+  if (n > 0) ev.mark(3);
   if (n > 0) {
     k_f2d_masked<<<ceil_div((size_t)n * k, 256), 256, 0, p->ctx->stream>>>(y.ptr, S->cols.ptr,
                                                                           (size_t)n * k,
@@ -596,6 +628,8 @@ extern "C" int abx_precond_create_learned(abx_operator *op, abx_mlp *mlp, double
       return ABX_ERR_CUDA;
     }
     pc->exact_rows = nexact;
+    ev.mark(4);
+    ev.elapsed(pc->phase_s);
   }
   pc->setup_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   ctx_retain(pc->ctx);

@@ -20,8 +20,9 @@ Rows: only rows whose nearest other point has phi = exp(-(eps d)^2) <= 0.5;
 the preconditioner solves the other rows exactly (exact_phi = 0.5).
 
 Instances: 2-D or 3-D (--dim), uniform or an 8-component Gaussian mixture
-(sigma 0.05), the scaled shape parameter eps*h uniform on [2, 3]
-(h = N^(-1/dim)), instance seeds from 1000 (disjoint from every test seed).
+(sigma 0.05), the scaled shape parameter eps*h uniform on [--eh-lo, --eh-hi]
+(h = N^(-1/dim); default [1, 3]), instance seeds from 1000 (disjoint from
+every test seed).
 Below eps*h ~ 0.75 the truncated Gaussian matrix is numerically singular and
 no preconditioner reaches 1e-8.
 
@@ -41,7 +42,7 @@ K = 32
 EXACT_PHI = 0.5
 
 
-def instance(seed, n, dim=2):
+def instance(seed, n, dim=2, eh_range=(1.0, 3.0)):
     rng = np.random.default_rng(seed)
     if rng.uniform() < 0.5:
         pos = rng.uniform(0.0, 1.0, size=(n, dim))
@@ -49,14 +50,14 @@ def instance(seed, n, dim=2):
         centres = rng.uniform(0.15, 0.85, size=(8, dim))
         pos = centres[rng.integers(0, 8, size=n)] + 0.05 * rng.standard_normal((n, dim))
         pos = np.clip(pos, 0.0, np.nextafter(1.0, 0.0))
-    eh = rng.uniform(2.0, 3.0)
+    eh = rng.uniform(*eh_range)
     eps = eh * n ** (1.0 / dim)
     return pos, eps
 
 
-def easy_rows(seed, n, dim=2):
+def easy_rows(seed, n, dim=2, eh_range=(1.0, 3.0)):
     """Features of the rows the network serves (phi of the nearest other point <= EXACT_PHI)."""
-    pos, eps = instance(seed, n, dim)
+    pos, eps = instance(seed, n, dim, eh_range)
     p = ab.Particles(dim).set(pos)
     p.init_octree([0.0] * dim, [1.0] * dim, [False] * dim, 256)
     idx, d2 = ab.knn(p, K)
@@ -83,9 +84,12 @@ def main():
     ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--batch", type=int, default=4096)
     ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--eh-lo", type=float, default=1.0)
+    ap.add_argument("--eh-hi", type=float, default=3.0)
     args = ap.parse_args()
     t0 = time.time()
-    X = np.concatenate([easy_rows(1000 + i, args.n, args.dim) for i in range(args.instances)])
+    X = np.concatenate([easy_rows(1000 + i, args.n, args.dim, (args.eh_lo, args.eh_hi))
+                        for i in range(args.instances)])
     print(f"rows {len(X)} in {time.time() - t0:.1f}s", flush=True)
     m = make_model(dim=args.dim)
     import torch

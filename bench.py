@@ -149,6 +149,58 @@ def slowest_rank(times, world):
     return [float(v) for v in t.cpu()]
 
 
+def cell_build_record(ctx, stream, p, pos, peaks, reps=5):
+    """Cell-list build (CellListOrdered::set_domain + sort + reorder) at the
+    benchmark's N, timed on the device with CUDA events (median of reps - 1
+    after one warm-up): (a) a rebuild, the particles already in cell order
+    (update_positions after a step that moved few particles across cells);
+    (b) a build from a random order (the stored order shuffled before each
+    build; the upload is outside the events).  Compulsory bytes: read
+    positions (24 B) and ids (8 B), write them in cell order (32 B), write
+    the bucket keys (4 B) per particle, plus bucket_begin/end (8 B) per
+    cell."""
+    import torch
+    lo, hi, per = [0, 0, 0], [1, 1, 1], [True, True, True]
+
+    def timed_build(prepare=None):
+        bt = []
+        for _ in range(reps):
+            if prepare:
+                prepare()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            p.init_neighbour_search(lo, hi, per, 10.0)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            bt.append(e0.elapsed_time(e1))
+        return float(np.median(bt[1:]))
+
+    ncells = p.grid()[2]
+    nb = len(p) * (24 + 8 + 32 + 4) + ncells * 8
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    rebuild_ms = timed_build()
+    sorted_pos, sorted_ids = p.positions, p.ids
+    rng = np.random.default_rng(11)
+
+    def shuffle():
+        perm = rng.permutation(len(sorted_pos))
+        p.set(sorted_pos[perm], sorted_ids[perm])
+    shuffled_ms = timed_build(shuffle)
+    p.set(sorted_pos, sorted_ids)
+    p.init_neighbour_search(lo, hi, per, 10.0)
+
+    def rec(ms):
+        gbs = nb / (ms / 1e3) / 1e9
+        return {"ms": ms, "achieved_gbs": gbs, "frac_of_hbm": gbs / hbm}
+    out = {"cells": ncells, "compulsory_bytes": nb, **rec(rebuild_ms),
+           "from_random_order": rec(shuffled_ms),
+           "note": "rebuild of particles in cell order (top level) and build from a random "
+                   "order; median of 4 builds (CUDA events), each including the device-to-host "
+                   "read of the dead count"}
+    return out
+
+
 def replica_throughput(world, steps, seconds):
     """Whole-job matvecs per second: every replica performs `steps` matvecs."""
     return world * steps / seconds
@@ -174,27 +226,9 @@ def run_ours(args):
     p.init_neighbour_search([0, 0, 0], [1, 1, 1], [True, True, True], 10.0)
     build_s = time.perf_counter() - t0
     ids0 = p.ids
-    # cell-list build (CellListOrdered::set_domain + sort + reorder), timed on
-    # the device: compulsory bytes = read positions (24 B) and ids (8 B), write
-    # them in cell order (32 B), write the bucket keys (4 B) per particle, plus
-    # bucket_begin/end (8 B) per cell
     peaks, _ = measured_peaks()
-    bt = []
-    for _ in range(5):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        p.init_neighbour_search([0, 0, 0], [1, 1, 1], [True, True, True], 10.0)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        bt.append(e0.elapsed_time(e1))
-    ncells = p.grid()[2]
-    build_bytes = N_PARTICLES * (24 + 8 + 32 + 4) + ncells * 8
-    build_ms = float(np.median(bt[1:]))
-    cell_build = {"ms": build_ms, "cells": ncells, "compulsory_bytes": build_bytes,
-                  "achieved_gbs": build_bytes / (build_ms / 1e3) / 1e9,
-                  "frac_of_hbm": build_bytes / (build_ms / 1e3) / 1e9 / peaks.get("hbm_gbs", 6800.0),
-                  "note": "median of 4 rebuilds (CUDA events); includes the host round trip "
-                          "for the alive count"}
+    cell_build = cell_build_record(ctx, stream, p, pos, peaks)
+    ncells = cell_build["cells"]
     assert np.array_equal(p.ids, ids0), "rebuild changed the order"
     ids = p.ids
     b_host = np.ascontiguousarray(b_by_id[ids])
@@ -430,6 +464,150 @@ def rbf_section(ctx, model_path, dim=2, n=None, run_schwarz=True, seed=4040):
     if "learned_mixed" in out and "plain_schwarz_fp64" in out:
         out["speedup_learned_vs_plain"] = (out["plain_schwarz_fp64"]["seconds"]
                                            / out["learned_mixed"]["seconds"])
+    return out
+
+
+RBF_GRID_EH = (0.75, 1.0, 1.5, 2.5)
+
+
+def rbf_case(ctx, models, dim, n, dist, eh, seed, plain=True, fallback=True, max_iters=2000):
+    """One RBF interpolation solve to 1e-8 (FP64 residual): N points (uniform,
+    or 8 Gaussians of sigma 0.05 clipped into the unit box), compact Gaussian
+    exp(-(eps |dx|)^2) cut at eps |dx| = 4, eps = eh * N^(1/dim), GMRES(100).
+    Methods as in rbf_section: plain Schwarz/FP64; the learned approximate
+    inverse on the mixed operator (Schwarz fallback after 100 iterations when
+    ``fallback``; else its own result is reported, up to 300 iterations); the
+    same without the network (identity rows where it answers).  Seconds
+    include every set-up; the learned set-up is split into its phases."""
+    import aboria_gb300 as ab
+    import workloads
+    eps = eh * n ** (1.0 / dim)
+    r = 4.0 / eps
+    pos = (workloads.uniform(n, dim, seed=seed) if dist == "uniform"
+           else workloads.clipped_mixture(n, dim, seed=seed))
+    p = ab.Particles(dim, ctx).set(pos)
+    p.init_octree([0.0] * dim, [1.0] * dim, [False] * dim, 256)
+    P = p.positions
+    f = np.sin(4 * np.pi * P[:, 0]) * np.cos(3 * np.pi * P[:, 1])
+    f += 1e-3 * np.random.default_rng(seed + 1).standard_normal(n)
+    kern = ab.Kernel.make(ab.K_COMPACT_GAUSSIAN, eps * eps)
+    K64 = ab.create_sparse_operator(p, p, r, kern, ab.PREC_FP64)
+    K32 = ab.create_sparse_operator(p, p, r, kern, ab.PREC_MIXED)
+    row = {"dim": dim, "n": n, "dist": dist, "eh": eh, "eps": eps, "seed": seed}
+
+    def check(x):
+        return float(np.linalg.norm(f - K64 * x) / np.linalg.norm(f))
+
+    if plain:
+        def run_plain():
+            M = ab.schwarz_preconditioner(K64)
+            x, it, res = ab.gmres(K64, f, M=M, restart=100, max_iters=max_iters, tol=1e-8)
+            return x, it, M.stats()["setup_s"]
+        (x, it, su), t = _timed(run_plain, ctx)
+        res = check(x)
+        row["plain"] = {"s": t, "setup_s": su, "it": it, "res": res, "ok": res <= 1e-8}
+    model = models / f"spai_mlp_{dim}d.bin"
+    mlp = ab.MLP.load(model, ctx=ctx)
+    ident = ab.MLP.load(model, ctx=ctx)
+    ident.params = np.zeros(ident.num_params, np.float32)
+    for name, net in (("learned", mlp), ("without", ident)):
+        def run(net=net):
+            M = ab.learned_preconditioner(K32, net, eps, exact_phi=EXACT_PHI)
+            if fallback:
+                x, it, res, fb = ab.gmres_with_fallback(K32, f, M, K64, restart=100,
+                                                        learned_max_iters=100,
+                                                        max_iters=max_iters, tol=1e-8,
+                                                        A_check=K64)
+            else:
+                x, it, res = ab.gmres(K32, f, M=M, restart=100, max_iters=300, tol=1e-8,
+                                      A_check=K64)
+                fb = False
+            return x, it, fb, M.stats()
+        (x, it, fb, st), t = _timed(run, ctx)
+        res = check(x)
+        row[name] = {"s": t, "setup_s": st["setup_s"], "it": it, "fallback": bool(fb),
+                     "res": res, "ok": res <= 1e-8, "exact_rows": st["domains"],
+                     "phases_s": {k: st[k] for k in ("knn_s", "features_s", "infer_s",
+                                                     "exact_rows_s")}}
+    return row
+
+
+def rbf_grid_section(ctx, models, quick=False, budget_s=900.0):
+    """The RBF solve over dimension x N x point distribution x eps*h, and the
+    fallback rate of the learned preconditioner over instances with eps*h
+    drawn per instance.  Uniform points at N = 50k, 500k, 2M (2-D, and 3-D
+    from eps*h = 1); the 8-Gaussian mixtures at N = 50k only: their clusters
+    are ~100x denser than h, so at larger N the FP64 operator alone holds
+    thousands of neighbours per row.  Plain Schwarz/FP64 is run where its FP64
+    block LU takes seconds (2-D N <= 500k, 3-D N = 50k); larger cells report
+    the approximate inverses without the Schwarz fallback.  Cells run in
+    order of cost and stop at the time budget (the rest are listed as
+    skipped)."""
+    t_start = time.perf_counter()
+    if quick:
+        cells = [(2, 200_000, "uniform", eh, True, True) for eh in (1.5, 2.5)]
+        cells += [(3, 50_000, "uniform", eh, True, True) for eh in (1.5, 2.5)]
+    else:
+        cells = []
+        for eh in RBF_GRID_EH:
+            cells.append((2, 50_000, "uniform", eh, True, True))
+        for eh in RBF_GRID_EH[1:]:
+            cells.append((3, 50_000, "uniform", eh, True, True))
+            cells.append((2, 50_000, "mixture", eh, True, True))
+            cells.append((3, 50_000, "mixture", eh, True, True))
+        for eh in RBF_GRID_EH:
+            cells.append((2, 500_000, "uniform", eh, True, True))
+        for eh in RBF_GRID_EH[1:]:
+            cells.append((3, 500_000, "uniform", eh, False, False))
+        for eh in RBF_GRID_EH:
+            cells.append((2, 2_000_000, "uniform", eh, False, False))
+        for eh in RBF_GRID_EH[1:]:
+            cells.append((3, 2_000_000, "uniform", eh, False, False))
+    out = {"cells": []}
+
+    def over_budget():
+        return time.perf_counter() - t_start > budget_s
+
+    # fallback rate: instances per (dim, distribution) at N = 50k, eps*h ~ U[1, 3]
+    rates = {}
+    for dim in (2, 3):
+        for dist in ("uniform", "mixture"):
+            rng = np.random.default_rng(900 + dim)
+            runs = []
+            for i in range(4 if quick else 10):
+                if over_budget():
+                    break
+                eh = float(rng.uniform(1.0, 3.0))
+                c = rbf_case(ctx, models, dim, 50_000, dist, eh, seed=7000 + 10 * dim + i,
+                             plain=False, fallback=True)
+                runs.append({"eh": eh, "fallback": c["learned"]["fallback"],
+                             "it": c["learned"]["it"], "ok": c["learned"]["ok"],
+                             "s": c["learned"]["s"],
+                             "without_fallback": c["without"]["fallback"],
+                             "without_it": c["without"]["it"], "without_s": c["without"]["s"]})
+                print(json.dumps({"dim": dim, "dist": dist, **runs[-1]}), file=sys.stderr,
+                      flush=True)
+            if runs:
+                rates[f"{dim}d_{dist}"] = {
+                    "instances": len(runs), "eh_range": [1.0, 3.0], "n": 50_000,
+                    "fallback_rate": sum(r["fallback"] for r in runs) / len(runs),
+                    "without_network_fallback_rate":
+                        sum(r["without_fallback"] for r in runs) / len(runs),
+                    "converged": sum(r["ok"] for r in runs), "runs": runs}
+    out["fallback"] = rates
+    for dim, n, dist, eh, plain, fb in cells:
+        if over_budget():
+            out["cells"].append({"dim": dim, "n": n, "dist": dist, "eh": eh,
+                                 "skipped": "time budget"})
+            continue
+        try:
+            out["cells"].append(rbf_case(ctx, models, dim, n, dist, eh, seed=4040 + dim,
+                                         plain=plain, fallback=fb))
+        except Exception as e:  # a cell that does not fit is recorded, not fatal
+            out["cells"].append({"dim": dim, "n": n, "dist": dist, "eh": eh,
+                                 "error": str(e)[:200]})
+        print(json.dumps(out["cells"][-1]), file=sys.stderr, flush=True)  # progress
+    out["seconds"] = time.perf_counter() - t_start
     return out
 
 
@@ -736,8 +914,16 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--matvec-only", action="store_true",
                     help="skip the RBF-solve and FMM sections (profiling runs)")
-    ap.add_argument("--only", choices=["fmm", "rbf"],
+    ap.add_argument("--only", choices=["fmm", "rbf", "rbf_grid", "cell_build"],
                     help="run one secondary section alone and print it (profiling runs)")
+    ap.add_argument("--fmm-n", type=int, default=0,
+                    help="with --only fmm: one problem size instead of 1M and 16M (profiling)")
+    ap.add_argument("--fmm-orders", default="3,5,7", help="with --only fmm and --fmm-n")
+    ap.add_argument("--grid-quick", action="store_true", help="with --only rbf_grid: 4 cells")
+    ap.add_argument("--grid-budget", type=float, default=900.0,
+                    help="with --only rbf_grid: seconds after which the remaining cells are skipped")
+    ap.add_argument("--models", default=str(ROOT / "aboria_gb300" / "models"),
+                    help="folder of the learned preconditioner's models (rbf_grid)")
     args = ap.parse_args()
     if args.only:
         import torch
@@ -746,8 +932,20 @@ def main():
         stream = torch.cuda.Stream()
         torch.cuda.set_stream(stream)  # events and library calls on one stream
         ctx = ab.Context(0, stream=stream.cuda_stream)
-        if args.only == "fmm":
+        if args.only == "fmm" and args.fmm_n:
+            orders = tuple(int(o) for o in args.fmm_orders.split(","))
+            sec = {f"n{args.fmm_n}": fmm_section(ctx, n=args.fmm_n, orders=orders,
+                                                 n_targets=min(10000, args.fmm_n))}
+        elif args.only == "fmm":
             sec = {"n1M": fmm_section(ctx), "n16M": fmm_section(ctx, n=1 << 24, orders=(5,), steps=1)}
+        elif args.only == "rbf_grid":
+            sec = rbf_grid_section(ctx, Path(args.models), quick=args.grid_quick,
+                                   budget_s=args.grid_budget)
+        elif args.only == "cell_build":
+            pos, _ = make_workload()
+            p = ab.Particles(3, ctx).set(pos)
+            p.init_neighbour_search([0, 0, 0], [1, 1, 1], [True, True, True], 10.0)
+            sec = cell_build_record(ctx, stream, p, pos, measured_peaks()[0])
         else:
             sec = rbf_section(ctx, ROOT / "aboria_gb300" / "models" / "spai_mlp_2d.bin")
         print(json.dumps({"section": args.only, **sec}))

@@ -328,6 +328,13 @@ ABX_API int abx_precond_apply(abx_precond *pc, const double *b, double *x);
  * Approximate inverses: ndomains = rows solved exactly, set-up seconds. */
 ABX_API int abx_precond_stats(abx_precond *pc, int64_t *ndomains, int64_t *max_size,
                               int64_t *elements, double *setup_seconds);
+/* Learned approximate inverse: device seconds of its set-up phases -- the
+ * k-NN search, the features, the network's inference and the exact FP64 rows
+ * next to close neighbours (CUDA events on the build stream; 0 for other
+ * preconditioners).  No reference counterpart (the learned preconditioner is
+ * new); any pointer may be NULL. */
+ABX_API int abx_precond_setup_phases(abx_precond *pc, double *knn_s, double *features_s,
+                                     double *infer_s, double *exact_s);
 /* Solve A x = b (x holds the initial guess) with restarted, right-
  * preconditioned flexible GMRES(restart): CGS2 orthogonalisation and Givens
  * rotations in FP64.  At every restart the true residual b - A_check x is

@@ -1,20 +1,27 @@
-"""The barrier protocol of the tcgen05 M2L pipeline (k_m2l_tc5 in
+"""The barrier protocol of the persistent tcgen05 M2L pipeline (k_m2l_tc5 in
 aboria_gb300/csrc/fmm.cu), restated as a model and run under random
-interleavings of its producer warp, its MMA-issuing thread and the
-asynchronous completions (bulk copies, cp.async groups, MMA commits), for
-every ring configuration the kernel is compiled with (read from fmm.cu).
+interleavings of its producer warp, its MMA-issuing thread, its four
+epilogue warps and the asynchronous completions (bulk copies, cp.async
+groups, MMA commits), for every ring configuration the kernel is compiled
+with (read from fmm.cu).
 
-The model follows the kernel: the producer waits for `empty` of block p - S,
-arrives on `fullA` (the bulk copy completes it later), issues block p's
-gathers as one cp.async group and, once at most LAG groups are pending,
-arrives on `fullB` for block p - LAG (the rest after its loop); the MMA
-thread waits for `fullA` and `fullB` of block c with parity (c / S) & 1 and
-commits to `empty`, then to `accb`.
+The model follows the kernel.  Blocks are numbered g = 0, 1, ... across the
+CTA's tiles (nkb blocks per tile).  The producer waits for `empty` of block
+g - S, arrives on `fullA` (the bulk copy completes it later), issues block
+g's gathers as one cp.async group and, once at most LAG groups are pending,
+arrives on `fullB` for block g - LAG (the rest after its loop).  The MMA
+thread, per tile it, waits for `accempty[it % 2]` phase (it - 2) / 2 (it >=
+2), then per block waits for `fullA` and `fullB` with parity (g / S) & 1 and
+commits to `empty`, after the tile to `accfull[it % 2]`, after all tiles to
+`mmadone`.  Each epilogue warp waits for `accfull[it % 2]` phase it / 2 and
+arrives on `accempty[it % 2]`, which completes a phase with its fourth
+arrival.
 
 Checked: no deadlock; every parity wait waits for the phase it means (a
 barrier is never two phases ahead of its waiter, which would make
 try_wait.parity spin until its bound); each barrier's phases complete in
-block order; the epilogue's barrier completes once.
+order; no epilogue warp arrives on a phase of `accempty` before the previous
+one has completed; `mmadone` completes once, after everything.
 """
 import random
 import re
@@ -62,9 +69,10 @@ def ring_configs():
     return {nrb: (_ternary(s_expr, nrb), _ternary(lag_expr, nrb)) for nrb in (1, 2, 3, 4)}
 
 
-def run(nkb, S, LAG, seed):
+def run(nkb, S, LAG, seed, tiles=3):
     rnd = random.Random(seed)
     done = {}  # barrier -> completed phases
+    arrivals = {}  # count-4 barrier -> arrivals in its pending phase
 
     def c(b):
         return done.get(b, 0)
@@ -73,16 +81,28 @@ def run(nkb, S, LAG, seed):
         assert c(b) == phase, ("phase order", b, phase, c(b))
         done[b] = phase + 1
 
+    def arrive4(b, phase):
+        assert c(b) == phase, ("arrival for a later phase", b, phase, c(b))
+        arrivals[b] = arrivals.get(b, 0) + 1
+        if arrivals[b] == 4:
+            arrivals[b] = 0
+            complete(b, phase)
+
     def ready(b, phase):  # try_wait.parity(phase & 1), checked against aliasing
         assert c(b) <= phase + 1, ("barrier two phases ahead of its waiter", b, phase)
         return (c(b) & 1) != (phase & 1)
 
+    total = nkb * tiles
     bulk, groups, mma = [], [], []
-    gdone, p, cc = 0, 0, 0
-    pstate, cstate = "issue", "loop"
-    for _ in range(200000):
+    gdone, g, cc = 0, 0, 0
+    pstate = "issue"
+    # MMA thread: tile index, block within the tile, state
+    mt, mp, mstate = 0, 0, "acq"
+    etile = [0, 0, 0, 0]  # per epilogue warp: the next tile it drains
+    for _ in range(400000):
         acts = [a for a, on in (("A", bulk), ("G", gdone < len(groups)), ("M", mma),
-                                ("P", pstate != "end"), ("C", cstate != "end")) if on]
+                                ("P", pstate != "end"), ("C", mstate != "end")) if on]
+        acts += [("E", w) for w in range(4) if etile[w] < tiles]
         if not acts:
             break
         a = rnd.choice(acts)
@@ -93,46 +113,69 @@ def run(nkb, S, LAG, seed):
             gdone += 1  # cp.async groups complete in issue order
         elif a == "M":
             q = mma.pop(0)  # MMAs complete in issue order
-            if q == "accb":
-                complete("accb", 0)
+            if q[0] == "mmadone":
+                complete("mmadone", 0)
+            elif q[0] == "accfull":
+                complete(("accfull", q[1] % 2), q[1] // 2)
             else:
-                complete(("empty", q % S), q // S)
+                complete(("empty", q[1] % S), q[1] // S)
         elif a == "P":
             if pstate == "issue":
-                if p == nkb:
+                if g == total:
                     pstate = "tail"
                     continue
-                if p >= S and not ready(("empty", p % S), (p - S) // S):
+                if g >= S and not ready(("empty", g % S), (g - S) // S):
                     continue
-                bulk.append(p)
-                groups.append(p)
-                pstate = "lag" if p >= LAG else "next"
+                bulk.append(g)
+                groups.append(g)
+                pstate = "lag" if g >= LAG else "next"
             if pstate == "lag":
                 if len(groups) - gdone > LAG:
                     continue
-                complete(("fullB", (p - LAG) % S), (p - LAG) // S)
+                complete(("fullB", (g - LAG) % S), (g - LAG) // S)
                 pstate = "next"
             if pstate == "next":
-                p += 1
+                g += 1
                 pstate = "issue"
             elif pstate == "tail":
                 if gdone < len(groups):
                     continue
-                for q in range(max(p - LAG, 0), p):
+                for q in range(max(g - LAG, 0), g):
                     complete(("fullB", q % S), q // S)
                 pstate = "end"
+        elif a == "C":
+            if mstate == "acq":
+                if mt == tiles:
+                    mma.append(("mmadone",))
+                    mstate = "end"
+                    continue
+                if mt >= 2 and not ready(("accempty", mt % 2), (mt - 2) // 2):
+                    continue
+                mstate = "blocks"
+                mp = 0
+            if mstate == "blocks":
+                if mp == nkb:
+                    mma.append(("accfull", mt))
+                    mt += 1
+                    mstate = "acq"
+                    continue
+                st, f = cc % S, cc // S
+                if ready(("fullA", st), f) and ready(("fullB", st), f):
+                    mma.append(("empty", cc))
+                    cc += 1
+                    mp += 1
         else:
-            if cc == nkb:
-                mma.append("accb")
-                cstate = "end"
-                continue
-            st, f = cc % S, cc // S
-            if ready(("fullA", st), f) and ready(("fullB", st), f):
-                mma.append(cc)
-                cc += 1
+            w = a[1]
+            it = etile[w]
+            if ready(("accfull", it % 2), it // 2):
+                arrive4(("accempty", it % 2), it // 2)
+                etile[w] += 1
     else:
         raise AssertionError("deadlock")
-    assert c("accb") == 1 and cc == nkb and p == nkb
+    if not all(e == tiles for e in etile) or mstate != "end" or pstate != "end":
+        raise AssertionError("deadlock")
+    assert c("mmadone") == 1 and cc == total and g == total
+    assert c(("accfull", 0)) + c(("accfull", 1)) == tiles
 
 
 def test_ring_configurations_are_read():
@@ -146,10 +189,11 @@ def test_ring_configurations_are_read():
 def test_protocol_has_no_deadlock_or_phase_aliasing(nrb):
     S, LAG = ring_configs()[nrb]
     # block counts: the short cases around the ring depth and the orders'
-    # own ceil(n^3 / 8) (orders 5..8: 16, 27, 43, 64)
-    for nkb in list(range(1, 2 * S + 3)) + [16, 27, 43, 64]:
-        for seed in range(12):
-            run(nkb, S, LAG, seed)
+    # own ceil(n^3 / 16) (orders 5..8: 8, 14, 22, 32); 1 to 4 tiles per CTA
+    for nkb in list(range(1, 2 * S + 3)) + [8, 14, 22, 32]:
+        for tiles in (1, 2, 3, 4):
+            for seed in range(6):
+                run(nkb, S, LAG, seed, tiles)
 
 
 def test_model_detects_a_lag_at_the_ring_depth():

@@ -36,3 +36,12 @@ def lattice(n, dim):
     idx = np.stack(np.meshgrid(*[np.arange(n)] * dim, indexing="ij"), -1).reshape(-1, dim)
     idx = idx[:, ::-1]
     return idx.astype(np.float64) + 0.5
+
+
+def clipped_mixture(n, dim, k=8, sigma=0.05, seed=0):
+    """k isotropic Gaussians (centres U[0.15,0.85]^D, sigma 0.05) clipped into
+    the unit box: the clustered point sets of the RBF-solve grid."""
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(0.15, 0.85, size=(k, dim))
+    pts = centres[rng.integers(0, k, size=n)] + sigma * rng.standard_normal((n, dim))
+    return np.clip(pts, 0.0, np.nextafter(1.0, 0.0))
