@@ -3,7 +3,7 @@
 // bucket index of src/detail/SpatialUtil.h:125-138; the stable sort_by_key of
 // src/detail/Algorithms.h:173-206; lower_bound/upper_bound per bucket,
 // src/CellListOrdered.h:231-239; Particles::reorder, src/Particles.h:694-726)
-// as four launches and one device-to-host read:
+// as five launches and one device-to-host read:
 //
 //  1. k_cl_keys      domain enforcement, alive test and bucket key per
 //                    particle in one pass over the positions; dead particles
@@ -12,13 +12,11 @@
 //  2. k_cl_onesweep  one launch per 10-bit digit of a stable LSD radix sort:
 //                    tiles claimed in order, per-tile digit counts published
 //                    and prefixed by decoupled look-back (no histogram scan
-//                    launches), each tile permuted into digit order in shared
-//                    memory before its writes; the first pass takes the input
-//                    positions as its values, the last one moves positions,
-//                    ids and the scalar column into cell order itself.
+//                    launches).
 //  3. k_cl_ranges    bucket_begin/bucket_end of every cell straight from the
 //                    sorted keys (each boundary between two keys writes the
 //                    cells in its gap; no memset, no scan).
+//  4. k_cl_gather    positions, ids and the scalar column into cell order.
 //
 // The grid depends on the alive count (set_domain_impl,
 // src/CellListOrdered.h:132-186).  The build assumes the grid that count n
@@ -260,55 +258,17 @@ __device__ __forceinline__ void st_release(unsigned long long *p, unsigned long 
   asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-// Dynamic shared memory of the sort pass: the tile's keys and values (in
-// input order, then in digit order), their ranks, the per-warp digit counts,
-// the tile's digit offsets and the digit bases.
+// Dynamic shared memory of the sort pass: the tile's keys, values and
+// within-warp ranks, the per-warp digit counts and the digit bases.
 struct SweepSmem {
   uint32_t key[CL_TILE];
   uint32_t val[CL_TILE];
-  uint16_t rank[CL_TILE];                   // rank in (warp, digit), then the slot in digit order
+  uint16_t rank[CL_TILE];
   uint16_t wcount[SW_WARPS][CL_RADIX + 2];  // counts, then offsets, per warp (<= 16384)
-  uint32_t toff[CL_RADIX];                  // the tile's exclusive digit offsets
   uint32_t dbase[CL_RADIX];
   uint32_t wsum[SW_WARPS + 1];
   uint32_t tile, fail;
 };
-
-// The last pass moves the particles' columns into cell order itself.
-struct ClGather {
-  const double *pos_in;
-  double *pos_out;
-  const int64_t *ids_in;
-  int64_t *ids_out;
-  const double *s_in;
-  double *s_out;
-  int64_t n;
-  int dim;
-};
-
-// Block-wide exclusive scan of one value per thread (SW_TPB threads); wsum
-// is shared scratch.  Returns the thread's exclusive prefix.
-__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t x, uint32_t *wsum) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t incl = x;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += t;
-  }
-  if (lane == 31) wsum[warp] = incl;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    uint32_t run = 0;
-    for (int w = 0; w < SW_WARPS; ++w) {
-      const uint32_t c = wsum[w];
-      wsum[w] = run;
-      run += c;
-    }
-  }
-  __syncthreads();
-  return wsum[warp] + incl - x;
-}
 
 // One stable LSD pass over the digit (key >> 10 pass) & (CL_RADIX - 1).
 // A tile is 16384 keys: warp w of 16 ranks its own 1024 consecutive keys in
@@ -317,17 +277,13 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t x, uint32_t *w
 // the warp), staging keys, values and ranks in shared memory.  The tile's
 // digit counts are published and prefixed by decoupled look-back over the
 // preceding tiles (tiles are claimed in order, so every tile waited on is
-// already running).  The staged keys are then permuted into digit order in
-// shared memory, so that the writes of one digit's run go to consecutive
-// addresses.  vals_in == nullptr: the values are the input positions (the
-// first pass).  vals_out == nullptr: the last pass, which moves positions, ids
-// and the scalar column of alive particles straight to their sorted place.
+// already running), then every key is written to its place.  vals_in ==
+// nullptr: the values are the input positions (the first pass).
 // Status word of (tile, digit): epoch << 34 | flag << 32 | count.
-__global__ void __launch_bounds__(SW_TPB, 1) k_cl_onesweep(
+__global__ void __launch_bounds__(SW_TPB) k_cl_onesweep(
     const uint32_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
     uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, uint32_t n, int pass,
-    unsigned long long *__restrict__ status, uint32_t epoch, ClHeader *__restrict__ H,
-    ClGather G) {
+    unsigned long long *__restrict__ status, uint32_t epoch, ClHeader *__restrict__ H) {
   extern __shared__ __align__(16) unsigned char sweep_raw[];
   SweepSmem &S = *reinterpret_cast<SweepSmem *>(sweep_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -337,17 +293,33 @@ __global__ void __launch_bounds__(SW_TPB, 1) k_cl_onesweep(
     S.fail = 0;
   }
   for (int i = tid; i < SW_WARPS * (CL_RADIX + 2); i += SW_TPB) (&S.wcount[0][0])[i] = 0;
-  // global digit bases: exclusive scan of the pass histogram (thread tid owns
-  // digits tid * DPT .. tid * DPT + DPT - 1 here and below)
-  constexpr int DPT = CL_RADIX / SW_TPB;
-  {
-    uint32_t g[DPT], gs = 0;
+  // global digit bases: exclusive scan of the pass histogram
+  constexpr int DPT = CL_RADIX / SW_TPB;  // digits per thread
+  uint32_t g[DPT], gs = 0;
 #pragma unroll
-    for (int q = 0; q < DPT; ++q) {
-      g[q] = H->hist[pass][tid * DPT + q];
-      gs += g[q];
+  for (int q = 0; q < DPT; ++q) {
+    g[q] = H->hist[pass][tid * DPT + q];
+    gs += g[q];
+  }
+  uint32_t incl = gs;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) S.wsum[warp] = incl;
+  __syncthreads();
+  if (tid == 0) {
+    uint32_t run = 0;
+    for (int w = 0; w < SW_WARPS; ++w) {
+      const uint32_t c = S.wsum[w];
+      S.wsum[w] = run;
+      run += c;
     }
-    uint32_t run = block_exclusive_scan(gs, S.wsum);
+  }
+  __syncthreads();
+  {
+    uint32_t run = S.wsum[warp] + incl - gs;
 #pragma unroll
     for (int q = 0; q < DPT; ++q) {
       S.dbase[tid * DPT + q] = run;
@@ -392,13 +364,13 @@ __global__ void __launch_bounds__(SW_TPB, 1) k_cl_onesweep(
   }
   __syncthreads();
   // per digit: warp prefixes and the tile's count, published for every digit
-  // first; the tile's own digit offsets; then the decoupled look-back over the
-  // preceding tiles and the inclusive publication
+  // first; then the decoupled look-back over the preceding tiles and the
+  // inclusive publication
   const unsigned long long ep = (unsigned long long)epoch << 34;
-  uint32_t tcount[DPT], tsum = 0;
+  uint32_t tcount[DPT];
 #pragma unroll
   for (int q = 0; q < DPT; ++q) {
-    const int d = tid * DPT + q;
+    const int d = tid + q * SW_TPB;
     uint32_t run = 0;
 #pragma unroll
     for (int w = 0; w < SW_WARPS; ++w) {
@@ -407,21 +379,12 @@ __global__ void __launch_bounds__(SW_TPB, 1) k_cl_onesweep(
       run += c;
     }
     tcount[q] = run;
-    tsum += run;
     st_release(status + (size_t)tile * CL_RADIX + d, ep | (tile == 0 ? ST_INCL : ST_AGG) | run);
-  }
-  {
-    uint32_t run = block_exclusive_scan(tsum, S.wsum);
-#pragma unroll
-    for (int q = 0; q < DPT; ++q) {
-      S.toff[tid * DPT + q] = run;
-      run += tcount[q];
-    }
   }
   if (tile > 0) {
 #pragma unroll
     for (int q = 0; q < DPT; ++q) {
-      const int d = tid * DPT + q;
+      const int d = tid + q * SW_TPB;
       uint32_t prefix = 0;
       for (int64_t t = (int64_t)tile - 1; t >= 0; --t) {
         const unsigned long long *pp = status + (size_t)t * CL_RADIX + d;
@@ -456,64 +419,18 @@ __global__ void __launch_bounds__(SW_TPB, 1) k_cl_onesweep(
       S.dbase[d] += prefix;
     }
   }
-  const int nvalid = (int)min((size_t)CL_TILE, (size_t)n - (size_t)tile * CL_TILE);
-  // slot in digit order of every staged key (thread tid owns entries tid +
-  // j * SW_TPB throughout): staged key li came from position tile * CL_TILE +
-  // li and was ranked by warp li / WCHUNK; keys past n were never staged
-  constexpr int PER = CL_TILE / SW_TPB;
-#pragma unroll 4
-  for (int j = 0; j < PER; ++j) {
-    const int li = tid + j * SW_TPB;
-    if (li < nvalid) {
-      const int d = (S.key[li] >> shift) & (CL_RADIX - 1);
-      S.rank[li] = (uint16_t)(S.toff[d] + S.wcount[li / WCHUNK][d] + S.rank[li]);
-    }
-  }
   __syncthreads();
   if (S.fail) return;
-  {
-    uint32_t reg[PER];
-#pragma unroll
-    for (int j = 0; j < PER; ++j) {
-      const int li = tid + j * SW_TPB;
-      reg[j] = li < nvalid ? S.key[li] : 0u;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < PER; ++j) {
-      const int li = tid + j * SW_TPB;
-      if (li < nvalid) S.key[S.rank[li]] = reg[j];
-    }
-#pragma unroll
-    for (int j = 0; j < PER; ++j) {
-      const int li = tid + j * SW_TPB;
-      reg[j] = li < nvalid ? S.val[li] : 0u;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < PER; ++j) {
-      const int li = tid + j * SW_TPB;
-      if (li < nvalid) S.val[S.rank[li]] = reg[j];
-    }
-  }
-  __syncthreads();
-  // the digit run of d occupies slots toff[d] .. toff[d] + count - 1 and goes
-  // to dbase[d] onwards
-  const uint32_t na = vals_out ? 0u : n - H->dead;
+  const int nvalid = (int)min((size_t)CL_TILE, (size_t)n - (size_t)tile * CL_TILE);
+  // staged key li came from position tile * CL_TILE + li and was ranked by
+  // warp li / WCHUNK; keys past n were never staged
   for (int li = tid; li < nvalid; li += SW_TPB) {
+    const int w = li / WCHUNK;
     const uint32_t k = S.key[li];
     const int d = (k >> shift) & (CL_RADIX - 1);
-    const uint32_t dst = S.dbase[d] + ((uint32_t)li - S.toff[d]);
-    const uint32_t v = S.val[li];
+    const uint32_t dst = S.dbase[d] + S.wcount[w][d] + S.rank[li];
     keys_out[dst] = k;
-    if (vals_out) {
-      vals_out[dst] = v;
-    } else if (dst < na) {
-      for (int e = 0; e < G.dim; ++e)
-        G.pos_out[(int64_t)e * na + dst] = G.pos_in[(int64_t)e * G.n + v];
-      G.ids_out[dst] = G.ids_in[v];
-      if (G.s_in) G.s_out[dst] = G.s_in[v];
-    }
+    vals_out[dst] = S.val[li];
   }
 }
 
@@ -531,6 +448,21 @@ __global__ void k_cl_ranges(const uint32_t *__restrict__ keys, const ClHeader *_
     const int64_t cur = k == (int64_t)na ? (int64_t)ncells : (int64_t)min(keys[k], ncells);
     for (int64_t c = prev + 1; c <= cur && c < (int64_t)ncells; ++c) bb[c] = (uint32_t)k;
     for (int64_t c = prev < 0 ? 0 : prev; c < cur; ++c) be[c] = (uint32_t)k;
+  }
+}
+
+__global__ void k_cl_gather(const double *__restrict__ pos_in, int64_t n, int dim,
+                            const uint32_t *__restrict__ perm, const ClHeader *__restrict__ H,
+                            double *__restrict__ pos_out, const int64_t *__restrict__ ids_in,
+                            int64_t *__restrict__ ids_out, const double *__restrict__ s_in,
+                            double *__restrict__ s_out) {
+  const int64_t na = n - (int64_t)H->dead;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < na;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t i = perm[k];
+    for (int d = 0; d < dim; ++d) pos_out[(int64_t)d * na + k] = pos_in[(int64_t)d * n + i];
+    ids_out[k] = ids_in[i];
+    if (s_in) s_out[k] = s_in[i];
   }
 }
 
@@ -633,7 +565,7 @@ int run_build(abx_particles *p, const GridDesc &g, uint32_t *dead_out) {
   for (int d = 0; d < D; ++d) P.bnd_total += (int)g.size[d] + 2;
   const size_t keys_smem = P.bnd_total <= CL_BND_SMEM ? (size_t)P.bnd_total * 8 : 0;
   const int ntiles = (int)((n + CL_TILE - 1) / CL_TILE);
-  // scratch: header, keys_alt, two value buffers
+  // scratch: header, vals, keys_alt, vals_alt
   size_t o = 0;
   carve_size<ClHeader>(o, 1);
   carve_size<uint32_t>(o, n);
@@ -643,16 +575,10 @@ int run_build(abx_particles *p, const GridDesc &g, uint32_t *dead_out) {
   unsigned char *sb = ctx->scratch.ptr;
   o = 0;
   ClHeader *H = carve<ClHeader>(sb, o, 1);
+  uint32_t *vals = carve<uint32_t>(sb, o, n);
   uint32_t *keys_alt = carve<uint32_t>(sb, o, n);
-  uint32_t *vals_a = carve<uint32_t>(sb, o, n);
-  uint32_t *vals_b = carve<uint32_t>(sb, o, n);
+  uint32_t *vals_alt = carve<uint32_t>(sb, o, n);
   ABX_TRY(p->keys.reserve(n));
-  ABX_TRY(p->pos_alt.reserve((size_t)D * n));
-  ABX_TRY(p->ids_alt.reserve(n));
-  if (p->has_scalar) ABX_TRY(p->scalar_alt.reserve(n));
-  // pass q reads kb[q & 1] and writes kb[(q + 1) & 1]; the last one writes p->keys
-  uint32_t *kb[2] = {(P.npasses & 1) ? keys_alt : p->keys.ptr,
-                     (P.npasses & 1) ? p->keys.ptr : keys_alt};
   const size_t nstatus = (size_t)ntiles * CL_RADIX;
   if (p->cl_status.cap < nstatus) {
     ABX_TRY(p->cl_status.reserve(nstatus));
@@ -664,30 +590,38 @@ int run_build(abx_particles *p, const GridDesc &g, uint32_t *dead_out) {
   const int kblocks = (int)std::min<int64_t>((n + CL_KEYS_TILE - 1) / CL_KEYS_TILE,
                                              (int64_t)ctx->num_sms * 4);
   if (D == 1)
-    k_cl_keys<1><<<kblocks, CL_TPB, keys_smem, s>>>(p->pos.ptr, n, P, kb[0], H);
+    k_cl_keys<1><<<kblocks, CL_TPB, keys_smem, s>>>(p->pos.ptr, n, P, p->keys.ptr, H);
   else if (D == 2)
-    k_cl_keys<2><<<kblocks, CL_TPB, keys_smem, s>>>(p->pos.ptr, n, P, kb[0], H);
+    k_cl_keys<2><<<kblocks, CL_TPB, keys_smem, s>>>(p->pos.ptr, n, P, p->keys.ptr, H);
   else
-    k_cl_keys<3><<<kblocks, CL_TPB, keys_smem, s>>>(p->pos.ptr, n, P, kb[0], H);
+    k_cl_keys<3><<<kblocks, CL_TPB, keys_smem, s>>>(p->pos.ptr, n, P, p->keys.ptr, H);
   ABX_CHECK_CUDA(cudaGetLastError());
-  ClGather G{p->pos.ptr, p->pos_alt.ptr, p->ids.ptr, p->ids_alt.ptr,
-             p->has_scalar ? p->scalar.ptr : nullptr, p->has_scalar ? p->scalar_alt.ptr : nullptr,
-             n, D};
-  uint32_t *vbuf[2] = {vals_a, vals_b};
+  uint32_t *ki = p->keys.ptr, *vi = nullptr, *ko = keys_alt, *vo = vals;
   for (int pass = 0; pass < P.npasses; ++pass) {
     p->cl_epoch = (p->cl_epoch + 1) & 0x3fffffffu;
     if (p->cl_epoch == 0) p->cl_epoch = 1;
-    const bool last = pass == P.npasses - 1;
-    k_cl_onesweep<<<ntiles, SW_TPB, sizeof(SweepSmem), s>>>(
-        kb[pass & 1], pass == 0 ? nullptr : vbuf[(pass + 1) & 1], kb[(pass + 1) & 1],
-        last ? nullptr : vbuf[pass & 1], (uint32_t)n, pass, p->cl_status.ptr, p->cl_epoch, H, G);
+    k_cl_onesweep<<<ntiles, SW_TPB, sizeof(SweepSmem), s>>>(ki, vi, ko, vo, (uint32_t)n, pass,
+                                                            p->cl_status.ptr, p->cl_epoch, H);
+    if (pass == 0) vi = vals_alt;
     ABX_CHECK_CUDA(cudaGetLastError());
+    std::swap(ki, ko);
+    std::swap(vi, vo);
   }
+  if (ki != p->keys.ptr)
+    ABX_CHECK_CUDA(cudaMemcpyAsync(p->keys.ptr, ki, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
   ABX_TRY(p->bucket_begin.reserve(g.ncells));
   ABX_TRY(p->bucket_end.reserve(g.ncells));
   const int rblocks = (int)std::min<int64_t>((n + 1 + 255) / 256, (int64_t)ctx->num_sms * 16);
   k_cl_ranges<<<rblocks, 256, 0, s>>>(p->keys.ptr, H, (uint32_t)n, g.ncells, p->bucket_begin.ptr,
                                       p->bucket_end.ptr);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  ABX_TRY(p->pos_alt.reserve((size_t)D * n));
+  ABX_TRY(p->ids_alt.reserve(n));
+  if (p->has_scalar) ABX_TRY(p->scalar_alt.reserve(n));
+  const int gblocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)ctx->num_sms * 16);
+  k_cl_gather<<<gblocks, 256, 0, s>>>(p->pos.ptr, n, D, vi, H, p->pos_alt.ptr, p->ids.ptr,
+                                      p->ids_alt.ptr, p->has_scalar ? p->scalar.ptr : nullptr,
+                                      p->has_scalar ? p->scalar_alt.ptr : nullptr);
   ABX_CHECK_CUDA(cudaGetLastError());
   uint32_t hd[2];
   ABX_CHECK_CUDA(cudaMemcpyAsync(hd, &H->dead, 8, cudaMemcpyDeviceToHost, s));

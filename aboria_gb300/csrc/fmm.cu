@@ -593,22 +593,24 @@ constexpr int T5_PART = 128 * T5_KB * 4;  // bytes of one K operand part: 128 ro
 constexpr uint32_t T5_POLL_CAP = 1u << 30;  // second bound on the polls of one wait
 constexpr int T5_THREADS = 192;             // producer, MMA issuer, four epilogue warps
 constexpr int T5_EPI_BYTES = 4 * 16 * 32 * 4;  // the epilogue warps' transpose tiles
-// Per row-block count: N pairs per tile, ring depth S, producer lag LAG and
-// TMEM columns (two accumulator sets of NRB x N).  One or two row blocks use
-// 128-pair tiles, three or four 64-pair tiles; one CTA per SM.
+// Per row-block count: N pairs per tile; two rings, SA stages of the K
+// operand (A, one bulk copy each) and SB stages of the gathered W rows (B);
+// the producer runs the gathers D blocks ahead of the bulk copies (D < SB),
+// so D blocks of gathers are in flight while the MMAs run; TMEM columns for
+// two accumulator sets of NRB x N.  One or two row blocks use 128-pair
+// tiles, three or four 64-pair tiles; one CTA per SM.
 template <int NRB> struct T5Cfg {
   static constexpr int N = NRB <= 2 ? 128 : 64;
-  static constexpr int S = NRB == 1 ? 6 : (NRB == 2 ? 4 : (NRB == 3 ? 3 : 2));  // ring depth
-  // the producer signals block p - LAG's W copies after issuing block p
-  // (LAG < S: the MMAs of block p - S, which free block p's stage, never wait
-  // for a block the producer has not signalled)
-  static constexpr int LAG = NRB == 1 ? 3 : (NRB == 2 ? 2 : 1);
+  static constexpr int SA = NRB == 1 ? 4 : (NRB == 4 ? 2 : 3);
+  static constexpr int SB = NRB == 2 ? 6 : 8;
+  static constexpr int D = SB - 2;
   static constexpr int A_BYTES = NRB * 2 * T5_PART;       // K hi, lo of every row block
   static constexpr int B_PART = N * T5_KB * 4;            // W of the N pairs, one part
-  static constexpr int STAGE = A_BYTES + 2 * B_PART;
+  static constexpr int B_BYTES = 2 * B_PART;              // Wh, Wl
   static constexpr int ACC_COLS = NRB * N;                // one accumulator set
   // + alignment, then barriers, pair indices (<= 4 KB)
-  static constexpr size_t SMEM = (size_t)S * STAGE + T5_EPI_BYTES + 1024 + 4096;
+  static constexpr size_t SMEM =
+      (size_t)SA * A_BYTES + (size_t)SB * B_BYTES + T5_EPI_BYTES + 1024 + 4096;
   static constexpr uint32_t TCOLS = 2 * NRB * N <= 256 ? 256u : 512u;
 };
 constexpr int t5_pairs(int nrb) { return nrb <= 2 ? T5Cfg<1>::N : T5Cfg<3>::N; }
@@ -626,10 +628,13 @@ static_assert(T5Cfg<1>::SMEM * 2 > 228 * 1024 && T5Cfg<2>::SMEM * 2 > 228 * 1024
 static_assert(T5Cfg<1>::SMEM <= 227 * 1024 && T5Cfg<2>::SMEM <= 227 * 1024 &&
                   T5Cfg<3>::SMEM <= 227 * 1024 && T5Cfg<4>::SMEM <= 227 * 1024,
               "shared memory per CTA");
-static_assert(T5_KB % 8 == 0, "a stage holds whole MMA K-steps");
-static_assert(T5Cfg<1>::LAG < T5Cfg<1>::S && T5Cfg<2>::LAG < T5Cfg<2>::S &&
-                  T5Cfg<3>::LAG < T5Cfg<3>::S && T5Cfg<4>::LAG < T5Cfg<4>::S,
-              "producer lag below the ring depth");
+static_assert(T5_KB == 16, "the producer's lane mapping: four 16-byte chunks per W row and stage");
+static_assert(T5Cfg<1>::D < T5Cfg<1>::SB && T5Cfg<2>::D < T5Cfg<2>::SB &&
+                  T5Cfg<3>::D < T5Cfg<3>::SB && T5Cfg<4>::D < T5Cfg<4>::SB &&
+                  T5Cfg<1>::D <= 6 && T5Cfg<2>::D <= 6 && T5Cfg<3>::D <= 6 && T5Cfg<4>::D <= 6,
+              "gathers run ahead by less than the B ring depth (and at most 6 groups)");
+static_assert(T5Cfg<1>::SA >= 2 && T5Cfg<2>::SA >= 2 && T5Cfg<3>::SA >= 2 && T5Cfg<4>::SA >= 2,
+              "double-buffered K operand");
 
 // Packed split-TF32 M2L matrices: per (matrix, T5_KB-column block kb, 128-row
 // block rb, part hi/lo) the shared-memory image of the operand tile,
@@ -721,6 +726,19 @@ __device__ __forceinline__ void cp16(uint32_t dst, const void *src, int nbytes) 
                : "memory");
 }
 
+// cp.async.wait_group takes its count as an immediate.
+__device__ __forceinline__ void cp_async_wait_upto(int pending) {
+  switch (pending) {
+    case 0: asm volatile("cp.async.wait_group 0;" ::: "memory"); break;
+    case 1: asm volatile("cp.async.wait_group 1;" ::: "memory"); break;
+    case 2: asm volatile("cp.async.wait_group 2;" ::: "memory"); break;
+    case 3: asm volatile("cp.async.wait_group 3;" ::: "memory"); break;
+    case 4: asm volatile("cp.async.wait_group 4;" ::: "memory"); break;
+    case 5: asm volatile("cp.async.wait_group 5;" ::: "memory"); break;
+    default: asm volatile("cp.async.wait_group 6;" ::: "memory"); break;
+  }
+}
+
 template <int NRB>
 __global__ void __launch_bounds__(T5_THREADS, 1) k_m2l_tc5(int ncheb, int nkb, int ldk, int ldg,
                                                          int ntiles,
@@ -735,26 +753,32 @@ __global__ void __launch_bounds__(T5_THREADS, 1) k_m2l_tc5(int ncheb, int nkb, i
                                                          int *__restrict__ status,
                                                          uint64_t limit_ns, int drop_arrive) {
   using C = T5Cfg<NRB>;
-  constexpr int S = C::S, LAG = C::LAG, T5_N = C::N;
+  constexpr int SA = C::SA, SB = C::SB, D = C::D, T5_N = C::N;
   extern __shared__ __align__(128) unsigned char t5raw[];
   unsigned char *sm = (unsigned char *)(((uintptr_t)t5raw + 1023) & ~(uintptr_t)1023);
-  float *epi = reinterpret_cast<float *>(sm + S * C::STAGE);
-  uint64_t *fullA = reinterpret_cast<uint64_t *>(sm + S * C::STAGE + T5_EPI_BYTES);
-  uint64_t *fullB = fullA + S, *empty = fullB + S;
-  uint64_t *accfull = empty + S, *accempty = accfull + 2, *mmadone = accempty + 2;
+  unsigned char *ringB = sm + SA * C::A_BYTES;
+  float *epi = reinterpret_cast<float *>(ringB + SB * C::B_BYTES);
+  uint64_t *fullA = reinterpret_cast<uint64_t *>(ringB + SB * C::B_BYTES + T5_EPI_BYTES);
+  uint64_t *emptyA = fullA + SA, *fullB = emptyA + SA, *emptyB = fullB + SB;
+  uint64_t *accfull = emptyB + SB, *accempty = accfull + 2, *mmadone = accempty + 2;
   uint32_t *tslot = reinterpret_cast<uint32_t *>(mmadone + 1);
-  // sInfo: 0 blocks issued by the producer, 1 blocks the MMA issuer took,
-  // 2 abort (any role gave up)
+  // sInfo: 0 K blocks whose bulk copy the producer issued, 1 blocks the MMA
+  // issuer took, 2 abort (any role gave up)
   int *sInfo = reinterpret_cast<int *>(tslot + 4);
-  int *sSrc = sInfo + 4;           // the producer's current tile's sources
-  int *sTgt = sSrc + T5_N;         // per epilogue warp: its current tile's targets
+  int *sTgt = sInfo + 4;  // per epilogue warp: its current tile's targets
   volatile int *abort_flag = sInfo + 2;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // tiles of this CTA, and its blocks (nkb per tile)
+  const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  const int total = my_tiles * nkb;
   if (tid == 0) {
-    for (int q = 0; q < S; ++q) {
+    for (int q = 0; q < SA; ++q) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&fullA[q])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&emptyA[q])));
+    }
+    for (int q = 0; q < SB; ++q) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&fullB[q])));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&empty[q])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&emptyB[q])));
     }
     for (int q = 0; q < 2; ++q) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&accfull[q])));
@@ -777,74 +801,97 @@ __global__ void __launch_bounds__(T5_THREADS, 1) k_m2l_tc5(int ncheb, int nkb, i
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tslot;
-  const uint32_t smbase = smem_addr(sm);
+  const uint32_t smbase = smem_addr(sm), sbB0 = smem_addr(ringB);
 
   if (warp == 0) {
-    // ---- producer: blocks g = 0, 1, ... over the CTA's tiles
+    // ---- producer.  Two streams over the CTA's blocks g = 0 .. total-1:
+    // the W gathers of block g + D are issued before the K bulk copy of
+    // block g, and block g's gathers are signalled (fullB) once at most D
+    // later groups are pending.  Lane l gathers the 16-byte chunk l % 4 of
+    // rows 8 j + l / 4 (j = 0 .. N/8 - 1) of every stage.
+    constexpr int NJ = T5_N / 8;
+    const int kq = lane & 3, rl = lane >> 2;
+    const uint32_t boff = (uint32_t)(kq * NJ * 128 + rl * 16);
+    size_t rowoff[NJ];
+    uint32_t valid = 0;
     bool ok = true;
-    int g = 0;
-    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-      const int m = tile_mat[t], p0 = tile_first[t];
-      const int np = min(T5_N, mat_off[m + 1] - p0);
-      __syncwarp();  // the previous tile's gathers are all issued
-      for (int q = lane; q < T5_N; q += 32) sSrc[q] = q < np ? pairs[p0 + q].y : -1;
-      __syncwarp();
-      const unsigned char *Am = (const unsigned char *)Ap + (size_t)m * nkb * C::A_BYTES;
-      for (int p = 0; p < nkb; ++p) {
-        const int st = g % S;
-        if (g >= S && !mbar_wait(smem_addr(&empty[st]), ((g - S) / S) & 1, limit_ns, abort_flag))
+    int gb = 0, ga = 0;
+    const unsigned char *Am = nullptr;
+    for (; ga < total; ++ga) {
+      // top the gathers up to block ga + D
+      for (; gb < total && gb <= ga + D; ++gb) {
+        const int pb = gb % nkb;
+        if (pb == 0) {
+          const int t = blockIdx.x + (gb / nkb) * gridDim.x;
+          const int m = tile_mat[t], p0 = tile_first[t];
+          const int np = min(T5_N, mat_off[m + 1] - p0);
+          valid = 0;
+#pragma unroll
+          for (int j = 0; j < NJ; ++j) {
+            const int r = j * 8 + rl;
+            const int src = r < np ? pairs[p0 + r].y : -1;
+            rowoff[j] = (size_t)(src >= 0 ? src : 0) * ldk + kq * 4;
+            if (src >= 0) valid |= 1u << j;
+          }
+        }
+        const int st = gb % SB;
+        if (gb >= SB && !mbar_wait(smem_addr(&emptyB[st]), ((gb - SB) / SB) & 1, limit_ns,
+                                   abort_flag))
           ok = false;
         if (!__all_sync(0xffffffffu, ok)) {
           ok = false;
           break;
         }
-        const uint32_t sb = smbase + (uint32_t)(st * C::STAGE);
-        if (lane == 0) {
-          const uint32_t fb = smem_addr(&fullA[st]);
-          asm volatile(
-              "{\n\t.reg .b64 state;\n\t"
-              "mbarrier.arrive.expect_tx.shared::cta.b64 state, [%0], %1;\n\t}" ::"r"(fb),
-              "r"(C::A_BYTES)
-              : "memory");
-          asm volatile(
-              "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
-              "[%3];" ::"r"(sb),
-              "l"(Am + (size_t)p * C::A_BYTES), "r"(C::A_BYTES), "r"(fb)
-              : "memory");
-        }
-        constexpr int KQ = T5_KB / 4;  // 16-byte chunks of a W row per stage
-#pragma unroll 4
-        for (int e = lane; e < T5_N * KQ; e += 32) {
-          // consecutive lanes take consecutive chunks of one row
-          const int kq = e % KQ, rl = (e / KQ) & 7, rh = e / (KQ * 8);
-          const int src = sSrc[rh * 8 + rl];
-          const uint32_t off = (uint32_t)((kq * (T5_N / 8) + rh) * 128 + rl * 16);
-          const size_t gi = (size_t)(src >= 0 ? src : 0) * ldk + p * T5_KB + kq * 4;
-          cp16(sb + C::A_BYTES + off, Wh + gi, src >= 0 ? 16 : 0);
-          cp16(sb + C::A_BYTES + C::B_PART + off, Wl + gi, src >= 0 ? 16 : 0);
+        const uint32_t sb = sbB0 + (uint32_t)(st * C::B_BYTES) + boff;
+        const size_t kof = (size_t)pb * T5_KB;
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+          const int nb = (valid >> j) & 1u ? 16 : 0;
+          cp16(sb + j * 128, Wh + rowoff[j] + kof, nb);
+          cp16(sb + C::B_PART + j * 128, Wl + rowoff[j] + kof, nb);
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
-        if (g >= LAG) {
-          // block g - LAG's W copies have landed: hand them to the async proxy
-          asm volatile("cp.async.wait_group %0;" ::"n"(LAG) : "memory");
-          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-          __syncwarp();
-          // drop_arrive (fault injection for tests): block 0's W copies are
-          // never signalled, so the MMA issuer's wait runs out
-          if (lane == 0 && !(drop_arrive && g - LAG == 0))
-            mbar_arrive(smem_addr(&fullB[(g - LAG) % S]));
-        }
-        ++g;
+      }
+      if (!ok) break;
+      // block ga's gathers have landed: hand them to the async proxy
+      cp_async_wait_upto(gb - ga - 1);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      // drop_arrive (fault injection for tests): block 0's W copies are never
+      // signalled, so the MMA issuer's wait runs out
+      if (lane == 0 && !(drop_arrive && ga == 0)) mbar_arrive(smem_addr(&fullB[ga % SB]));
+      // the K operand of block ga: one bulk copy
+      const int pa = ga % nkb;
+      if (pa == 0) {
+        const int t = blockIdx.x + (ga / nkb) * gridDim.x;
+        Am = (const unsigned char *)Ap + (size_t)tile_mat[t] * nkb * C::A_BYTES;
+      }
+      const int sa = ga % SA;
+      if (ga >= SA &&
+          !mbar_wait(smem_addr(&emptyA[sa]), ((ga - SA) / SA) & 1, limit_ns, abort_flag))
+        ok = false;
+      if (!__all_sync(0xffffffffu, ok)) {
+        ok = false;
+        break;
+      }
+      if (lane == 0) {
+        const uint32_t fb = smem_addr(&fullA[sa]);
+        asm volatile(
+            "{\n\t.reg .b64 state;\n\t"
+            "mbarrier.arrive.expect_tx.shared::cta.b64 state, [%0], %1;\n\t}" ::"r"(fb),
+            "r"(C::A_BYTES)
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+            "[%3];" ::"r"(smbase + (uint32_t)(sa * C::A_BYTES)),
+            "l"(Am + (size_t)pa * C::A_BYTES), "r"(C::A_BYTES), "r"(fb)
+            : "memory");
       }
     }
-    // the last min(g, LAG) blocks
     asm volatile("cp.async.wait_all;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncwarp();
     if (lane == 0) {
-      for (int q = max(g - LAG, 0); q < g; ++q)
-        if (!(drop_arrive && q == 0)) mbar_arrive(smem_addr(&fullB[q % S]));
-      sInfo[0] = g;
+      sInfo[0] = ga;  // bulk copies issued: blocks 0 .. ga - 1
       if (!ok) *abort_flag = 1;
     }
   } else if (warp == 1) {
@@ -855,7 +902,7 @@ __global__ void __launch_bounds__(T5_THREADS, 1) k_m2l_tc5(int ncheb, int nkb, i
       constexpr uint32_t bks = (T5_N / 8) * 128;  // the same for the T5_N pair rows
       bool ok = true;
       int c = 0, it = 0;
-      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++it) {
+      for (; it < my_tiles && ok; ++it) {
         const int ab = it & 1;
         if (it >= 2 && !mbar_wait(smem_addr(&accempty[ab]), ((it - 2) >> 1) & 1, limit_ns,
                                   abort_flag)) {
@@ -865,23 +912,23 @@ __global__ void __launch_bounds__(T5_THREADS, 1) k_m2l_tc5(int ncheb, int nkb, i
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t dacc = tmem + (uint32_t)(ab * C::ACC_COLS);
         for (int p = 0; p < nkb; ++p) {
-          const int st = c % S;
-          const uint32_t par = (c / S) & 1;
-          if (!mbar_wait(smem_addr(&fullA[st]), par, limit_ns, abort_flag) ||
-              !mbar_wait(smem_addr(&fullB[st]), par, limit_ns, abort_flag)) {
+          const int sa = c % SA, sb = c % SB;
+          if (!mbar_wait(smem_addr(&fullA[sa]), (c / SA) & 1, limit_ns, abort_flag) ||
+              !mbar_wait(smem_addr(&fullB[sb]), (c / SB) & 1, limit_ns, abort_flag)) {
             ok = false;
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          const uint32_t base = smbase + (uint32_t)(st * C::STAGE);
+          const uint32_t abase = smbase + (uint32_t)(sa * C::A_BYTES);
+          const uint32_t bbase = sbB0 + (uint32_t)(sb * C::B_BYTES);
 #pragma unroll
           for (int kk = 0; kk < T5_KB / 8; ++kk) {
             // MMA K-step kk: two core-matrix columns further along K
-            const uint64_t bhk = umma_desc(base + C::A_BYTES + kk * 2 * bks, bks, 128);
-            const uint64_t blk = umma_desc(base + C::A_BYTES + C::B_PART + kk * 2 * bks, bks, 128);
+            const uint64_t bhk = umma_desc(bbase + kk * 2 * bks, bks, 128);
+            const uint64_t blk = umma_desc(bbase + C::B_PART + kk * 2 * bks, bks, 128);
 #pragma unroll
             for (int rb = 0; rb < NRB; ++rb) {
-              const uint32_t a0 = base + rb * 2 * T5_PART + kk * 2 * ks;
+              const uint32_t a0 = abase + rb * 2 * T5_PART + kk * 2 * ks;
               const uint64_t ah = umma_desc(a0, ks, 128);
               const uint64_t al = umma_desc(a0 + T5_PART, ks, 128);
               const uint64_t ad[3] = {al, ah, ah}, bd[3] = {bhk, blk, bhk};
@@ -896,7 +943,8 @@ __global__ void __launch_bounds__(T5_THREADS, 1) k_m2l_tc5(int ncheb, int nkb, i
               }
             }
           }
-          umma_commit(smem_addr(&empty[st]));
+          umma_commit(smem_addr(&emptyA[sa]));
+          umma_commit(smem_addr(&emptyB[sb]));
           ++c;
         }
         if (ok) umma_commit(smem_addr(&accfull[ab]));
@@ -913,8 +961,8 @@ __global__ void __launch_bounds__(T5_THREADS, 1) k_m2l_tc5(int ncheb, int nkb, i
     float *tt = epi + ew * (16 * 32);
     int *tg = sTgt + ew * T5_N;
     bool ok = true;
-    int it = 0;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
+    for (int it = 0; it < my_tiles; ++it) {
+      const int t = blockIdx.x + it * gridDim.x;
       const int ab = it & 1;
       const int m = tile_mat[t], p0 = tile_first[t];
       const int np = min(T5_N, mat_off[m + 1] - p0);
@@ -977,7 +1025,7 @@ __global__ void __launch_bounds__(T5_THREADS, 1) k_m2l_tc5(int ncheb, int nkb, i
       // bulk copies issued but never taken by the MMA issuer complete before
       // shared memory is released (bounded waits)
       for (int q = sInfo[1]; q < sInfo[0]; ++q)
-        mbar_wait(smem_addr(&fullA[q % S]), (q / S) & 1, limit_ns);
+        mbar_wait(smem_addr(&fullA[q % SA]), (q / SA) & 1, limit_ns);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

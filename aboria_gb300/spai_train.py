@@ -26,6 +26,8 @@ every test seed).
 Below eps*h ~ 0.75 the truncated Gaussian matrix is numerically singular and
 no preconditioner reaches 1e-8.
 
+The committed models were trained with the defaults (eps*h in [1, 3]):
+
     python -m aboria_gb300.spai_train --out aboria_gb300/models/spai_mlp_2d.bin
     python -m aboria_gb300.spai_train --dim 3 --out aboria_gb300/models/spai_mlp_3d.bin
 """

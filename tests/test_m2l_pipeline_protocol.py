@@ -6,13 +6,16 @@ groups, MMA commits), for every ring configuration the kernel is compiled
 with (read from fmm.cu).
 
 The model follows the kernel.  Blocks are numbered g = 0, 1, ... across the
-CTA's tiles (nkb blocks per tile).  The producer waits for `empty` of block
-g - S, arrives on `fullA` (the bulk copy completes it later), issues block
-g's gathers as one cp.async group and, once at most LAG groups are pending,
-arrives on `fullB` for block g - LAG (the rest after its loop).  The MMA
-thread, per tile it, waits for `accempty[it % 2]` phase (it - 2) / 2 (it >=
-2), then per block waits for `fullA` and `fullB` with parity (g / S) & 1 and
-commits to `empty`, after the tile to `accfull[it % 2]`, after all tiles to
+CTA's tiles (nkb blocks per tile); the K operand (A) and the gathered W rows
+(B) have rings of SA and SB stages.  Per block ga the producer first issues
+the gathers of the blocks up to ga + D (each waits for `emptyB` of block
+gb - SB and is one cp.async group), then waits until at most gb - ga - 1
+groups are pending and arrives on `fullB` of block ga, then waits for
+`emptyA` of block ga - SA and issues block ga's bulk copy (completing
+`fullA`).  The MMA thread, per tile it, waits for `accempty[it % 2]` phase
+(it - 2) / 2 (it >= 2), then per block c waits for `fullA` (parity (c / SA)
+& 1) and `fullB` (parity (c / SB) & 1) and commits to `emptyA` and
+`emptyB`, after the tile to `accfull[it % 2]`, after all tiles to
 `mmadone`.  Each epilogue warp waits for `accfull[it % 2]` phase it / 2 and
 arrives on `accempty[it % 2]`, which completes a phase with its fourth
 arrival.
@@ -64,12 +67,18 @@ def _ternary(expr, nrb):
 def ring_configs():
     src = FMM.read_text()
     body = src[src.index("template <int NRB> struct T5Cfg {"):]
-    s_expr = re.search(r"static constexpr int S = ([^;]+);", body).group(1)
-    lag_expr = re.search(r"static constexpr int LAG = ([^;]+);", body).group(1)
-    return {nrb: (_ternary(s_expr, nrb), _ternary(lag_expr, nrb)) for nrb in (1, 2, 3, 4)}
+    sa_expr = re.search(r"static constexpr int SA = ([^;]+);", body).group(1)
+    sb_expr = re.search(r"static constexpr int SB = ([^;]+);", body).group(1)
+    d_expr = re.search(r"static constexpr int D = ([^;]+);", body).group(1)
+    out = {}
+    for nrb in (1, 2, 3, 4):
+        sa, sb = _ternary(sa_expr, nrb), _ternary(sb_expr, nrb)
+        d = eval(d_expr.replace("SB", str(sb)).replace("SA", str(sa)))
+        out[nrb] = (sa, sb, d)
+    return out
 
 
-def run(nkb, S, LAG, seed, tiles=3):
+def run(nkb, SA, SB, D, seed, tiles=3):
     rnd = random.Random(seed)
     done = {}  # barrier -> completed phases
     arrivals = {}  # count-4 barrier -> arrivals in its pending phase
@@ -94,9 +103,8 @@ def run(nkb, S, LAG, seed, tiles=3):
 
     total = nkb * tiles
     bulk, groups, mma = [], [], []
-    gdone, g, cc = 0, 0, 0
-    pstate = "issue"
-    # MMA thread: tile index, block within the tile, state
+    gdone, ga, gb, cc = 0, 0, 0, 0
+    pstate = "gathers"
     mt, mp, mstate = 0, 0, "acq"
     etile = [0, 0, 0, 0]  # per epilogue warp: the next tile it drains
     for _ in range(400000):
@@ -108,41 +116,42 @@ def run(nkb, S, LAG, seed, tiles=3):
         a = rnd.choice(acts)
         if a == "A":
             q = bulk.pop(rnd.randrange(len(bulk)))
-            complete(("fullA", q % S), q // S)
+            complete(("fullA", q % SA), q // SA)
         elif a == "G":
             gdone += 1  # cp.async groups complete in issue order
         elif a == "M":
-            q = mma.pop(0)  # MMAs complete in issue order
+            q = mma.pop(0)  # MMA commits complete in issue order
             if q[0] == "mmadone":
                 complete("mmadone", 0)
             elif q[0] == "accfull":
                 complete(("accfull", q[1] % 2), q[1] // 2)
+            elif q[0] == "emptyA":
+                complete(("emptyA", q[1] % SA), q[1] // SA)
             else:
-                complete(("empty", q[1] % S), q[1] // S)
+                complete(("emptyB", q[1] % SB), q[1] // SB)
         elif a == "P":
-            if pstate == "issue":
-                if g == total:
-                    pstate = "tail"
+            if pstate == "gathers":
+                if ga == total:
+                    pstate = "end"
                     continue
-                if g >= S and not ready(("empty", g % S), (g - S) // S):
+                if gb < total and gb <= ga + D:
+                    if gb >= SB and not ready(("emptyB", gb % SB), (gb - SB) // SB):
+                        continue
+                    groups.append(gb)
+                    gb += 1
                     continue
-                bulk.append(g)
-                groups.append(g)
-                pstate = "lag" if g >= LAG else "next"
-            if pstate == "lag":
-                if len(groups) - gdone > LAG:
+                pstate = "signal"
+            if pstate == "signal":
+                if len(groups) - gdone > gb - ga - 1:
                     continue
-                complete(("fullB", (g - LAG) % S), (g - LAG) // S)
-                pstate = "next"
-            if pstate == "next":
-                g += 1
-                pstate = "issue"
-            elif pstate == "tail":
-                if gdone < len(groups):
+                complete(("fullB", ga % SB), ga // SB)
+                pstate = "bulk"
+            if pstate == "bulk":
+                if ga >= SA and not ready(("emptyA", ga % SA), (ga - SA) // SA):
                     continue
-                for q in range(max(g - LAG, 0), g):
-                    complete(("fullB", q % S), q // S)
-                pstate = "end"
+                bulk.append(ga)
+                ga += 1
+                pstate = "gathers"
         elif a == "C":
             if mstate == "acq":
                 if mt == tiles:
@@ -159,9 +168,9 @@ def run(nkb, S, LAG, seed, tiles=3):
                     mt += 1
                     mstate = "acq"
                     continue
-                st, f = cc % S, cc // S
-                if ready(("fullA", st), f) and ready(("fullB", st), f):
-                    mma.append(("empty", cc))
+                if ready(("fullA", cc % SA), cc // SA) and ready(("fullB", cc % SB), cc // SB):
+                    mma.append(("emptyA", cc))
+                    mma.append(("emptyB", cc))
                     cc += 1
                     mp += 1
         else:
@@ -174,30 +183,30 @@ def run(nkb, S, LAG, seed, tiles=3):
         raise AssertionError("deadlock")
     if not all(e == tiles for e in etile) or mstate != "end" or pstate != "end":
         raise AssertionError("deadlock")
-    assert c("mmadone") == 1 and cc == total and g == total
+    assert c("mmadone") == 1 and cc == total and ga == total and gb == total
     assert c(("accfull", 0)) + c(("accfull", 1)) == tiles
 
 
 def test_ring_configurations_are_read():
     cfg = ring_configs()
     assert set(cfg) == {1, 2, 3, 4}
-    for S, LAG in cfg.values():
-        assert 1 <= LAG < S
+    for SA, SB, D in cfg.values():
+        assert SA >= 2 and 1 <= D < SB
 
 
 @pytest.mark.parametrize("nrb", [1, 2, 3, 4])
 def test_protocol_has_no_deadlock_or_phase_aliasing(nrb):
-    S, LAG = ring_configs()[nrb]
-    # block counts: the short cases around the ring depth and the orders'
+    SA, SB, D = ring_configs()[nrb]
+    # block counts: the short cases around the ring depths and the orders'
     # own ceil(n^3 / 16) (orders 5..8: 8, 14, 22, 32); 1 to 4 tiles per CTA
-    for nkb in list(range(1, 2 * S + 3)) + [8, 14, 22, 32]:
+    for nkb in list(range(1, 2 * SB + 3)) + [8, 14, 22, 32]:
         for tiles in (1, 2, 3, 4):
-            for seed in range(6):
-                run(nkb, S, LAG, seed, tiles)
+            for seed in range(4):
+                run(nkb, SA, SB, D, seed, tiles)
 
 
-def test_model_detects_a_lag_at_the_ring_depth():
-    """The check has teeth: with LAG = S the producer waits for MMAs of a
-    block whose operands it has not yet signalled."""
+def test_model_detects_gathers_ahead_by_the_ring_depth():
+    """The check has teeth: with D = SB the producer waits for the MMAs of a
+    block whose gathers it has not yet signalled."""
     with pytest.raises(AssertionError, match="deadlock"):
-        run(8, 3, 3, 0)
+        run(8, 3, 4, 4, 0)
