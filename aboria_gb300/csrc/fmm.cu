@@ -551,12 +551,12 @@ __global__ void __launch_bounds__(64 * WM) k_m2l_tc2(int ncheb, int ldk, int ldg
 }
 
 // ------------------------------------------------- M2L on tcgen05 (TMEM) ---
-// The same tile GEMM on the 5th-generation tensor cores.  A tile is (M2L
-// matrix, N target/source pairs); for all NRB = ceil(ncheb/128) row blocks
+// The same tile GEMM on the 5th-generation tensor cores.  One CTA (4 warps)
+// per (M2L matrix, N-pair tile) computes all NRB = ceil(ncheb/128) row
+// blocks, so the gathered source expansions of the tile are read once:
 //   G[targets][rb*128 + r] += sum_k K[rb*128 + r][k] * W[sources][k]
 // as split TF32 (K = Kh + Kl, W = Wh + Wl; Kl Wh + Kh Wl + Kh Wh) on
-// tcgen05.mma kind::tf32 into NRB accumulators of 128 x N FP32 in TMEM, so
-// the tile's gathered source expansions are read once.
+// tcgen05.mma kind::tf32 into NRB accumulators of 128 x N FP32 in TMEM.
 // The K matrices are packed once per plan into the shared-memory image of a
 // pipeline stage (k_pack_tf32), so a stage's A operand is one bulk copy on the
 // TMA engine (cp.async.bulk, completion counted on the stage's `fullA`
@@ -565,79 +565,50 @@ __global__ void __launch_bounds__(64 * WM) k_m2l_tc2(int ncheb, int ldk, int ldg
 // no-swizzle K-major core-matrix layout (8 rows x 16 bytes per core matrix;
 // the descriptor's leading byte offset is the core-matrix stride along K, the
 // stride byte offset along rows).
-// The kernel is persistent: one CTA per SM walks the tiles blockIdx.x,
-// blockIdx.x + gridDim.x, ... with the operand ring running on across tile
-// boundaries and two TMEM accumulator sets, so that the epilogue of tile t
-// overlaps the loads and MMAs of tile t + 1.  Roles (6 warps, no CTA-wide
-// barrier inside the loop):
-//  * warp 0 produces: per block (T5_KB columns of K) it waits for the stage's
-//    `empty` barrier, issues the bulk copy and the gathers, then for the block
-//    LAG back waits its gathers, fences them to the async proxy and arrives on
-//    `fullB`;
-//  * lane 0 of warp 1 issues the MMAs: per tile it waits until the epilogue
-//    has drained the accumulator set (`accempty`), then per block waits for
-//    `fullA` and `fullB`, issues 2 NRB * 3 MMAs (two K-steps of 8) and
-//    commits them to `empty`; after the tile's last block it commits to
-//    `accfull`;
-//  * warps 2-5 run the epilogue: each reads its 32 accumulator lanes (rows,
-//    warp % 4 selects them) with tcgen05.ld, transposes through shared memory
-//    and adds into G with 16-byte reductions coalesced along the rows, then
-//    releases the set (`accempty` completes with the fourth warp's arrival).
-// Every wait is bounded by the GPU's global timer and ends early once another
-// role has given up; the CTA then sets *status, waits (bounded) for its MMAs
-// and bulk copies in flight and still releases its TMEM.
-// K columns per pipeline stage: two MMA K-steps (tf32: 8 columns each) per
-// fullA/fullB/empty handshake
-constexpr int T5_KB = 16;
-constexpr int T5_PART = 128 * T5_KB * 4;  // bytes of one K operand part: 128 rows x T5_KB columns
+// Roles, with no CTA-wide barrier inside the loop: warp 0 produces (waits for
+// the stage's `empty` barrier, issues block p, then waits for block p-LAG's
+// W copies, fences them to the async proxy and arrives on `fullB`); lane 0 of
+// warp 1 waits for `fullA` and `fullB`, issues the 3 NRB MMAs of the block
+// and commits them to `empty`, and after the last block to `accb`; all four
+// warps then wait for `accb` and run the epilogue: each reads its 32
+// accumulator lanes (rows) with tcgen05.ld and adds them into G with
+// reductions that are coalesced along the rows.  Every wait is bounded: on
+// timeout the kernel sets *status, skips the epilogue, waits (bounded) for
+// its copies and MMAs in flight and still releases its TMEM.  The ring depth
+// keeps the CTAs resident on an SM (by shared memory) within the SM's 512
+// TMEM columns.
+constexpr int T5_KB = 8;
+constexpr int T5_PART = 128 * T5_KB * 4;  // bytes of one K operand part: 128 rows x 8 columns
 constexpr uint32_t T5_POLL_CAP = 1u << 30;  // second bound on the polls of one wait
-constexpr int T5_THREADS = 192;             // producer, MMA issuer, four epilogue warps
-constexpr int T5_EPI_BYTES = 4 * 16 * 32 * 4;  // the epilogue warps' transpose tiles
-// Per row-block count: N pairs per tile; two rings, SA stages of the K
-// operand (A, one bulk copy each) and SB stages of the gathered W rows (B);
-// the producer runs the gathers D blocks ahead of the bulk copies (D < SB),
-// so D blocks of gathers are in flight while the MMAs run; TMEM columns for
-// two accumulator sets of NRB x N.  One or two row blocks use 128-pair
-// tiles, three or four 64-pair tiles; one CTA per SM.
+// Per row-block count: N pairs per tile, ring depth S, producer lag LAG and
+// TMEM columns.  Three or four row blocks use 64-pair tiles so that two CTAs
+// share an SM (their latencies overlap); one or two use 128-pair tiles.
 template <int NRB> struct T5Cfg {
   static constexpr int N = NRB <= 2 ? 128 : 64;
-  static constexpr int SA = NRB == 1 ? 4 : (NRB == 4 ? 2 : 3);
-  static constexpr int SB = NRB == 2 ? 6 : 8;
-  static constexpr int D = SB - 2;
+  static constexpr int S = NRB == 2 ? 4 : 3;  // ring depth
+  // the producer signals block p - LAG's W copies after issuing block p
+  // (LAG < S: the MMAs of block p - S, which free block p's stage, never wait
+  // for a block the producer has not signalled)
+  static constexpr int LAG = NRB == 2 ? 2 : 1;
   static constexpr int A_BYTES = NRB * 2 * T5_PART;       // K hi, lo of every row block
   static constexpr int B_PART = N * T5_KB * 4;            // W of the N pairs, one part
-  static constexpr int B_BYTES = 2 * B_PART;              // Wh, Wl
-  static constexpr int ACC_COLS = NRB * N;                // one accumulator set
-  // + alignment, then barriers, pair indices (<= 4 KB)
-  static constexpr size_t SMEM =
-      (size_t)SA * A_BYTES + (size_t)SB * B_BYTES + T5_EPI_BYTES + 1024 + 4096;
-  static constexpr uint32_t TCOLS = 2 * NRB * N <= 256 ? 256u : 512u;
+  static constexpr int STAGE = A_BYTES + 2 * B_PART;
+  static constexpr size_t SMEM = (size_t)S * STAGE + 1024 + 2048;  // + alignment, barriers, indices
+  static constexpr uint32_t TCOLS = NRB * N <= 128 ? 128u : (NRB * N <= 256 ? 256u : 512u);
 };
 constexpr int t5_pairs(int nrb) { return nrb <= 2 ? T5Cfg<1>::N : T5Cfg<3>::N; }
 static_assert(T5Cfg<1>::N == T5Cfg<2>::N && T5Cfg<3>::N == T5Cfg<4>::N, "tile width per t5_pairs");
-// two accumulator sets fit the CTA's TMEM allocation, one CTA per SM (by
-// shared memory), so the allocation never waits for another CTA
-static_assert(2 * T5Cfg<1>::ACC_COLS <= (int)T5Cfg<1>::TCOLS &&
-                  2 * T5Cfg<2>::ACC_COLS <= (int)T5Cfg<2>::TCOLS &&
-                  2 * T5Cfg<3>::ACC_COLS <= (int)T5Cfg<3>::TCOLS &&
-                  2 * T5Cfg<4>::ACC_COLS <= (int)T5Cfg<4>::TCOLS,
-              "two accumulator sets per CTA");
-static_assert(T5Cfg<1>::SMEM * 2 > 228 * 1024 && T5Cfg<2>::SMEM * 2 > 228 * 1024 &&
-                  T5Cfg<3>::SMEM * 2 > 228 * 1024 && T5Cfg<4>::SMEM * 2 > 228 * 1024,
-              "one resident CTA per SM");
-static_assert(T5Cfg<1>::SMEM <= 227 * 1024 && T5Cfg<2>::SMEM <= 227 * 1024 &&
-                  T5Cfg<3>::SMEM <= 227 * 1024 && T5Cfg<4>::SMEM <= 227 * 1024,
-              "shared memory per CTA");
-static_assert(T5_KB == 16, "the producer's lane mapping: four 16-byte chunks per W row and stage");
-static_assert(T5Cfg<1>::D < T5Cfg<1>::SB && T5Cfg<2>::D < T5Cfg<2>::SB &&
-                  T5Cfg<3>::D < T5Cfg<3>::SB && T5Cfg<4>::D < T5Cfg<4>::SB &&
-                  T5Cfg<1>::D <= 6 && T5Cfg<2>::D <= 6 && T5Cfg<3>::D <= 6 && T5Cfg<4>::D <= 6,
-              "gathers run ahead by less than the B ring depth (and at most 6 groups)");
-static_assert(T5Cfg<1>::SA >= 2 && T5Cfg<2>::SA >= 2 && T5Cfg<3>::SA >= 2 && T5Cfg<4>::SA >= 2,
-              "double-buffered K operand");
+// resident CTAs per SM (bounded by shared memory) x TCOLS <= the SM's 512 TMEM columns
+static_assert(T5Cfg<1>::SMEM * 5 > 228 * 1024 && T5Cfg<2>::SMEM * 3 > 228 * 1024 &&
+                  T5Cfg<3>::SMEM * 3 > 228 * 1024 && T5Cfg<4>::SMEM * 3 > 228 * 1024,
+              "resident CTAs per SM must fit the SM's 512 TMEM columns");
+static_assert(T5Cfg<3>::SMEM <= 227 * 1024 && T5Cfg<4>::SMEM <= 227 * 1024, "shared memory per CTA");
+static_assert(T5Cfg<1>::LAG < T5Cfg<1>::S && T5Cfg<2>::LAG < T5Cfg<2>::S &&
+                  T5Cfg<3>::LAG < T5Cfg<3>::S && T5Cfg<4>::LAG < T5Cfg<4>::S,
+              "producer lag below the ring depth");
 
-// Packed split-TF32 M2L matrices: per (matrix, T5_KB-column block kb, 128-row
-// block rb, part hi/lo) the shared-memory image of the operand tile,
+// Packed split-TF32 M2L matrices: per (matrix, 8-column block kb, 128-row
+// block rb, part hi/lo) the 4 KB shared-memory image of the operand tile,
 // element (r, k) at ((k/4) * 16 + r/8) * 128 + (r%8) * 16 + (k%4) * 4 bytes;
 // zero beyond ncheb.  hi = tf32(K), lo = tf32(K - hi).
 __global__ void k_pack_tf32(const double *__restrict__ K, int64_t nmat, int ncheb, int nkb,
@@ -684,9 +655,8 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
 
 // Wait for the given phase of an mbarrier for at most limit_ns nanoseconds
 // of the GPU's global timer (and at most T5_POLL_CAP polls); false if it ran
-// out, or (checked every 16 polls) once *abort is set.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint64_t limit_ns,
-                                          const volatile int *abort = nullptr) {
+// out.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint64_t limit_ns) {
   uint64_t t0 = 0;
   for (uint32_t it = 0; it < T5_POLL_CAP; ++it) {
     uint32_t ok;
@@ -698,7 +668,6 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint64_
         : "memory");
     if (ok) return true;
     if ((it & 15u) == 0u) {
-      if (abort && *abort) return false;
       const uint64_t now = globaltimer_ns();
       if (it == 0u)
         t0 = now;
@@ -709,87 +678,52 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint64_
   return false;
 }
 
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("{\n\t.reg .b64 state;\n\tmbarrier.arrive.shared::cta.b64 state, [%0];\n\t}" ::"r"(bar)
-               : "memory");
-}
-
-__device__ __forceinline__ void umma_commit(uint32_t bar) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-      : "memory");
-}
-
 // 16-byte asynchronous copy; nbytes = 0 writes zeros.
 __device__ __forceinline__ void cp16(uint32_t dst, const void *src, int nbytes) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(nbytes)
                : "memory");
 }
 
-// cp.async.wait_group takes its count as an immediate.
-__device__ __forceinline__ void cp_async_wait_upto(int pending) {
-  switch (pending) {
-    case 0: asm volatile("cp.async.wait_group 0;" ::: "memory"); break;
-    case 1: asm volatile("cp.async.wait_group 1;" ::: "memory"); break;
-    case 2: asm volatile("cp.async.wait_group 2;" ::: "memory"); break;
-    case 3: asm volatile("cp.async.wait_group 3;" ::: "memory"); break;
-    case 4: asm volatile("cp.async.wait_group 4;" ::: "memory"); break;
-    case 5: asm volatile("cp.async.wait_group 5;" ::: "memory"); break;
-    default: asm volatile("cp.async.wait_group 6;" ::: "memory"); break;
-  }
-}
-
 template <int NRB>
-__global__ void __launch_bounds__(T5_THREADS, 1) k_m2l_tc5(int ncheb, int nkb, int ldk, int ldg,
-                                                         int ntiles,
-                                                         const float *__restrict__ Ap,
-                                                         const int2 *__restrict__ pairs,
-                                                         const int *__restrict__ mat_off,
-                                                         const int *__restrict__ tile_mat,
-                                                         const int *__restrict__ tile_first,
-                                                         const float *__restrict__ Wh,
-                                                         const float *__restrict__ Wl,
-                                                         float *__restrict__ G32,
-                                                         int *__restrict__ status,
-                                                         uint64_t limit_ns, int drop_arrive) {
+__global__ void __launch_bounds__(128) k_m2l_tc5(int ncheb, int nkb, int ldk, int ldg,
+                                                 const float *__restrict__ Ap,
+                                                 const int2 *__restrict__ pairs,
+                                                 const int *__restrict__ mat_off,
+                                                 const int *__restrict__ tile_mat,
+                                                 const int *__restrict__ tile_first,
+                                                 const float *__restrict__ Wh,
+                                                 const float *__restrict__ Wl,
+                                                 float *__restrict__ G32, int *__restrict__ status,
+                                                 uint64_t limit_ns, int drop_arrive) {
   using C = T5Cfg<NRB>;
-  constexpr int SA = C::SA, SB = C::SB, D = C::D, T5_N = C::N;
+  constexpr int S = C::S, LAG = C::LAG, T5_N = C::N;
   extern __shared__ __align__(128) unsigned char t5raw[];
   unsigned char *sm = (unsigned char *)(((uintptr_t)t5raw + 1023) & ~(uintptr_t)1023);
-  unsigned char *ringB = sm + SA * C::A_BYTES;
-  float *epi = reinterpret_cast<float *>(ringB + SB * C::B_BYTES);
-  uint64_t *fullA = reinterpret_cast<uint64_t *>(ringB + SB * C::B_BYTES + T5_EPI_BYTES);
-  uint64_t *emptyA = fullA + SA, *fullB = emptyA + SA, *emptyB = fullB + SB;
-  uint64_t *accfull = emptyB + SB, *accempty = accfull + 2, *mmadone = accempty + 2;
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(mmadone + 1);
-  // sInfo: 0 K blocks whose bulk copy the producer issued, 1 blocks the MMA
-  // issuer took, 2 abort (any role gave up)
-  int *sInfo = reinterpret_cast<int *>(tslot + 4);
-  int *sTgt = sInfo + 4;  // per epilogue warp: its current tile's targets
-  volatile int *abort_flag = sInfo + 2;
+  uint64_t *fullA = (uint64_t *)(sm + S * C::STAGE);
+  uint64_t *fullB = fullA + S, *empty = fullB + S, *accb = empty + S;
+  uint32_t *tslot = (uint32_t *)(accb + 1);
+  int *sSrc = (int *)(tslot + 4), *sTgt = sSrc + T5_N, *sInfo = sTgt + T5_N;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  // tiles of this CTA, and its blocks (nkb per tile)
-  const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-  const int total = my_tiles * nkb;
+  const int tile = blockIdx.x;
+  const int m = tile_mat[tile], p0 = tile_first[tile];
+  const int np = min(T5_N, mat_off[m + 1] - p0);
+  if (tid < T5_N) {
+    const int2 pr = tid < np ? pairs[p0 + tid] : make_int2(-1, -1);
+    sTgt[tid] = pr.x;
+    sSrc[tid] = pr.y;
+  }
   if (tid == 0) {
-    for (int q = 0; q < SA; ++q) {
+    for (int q = 0; q < S; ++q) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&fullA[q])));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&emptyA[q])));
-    }
-    for (int q = 0; q < SB; ++q) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&fullB[q])));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&emptyB[q])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&empty[q])));
     }
-    for (int q = 0; q < 2; ++q) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&accfull[q])));
-      // one arrival per epilogue warp
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" ::"r"(smem_addr(&accempty[q])));
-    }
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(mmadone)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(accb)));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    sInfo[0] = 0;
-    sInfo[1] = 0;
-    sInfo[2] = 0;
+    sInfo[0] = 0;  // blocks issued by the producer
+    sInfo[1] = 0;  // blocks whose operands the MMA issuer received
+    sInfo[2] = 1;  // producer ok
+    sInfo[3] = 1;  // MMA issuer ok
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -801,81 +735,20 @@ __global__ void __launch_bounds__(T5_THREADS, 1) k_m2l_tc5(int ncheb, int nkb, i
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tslot;
-  const uint32_t smbase = smem_addr(sm), sbB0 = smem_addr(ringB);
+  const uint32_t smbase = smem_addr(sm);
 
   if (warp == 0) {
-    // ---- producer.  Two streams over the CTA's blocks g = 0 .. total-1:
-    // the W gathers of block g + D are issued before the K bulk copy of
-    // block g, and block g's gathers are signalled (fullB) once at most D
-    // later groups are pending.  Lane l gathers the 16-byte chunk l % 4 of
-    // rows 8 j + l / 4 (j = 0 .. N/8 - 1) of every stage.
-    constexpr int NJ = T5_N / 8;
-    const int kq = lane & 3, rl = lane >> 2;
-    const uint32_t boff = (uint32_t)(kq * NJ * 128 + rl * 16);
-    size_t rowoff[NJ];
-    uint32_t valid = 0;
+    // ---- producer
+    const unsigned char *Am = (const unsigned char *)Ap + (size_t)m * nkb * C::A_BYTES;
     bool ok = true;
-    int gb = 0, ga = 0;
-    const unsigned char *Am = nullptr;
-    for (; ga < total; ++ga) {
-      // top the gathers up to block ga + D
-      for (; gb < total && gb <= ga + D; ++gb) {
-        const int pb = gb % nkb;
-        if (pb == 0) {
-          const int t = blockIdx.x + (gb / nkb) * gridDim.x;
-          const int m = tile_mat[t], p0 = tile_first[t];
-          const int np = min(T5_N, mat_off[m + 1] - p0);
-          valid = 0;
-#pragma unroll
-          for (int j = 0; j < NJ; ++j) {
-            const int r = j * 8 + rl;
-            const int src = r < np ? pairs[p0 + r].y : -1;
-            rowoff[j] = (size_t)(src >= 0 ? src : 0) * ldk + kq * 4;
-            if (src >= 0) valid |= 1u << j;
-          }
-        }
-        const int st = gb % SB;
-        if (gb >= SB && !mbar_wait(smem_addr(&emptyB[st]), ((gb - SB) / SB) & 1, limit_ns,
-                                   abort_flag))
-          ok = false;
-        if (!__all_sync(0xffffffffu, ok)) {
-          ok = false;
-          break;
-        }
-        const uint32_t sb = sbB0 + (uint32_t)(st * C::B_BYTES) + boff;
-        const size_t kof = (size_t)pb * T5_KB;
-#pragma unroll
-        for (int j = 0; j < NJ; ++j) {
-          const int nb = (valid >> j) & 1u ? 16 : 0;
-          cp16(sb + j * 128, Wh + rowoff[j] + kof, nb);
-          cp16(sb + C::B_PART + j * 128, Wl + rowoff[j] + kof, nb);
-        }
-        asm volatile("cp.async.commit_group;" ::: "memory");
-      }
-      if (!ok) break;
-      // block ga's gathers have landed: hand them to the async proxy
-      cp_async_wait_upto(gb - ga - 1);
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      __syncwarp();
-      // drop_arrive (fault injection for tests): block 0's W copies are never
-      // signalled, so the MMA issuer's wait runs out
-      if (lane == 0 && !(drop_arrive && ga == 0)) mbar_arrive(smem_addr(&fullB[ga % SB]));
-      // the K operand of block ga: one bulk copy
-      const int pa = ga % nkb;
-      if (pa == 0) {
-        const int t = blockIdx.x + (ga / nkb) * gridDim.x;
-        Am = (const unsigned char *)Ap + (size_t)tile_mat[t] * nkb * C::A_BYTES;
-      }
-      const int sa = ga % SA;
-      if (ga >= SA &&
-          !mbar_wait(smem_addr(&emptyA[sa]), ((ga - SA) / SA) & 1, limit_ns, abort_flag))
-        ok = false;
-      if (!__all_sync(0xffffffffu, ok)) {
-        ok = false;
-        break;
-      }
+    int p = 0;
+    for (; p < nkb; ++p) {
+      const int st = p % S;
+      if (p >= S && !mbar_wait(smem_addr(&empty[st]), ((p - S) / S) & 1, limit_ns)) ok = false;
+      if (!__all_sync(0xffffffffu, ok)) break;
+      const uint32_t sb = smbase + (uint32_t)(st * C::STAGE);
       if (lane == 0) {
-        const uint32_t fb = smem_addr(&fullA[sa]);
+        const uint32_t fb = smem_addr(&fullA[st]);
         asm volatile(
             "{\n\t.reg .b64 state;\n\t"
             "mbarrier.arrive.expect_tx.shared::cta.b64 state, [%0], %1;\n\t}" ::"r"(fb),
@@ -883,149 +756,143 @@ __global__ void __launch_bounds__(T5_THREADS, 1) k_m2l_tc5(int ncheb, int nkb, i
             : "memory");
         asm volatile(
             "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
-            "[%3];" ::"r"(smbase + (uint32_t)(sa * C::A_BYTES)),
-            "l"(Am + (size_t)pa * C::A_BYTES), "r"(C::A_BYTES), "r"(fb)
+            "[%3];" ::"r"(sb),
+            "l"(Am + (size_t)p * C::A_BYTES), "r"(C::A_BYTES), "r"(fb)
             : "memory");
       }
-    }
-    asm volatile("cp.async.wait_all;" ::: "memory");
-    __syncwarp();
-    if (lane == 0) {
-      sInfo[0] = ga;  // bulk copies issued: blocks 0 .. ga - 1
-      if (!ok) *abort_flag = 1;
-    }
-  } else if (warp == 1) {
-    if (lane == 0) {
-      // ---- MMA issuer
-      constexpr uint32_t idesc = umma_idesc_tf32(128, T5_N);
-      constexpr uint32_t ks = (128 / 8) * 128;    // core-matrix stride along K (K rows)
-      constexpr uint32_t bks = (T5_N / 8) * 128;  // the same for the T5_N pair rows
-      bool ok = true;
-      int c = 0, it = 0;
-      for (; it < my_tiles && ok; ++it) {
-        const int ab = it & 1;
-        if (it >= 2 && !mbar_wait(smem_addr(&accempty[ab]), ((it - 2) >> 1) & 1, limit_ns,
-                                  abort_flag)) {
-          ok = false;
-          break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t dacc = tmem + (uint32_t)(ab * C::ACC_COLS);
-        for (int p = 0; p < nkb; ++p) {
-          const int sa = c % SA, sb = c % SB;
-          if (!mbar_wait(smem_addr(&fullA[sa]), (c / SA) & 1, limit_ns, abort_flag) ||
-              !mbar_wait(smem_addr(&fullB[sb]), (c / SB) & 1, limit_ns, abort_flag)) {
-            ok = false;
-            break;
-          }
-          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          const uint32_t abase = smbase + (uint32_t)(sa * C::A_BYTES);
-          const uint32_t bbase = sbB0 + (uint32_t)(sb * C::B_BYTES);
 #pragma unroll
-          for (int kk = 0; kk < T5_KB / 8; ++kk) {
-            // MMA K-step kk: two core-matrix columns further along K
-            const uint64_t bhk = umma_desc(bbase + kk * 2 * bks, bks, 128);
-            const uint64_t blk = umma_desc(bbase + C::B_PART + kk * 2 * bks, bks, 128);
-#pragma unroll
-            for (int rb = 0; rb < NRB; ++rb) {
-              const uint32_t a0 = abase + rb * 2 * T5_PART + kk * 2 * ks;
-              const uint64_t ah = umma_desc(a0, ks, 128);
-              const uint64_t al = umma_desc(a0 + T5_PART, ks, 128);
-              const uint64_t ad[3] = {al, ah, ah}, bd[3] = {bhk, blk, bhk};
-#pragma unroll
-              for (int q = 0; q < 3; ++q) {
-                const uint32_t acc = (p > 0 || kk > 0 || q > 0) ? 1u : 0u;
-                asm volatile(
-                    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                    "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(
-                        dacc + (uint32_t)(rb * T5_N)),
-                    "l"(ad[q]), "l"(bd[q]), "r"(idesc), "r"(acc));
-              }
-            }
-          }
-          umma_commit(smem_addr(&emptyA[sa]));
-          umma_commit(smem_addr(&emptyB[sb]));
-          ++c;
-        }
-        if (ok) umma_commit(smem_addr(&accfull[ab]));
+      for (int e = lane; e < T5_N * (T5_KB / 4); e += 32) {
+        const int rl = e & 7, kq = (e >> 3) & 1, rh = e >> 4;
+        const int src = sSrc[rh * 8 + rl];
+        const uint32_t off = (uint32_t)((kq * (T5_N / 8) + rh) * 128 + rl * 16);
+        const size_t g = (size_t)(src >= 0 ? src : 0) * ldk + p * T5_KB + kq * 4;
+        cp16(sb + C::A_BYTES + off, Wh + g, src >= 0 ? 16 : 0);
+        cp16(sb + C::A_BYTES + C::B_PART + off, Wl + g, src >= 0 ? 16 : 0);
       }
-      // completes once every MMA issued above has completed
-      umma_commit(smem_addr(mmadone));
-      sInfo[1] = c;
-      if (!ok) *abort_flag = 1;
+      asm volatile("cp.async.commit_group;" ::: "memory");
+      if (p >= LAG) {
+        // block p - LAG's W copies have landed: hand them to the async proxy
+        asm volatile("cp.async.wait_group %0;" ::"n"(LAG) : "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        // drop_arrive (fault injection for tests): block 0's W copies are
+        // never signalled, so the MMA issuer's wait runs out
+        if (lane == 0 && !(drop_arrive && p - LAG == 0))
+          asm volatile("{\n\t.reg .b64 state;\n\tmbarrier.arrive.shared::cta.b64 state, [%0];\n\t}" ::"r"(
+                           smem_addr(&fullB[(p - LAG) % S]))
+                       : "memory");
+      }
     }
+    // the last min(p, LAG) blocks
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncwarp();
-  } else {
-    // ---- epilogue: warps 2-5, TMEM lanes 32 (warp % 4) .. + 31
-    const int ew = warp - 2, q4 = warp & 3;
-    float *tt = epi + ew * (16 * 32);
-    int *tg = sTgt + ew * T5_N;
+    if (lane == 0) {
+      for (int q = max(p - LAG, 0); q < p; ++q)
+        if (!(drop_arrive && q == 0))
+          asm volatile("{\n\t.reg .b64 state;\n\tmbarrier.arrive.shared::cta.b64 state, [%0];\n\t}" ::"r"(
+                         smem_addr(&fullB[q % S]))
+                     : "memory");
+      sInfo[0] = p;
+      if (!ok) sInfo[2] = 0;
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---- MMA issuer
+    constexpr uint32_t idesc = umma_idesc_tf32(128, T5_N);
+    constexpr uint32_t ks = (128 / 8) * 128;    // core-matrix stride along K (K rows)
+    constexpr uint32_t bks = (T5_N / 8) * 128;  // the same for the T5_N pair rows
     bool ok = true;
-    for (int it = 0; it < my_tiles; ++it) {
-      const int t = blockIdx.x + it * gridDim.x;
-      const int ab = it & 1;
-      const int m = tile_mat[t], p0 = tile_first[t];
-      const int np = min(T5_N, mat_off[m + 1] - p0);
-      for (int q = lane; q < T5_N; q += 32) tg[q] = q < np ? pairs[p0 + q].x : -1;
-      __syncwarp();
-      if (!__all_sync(0xffffffffu,
-                      mbar_wait(smem_addr(&accfull[ab]), (it >> 1) & 1, limit_ns, abort_flag))) {
+    int c = 0;
+    for (; c < nkb; ++c) {
+      const int st = c % S;
+      const uint32_t par = (c / S) & 1;
+      if (!mbar_wait(smem_addr(&fullA[st]), par, limit_ns) ||
+          !mbar_wait(smem_addr(&fullB[st]), par, limit_ns)) {
         ok = false;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll 1
+      const uint32_t base = smbase + (uint32_t)(st * C::STAGE);
+      const uint64_t bh = umma_desc(base + C::A_BYTES, bks, 128);
+      const uint64_t bl = umma_desc(base + C::A_BYTES + C::B_PART, bks, 128);
+#pragma unroll
       for (int rb = 0; rb < NRB; ++rb) {
-        const int i0 = rb * 128 + 32 * q4;
-#pragma unroll 1
-        for (int c0 = 0; c0 < T5_N; c0 += 16) {
-          uint32_t v[16];
+        const uint64_t ah = umma_desc(base + rb * 2 * T5_PART, ks, 128);
+        const uint64_t al = umma_desc(base + rb * 2 * T5_PART + T5_PART, ks, 128);
+        const uint64_t ad[3] = {al, ah, ah}, bd[3] = {bh, bl, bh};
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+          const uint32_t acc = (c > 0 || t > 0) ? 1u : 0u;
           asm volatile(
-              "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-              "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-              : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
-                "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
-                "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-              : "r"(tmem + ((uint32_t)(32 * q4) << 16) +
-                    (uint32_t)(ab * C::ACC_COLS + rb * T5_N + c0)));
-          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-          for (int q = 0; q < 16; ++q) tt[q * 32 + lane] = __uint_as_float(v[q]);
-          __syncwarp();
-#pragma unroll
-          for (int r = 0; r < 4; ++r) {
-            const int q = r * 4 + (lane >> 3), g4 = (lane & 7) * 4;
-            const int tgt = tg[c0 + q];
-            if (tgt >= 0 && i0 + g4 < ncheb) {
-              const float4 a = *reinterpret_cast<const float4 *>(&tt[q * 32 + g4]);
-              float *dst = G32 + (size_t)tgt * ldg + i0 + g4;
-              asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst), "f"(a.x),
-                           "f"(a.y), "f"(a.z), "f"(a.w)
-                           : "memory");
-            }
-          }
-          __syncwarp();
+              "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+              "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(
+                  tmem + (uint32_t)(rb * T5_N)),
+              "l"(ad[t]), "l"(bd[t]), "r"(idesc), "r"(acc));
         }
       }
-      // this warp has read its lanes of the set: once all four have, the
-      // MMA issuer may overwrite it
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncwarp();
-      if (lane == 0) mbar_arrive(smem_addr(&accempty[ab]));
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_addr(&empty[st])));
     }
-    if (!ok && lane == 0) *abort_flag = 1;
+    // completes once every MMA issued above has completed
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_addr(accb)));
+    sInfo[1] = c;
+    if (!ok) sInfo[3] = 0;
   }
   __syncthreads();
-  if (tid == 0) {
-    // every MMA of the CTA has completed before TMEM is released and the
-    // CTA exits (the final commit's arrival must not outlive the CTA)
-    const bool done = mbar_wait(smem_addr(mmadone), 0, limit_ns);
-    if (*abort_flag || !done) {
+  const bool acc_ready = mbar_wait(smem_addr(accb), 0, limit_ns);
+  const bool ok = __syncthreads_and(acc_ready && sInfo[2] && sInfo[3] && sInfo[1] == nkb);
+  if (!ok) {
+    if (tid == 0) {
       atomicExch(status, 1);
-      // bulk copies issued but never taken by the MMA issuer complete before
-      // shared memory is released (bounded waits)
+      // the MMAs issued so far (accb) and the bulk copies still in flight
+      // (fullA) complete before TMEM and shared memory are released; each of
+      // these waits is bounded as well
+      if (!acc_ready) mbar_wait(smem_addr(accb), 0, limit_ns);
       for (int q = sInfo[1]; q < sInfo[0]; ++q)
-        mbar_wait(smem_addr(&fullA[q % SA]), (q / SA) & 1, limit_ns);
+        mbar_wait(smem_addr(&fullA[q % S]), (q / S) & 1, limit_ns);
+    }
+    __syncthreads();
+  } else {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // per warp a 16 x 32 transpose tile in the (now idle) first stage: lane
+    // = row on the way in, (pair, 4 consecutive rows) on the way out, so that
+    // G receives 16-byte vector reductions (ldg and the row groups are
+    // multiples of 4; groups at or beyond ncheb are skipped)
+    float *tt = reinterpret_cast<float *>(sm) + warp * (16 * 32);
+#pragma unroll 1
+    for (int rb = 0; rb < NRB; ++rb) {
+      const int i0 = rb * 128 + 32 * warp;
+#pragma unroll 1
+      for (int c0 = 0; c0 < T5_N; c0 += 16) {
+        uint32_t v[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+            "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+              "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+              "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+            : "r"(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(rb * T5_N + c0)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int q = 0; q < 16; ++q) tt[q * 32 + lane] = __uint_as_float(v[q]);
+        __syncwarp();
+#pragma unroll
+        for (int it = 0; it < 4; ++it) {
+          const int q = it * 4 + (lane >> 3), g = (lane & 7) * 4;
+          const int tgt = sTgt[c0 + q];
+          if (tgt >= 0 && i0 + g < ncheb) {
+            const float4 a = *reinterpret_cast<const float4 *>(&tt[q * 32 + g]);
+            float *dst = G32 + (size_t)tgt * ldg + i0 + g;
+            asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst), "f"(a.x),
+                         "f"(a.y), "f"(a.z), "f"(a.w)
+                         : "memory");
+          }
+        }
+        __syncwarp();
+      }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -1653,13 +1520,10 @@ int fmm_matvec_device(abx_operator *op, const double *b, double *c) {
         auto launch_tc5 = [&](auto kern, size_t smem) -> int {
           ABX_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)smem));
-          // persistent: one CTA per SM (shared memory admits no second one)
-          const int grid = std::min(P->ntiles, p->ctx->num_sms);
-          kern<<<grid, T5_THREADS, smem, s>>>(nc, nkb, ldk, ldg, P->ntiles, P->Kp.ptr,
-                                              P->m2l_by_mat.ptr, P->mat_off_d.ptr,
-                                              P->tile_mat.ptr, P->tile_first.ptr, P->W32.ptr,
-                                              P->W32l.ptr, P->G32.ptr, status,
-                                              (uint64_t)(P->wait_limit_s * 1e9), P->drop_arrive);
+          kern<<<P->ntiles, 128, smem, s>>>(nc, nkb, ldk, ldg, P->Kp.ptr, P->m2l_by_mat.ptr,
+                                            P->mat_off_d.ptr, P->tile_mat.ptr, P->tile_first.ptr,
+                                            P->W32.ptr, P->W32l.ptr, P->G32.ptr, status,
+                                            (uint64_t)(P->wait_limit_s * 1e9), P->drop_arrive);
           return ABX_OK;
         };
         switch (nrb) {

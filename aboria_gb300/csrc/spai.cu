@@ -100,6 +100,7 @@ constexpr int LS_T = 256;
 constexpr int LS_HT = 8192;   // hash slots
 constexpr int LS_MCAP = 3072; // max |U|
 constexpr int LS_K = 32;
+constexpr int LS_LOCAL_T = 256;  // local mode: 8 rows (warps) per block
 
 struct LsParams {
   int dim, kind;
@@ -324,6 +325,118 @@ template <int KIND> __global__ void __launch_bounds__(LS_T) k_spai_ls(LsParams P
   }
 }
 
+// Local mode (U = S, the k x k system of the row's support) with one warp
+// per row: lane c holds column c of B, B(u, c) = coeff(S[c], S[u]), in
+// registers, and lane u the rhs entry e_u.  The same Householder QR with
+// column pivoting as k_spai_ls (pivot: the first column of largest norm over
+// the remaining rows; stop at a norm <= 1e-13 |R00|), then the back
+// substitution over the rank; the Householder vector passes through a
+// per-warp shared-memory row.
+template <int KIND> __global__ void __launch_bounds__(LS_LOCAL_T) k_spai_local(LsParams P) {
+  constexpr int WPB = LS_LOCAL_T / 32;
+  __shared__ double vsh[WPB][LS_K];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int k = P.k;
+  double *v = vsh[wib];
+  for (int64_t r = (int64_t)blockIdx.x * WPB + wib; r < P.nrows; r += (int64_t)gridDim.x * WPB) {
+    const int64_t i = P.subset ? P.subset[r] : r;
+    const int s = lane < k ? P.knn[i * k + lane] : -1;
+    double col[LS_K];
+#pragma unroll
+    for (int u = 0; u < LS_K; ++u) {
+      const int su = __shfl_sync(0xffffffffu, s, u);
+      col[u] = (s >= 0 && su >= 0) ? ls_coeff<KIND>(P, s, su) : 0.0;
+    }
+    double eu = (s >= 0 && s == i) ? 1.0 : 0.0;
+    int perm = lane;
+    int rank = k;
+    double r00 = 0.0;
+    for (int j = 0; j < k; ++j) {
+      // norms of the remaining columns over rows j..k-1
+      double cn = 0.0;
+#pragma unroll
+      for (int u = 0; u < LS_K; ++u)
+        if (u >= j) cn = fma(col[u], col[u], cn);
+      double bv = (lane >= j && lane < k) ? cn : -1.0;
+      int bl = lane;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        const int ol = __shfl_xor_sync(0xffffffffu, bl, o);
+        if (ov > bv || (ov == bv && ol < bl)) {
+          bv = ov;
+          bl = ol;
+        }
+      }
+      const int p = bl;
+      if (p != j) {  // swap columns j and p (and their permutation entries)
+        const int src = lane == j ? p : (lane == p ? j : lane);
+#pragma unroll
+        for (int u = 0; u < LS_K; ++u) col[u] = __shfl_sync(0xffffffffu, col[u], src);
+        perm = __shfl_sync(0xffffffffu, perm, src);
+      }
+      const double nrm = sqrt(bv);
+      if (j == 0) r00 = nrm;
+      if (nrm <= 1e-13 * r00 || nrm == 0.0) {
+        rank = j;
+        break;
+      }
+      // Householder vector of column j (rows j..k-1): v = x - alpha e_j
+      if (lane == j) {
+#pragma unroll
+        for (int u = 0; u < LS_K; ++u) v[u] = u >= j ? col[u] : 0.0;
+      }
+      __syncwarp();
+      const double x0 = v[j];
+      const double alpha = x0 > 0 ? -nrm : nrm;
+      __syncwarp();
+      if (lane == 0) v[j] = x0 - alpha;
+      __syncwarp();
+      double vv = 0.0;
+#pragma unroll
+      for (int u = 0; u < LS_K; ++u)
+        if (u >= j) vv = fma(v[u], v[u], vv);
+      const double tau = vv > 0 ? 2.0 / vv : 0.0;
+      // apply to the columns j+1..k-1 and to e
+      if (lane > j && lane < k) {
+        double d = 0.0;
+#pragma unroll
+        for (int u = 0; u < LS_K; ++u)
+          if (u >= j) d = fma(v[u], col[u], d);
+        const double f = tau * d;
+#pragma unroll
+        for (int u = 0; u < LS_K; ++u)
+          if (u >= j) col[u] = fma(-f, v[u], col[u]);
+      }
+      double se = lane >= j ? v[lane] * eu : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) se += __shfl_xor_sync(0xffffffffu, se, o);
+      if (lane >= j) eu = fma(-tau * se, v[lane], eu);
+      if (lane == j) {
+#pragma unroll
+        for (int u = 0; u < LS_K; ++u)
+          if (u == j) col[u] = alpha;
+      }
+      __syncwarp();
+    }
+    // back substitution R w = (Q^T e) over the first `rank` columns: lane c
+    // holds R(0..c, c) in col[0..c], lane j holds (Q^T e)_j in eu
+    double w = 0.0;
+    for (int j = rank - 1; j >= 0; --j) {
+      double rjc = 0.0;
+#pragma unroll
+      for (int u = 0; u < LS_K; ++u)
+        if (u == j) rjc = col[u];
+      double t = (lane > j && lane < rank) ? rjc * w : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      const double ej = __shfl_sync(0xffffffffu, eu, j);
+      if (lane == j) w = (ej - t) / rjc;
+    }
+    if (lane < k) P.vals[i * k + perm] = lane < rank ? w : 0.0;
+  }
+}
+
 }  // namespace
 
 // Exact least-squares SPAI rows for the sparse operator `op` (rows == cols)
@@ -350,8 +463,9 @@ struct PhaseEvents {
   void mark(int i) {
     if (ok) ok = cudaEventRecord(e[i], s) == cudaSuccess;
   }
-  // after the stream has been synchronised past mark(4)
+  // once mark(4) has been recorded
   void elapsed(double out[4]) {
+    if (ok) ok = cudaEventSynchronize(e[4]) == cudaSuccess;
     for (int i = 0; i < 4; ++i) {
       float ms = 0.0f;
       const bool got = ok && cudaEventElapsedTime(&ms, e[i], e[i + 1]) == cudaSuccess;
@@ -385,7 +499,7 @@ int spai_exact_rows(abx_operator *op, int k, int32_t *cols_out, double *vals_out
   const int grid = (int)std::min<int64_t>(nrows, (int64_t)ctx->num_sms * 2);
   DevBuf<double> scratch;
   DevBuf<int> flags;
-  ABX_TRY(scratch.reserve((size_t)grid * LS_MCAP * LS_K));
+  if (!local) ABX_TRY(scratch.reserve((size_t)grid * LS_MCAP * LS_K));
   ABX_TRY(flags.reserve(2));
   ABX_CHECK_CUDA(cudaMemsetAsync(flags.ptr, 0, 2 * sizeof(int), s));
   LsParams P{};
@@ -416,13 +530,31 @@ int spai_exact_rows(abx_operator *op, int k, int32_t *cols_out, double *vals_out
     kern<<<grid, LS_T, LS_SMEM, s>>>(P);
     return ABX_OK;
   };
-  switch (P.kind) {
-  case ABX_K_CONST: ABX_TRY(launch(k_spai_ls<ABX_K_CONST>)); break;
-  case ABX_K_GAUSSIAN: ABX_TRY(launch(k_spai_ls<ABX_K_GAUSSIAN>)); break;
-  case ABX_K_WENDLAND_C2: ABX_TRY(launch(k_spai_ls<ABX_K_WENDLAND_C2>)); break;
-  case ABX_K_COMPACT_GAUSSIAN: ABX_TRY(launch(k_spai_ls<ABX_K_COMPACT_GAUSSIAN>)); break;
-  case ABX_K_LAPLACE: ABX_TRY(launch(k_spai_ls<ABX_K_LAPLACE>)); break;
-  case ABX_K_MULTIQUADRIC: ABX_TRY(launch(k_spai_ls<ABX_K_MULTIQUADRIC>)); break;
+  // local mode: a warp per row, every SM kept full
+  const int lgrid = (int)std::min<int64_t>((nrows + LS_LOCAL_T / 32 - 1) / (LS_LOCAL_T / 32),
+                                           (int64_t)ctx->num_sms * 8);
+  auto launch_local = [&](auto kern) -> int {
+    kern<<<lgrid, LS_LOCAL_T, 0, s>>>(P);
+    return ABX_OK;
+  };
+  if (local) {
+    switch (P.kind) {
+    case ABX_K_CONST: ABX_TRY(launch_local(k_spai_local<ABX_K_CONST>)); break;
+    case ABX_K_GAUSSIAN: ABX_TRY(launch_local(k_spai_local<ABX_K_GAUSSIAN>)); break;
+    case ABX_K_WENDLAND_C2: ABX_TRY(launch_local(k_spai_local<ABX_K_WENDLAND_C2>)); break;
+    case ABX_K_COMPACT_GAUSSIAN: ABX_TRY(launch_local(k_spai_local<ABX_K_COMPACT_GAUSSIAN>)); break;
+    case ABX_K_LAPLACE: ABX_TRY(launch_local(k_spai_local<ABX_K_LAPLACE>)); break;
+    case ABX_K_MULTIQUADRIC: ABX_TRY(launch_local(k_spai_local<ABX_K_MULTIQUADRIC>)); break;
+    }
+  } else {
+    switch (P.kind) {
+    case ABX_K_CONST: ABX_TRY(launch(k_spai_ls<ABX_K_CONST>)); break;
+    case ABX_K_GAUSSIAN: ABX_TRY(launch(k_spai_ls<ABX_K_GAUSSIAN>)); break;
+    case ABX_K_WENDLAND_C2: ABX_TRY(launch(k_spai_ls<ABX_K_WENDLAND_C2>)); break;
+    case ABX_K_COMPACT_GAUSSIAN: ABX_TRY(launch(k_spai_ls<ABX_K_COMPACT_GAUSSIAN>)); break;
+    case ABX_K_LAPLACE: ABX_TRY(launch(k_spai_ls<ABX_K_LAPLACE>)); break;
+    case ABX_K_MULTIQUADRIC: ABX_TRY(launch(k_spai_ls<ABX_K_MULTIQUADRIC>)); break;
+    }
   }
   ABX_CHECK_CUDA(cudaGetLastError());
   int st[2];

@@ -538,9 +538,10 @@ def rbf_case(ctx, models, dim, n, dist, eh, seed, plain=True, fallback=True, max
 def rbf_grid_section(ctx, models, quick=False, budget_s=900.0):
     """The RBF solve over dimension x N x point distribution x eps*h, and the
     fallback rate of the learned preconditioner over instances with eps*h
-    drawn per instance.  Uniform points at N = 50k, 500k, 2M (2-D, and 3-D
-    from eps*h = 1); the 8-Gaussian mixtures at N = 50k only: their clusters
-    are ~100x denser than h, so at larger N the FP64 operator alone holds
+    drawn per instance.  Uniform points at N = 50k (eps*h from 0.75 in 2-D,
+    from 1 in 3-D), 500k and 2M (eps*h 1.5, 2.5); the 8-Gaussian mixtures at
+    N = 50k only (eps*h 1.5 and 2.5 in 2-D, 2.5 in 3-D): their clusters are
+    ~100x denser than h, so at larger N the FP64 operator alone holds
     thousands of neighbours per row.  Plain Schwarz/FP64 is run where its FP64
     block LU takes seconds (2-D N <= 500k, 3-D N = 50k); larger cells report
     the approximate inverses without the Schwarz fallback.  Mixture systems
@@ -552,21 +553,17 @@ def rbf_grid_section(ctx, models, quick=False, budget_s=900.0):
         cells = [(2, 200_000, "uniform", eh, True, True) for eh in (1.5, 2.5)]
         cells += [(3, 50_000, "uniform", eh, True, True) for eh in (1.5, 2.5)]
     else:
-        cells = []
-        for eh in RBF_GRID_EH:
-            cells.append((2, 50_000, "uniform", eh, True, True))
-        for eh in RBF_GRID_EH[1:]:
-            cells.append((3, 50_000, "uniform", eh, True, True))
-            cells.append((2, 50_000, "mixture", eh, True, True))
-            cells.append((3, 50_000, "mixture", eh, True, True))
-        for eh in RBF_GRID_EH:
-            cells.append((2, 500_000, "uniform", eh, True, True))
-        for eh in RBF_GRID_EH[1:]:
-            cells.append((3, 500_000, "uniform", eh, False, False))
-        for eh in RBF_GRID_EH:
-            cells.append((2, 2_000_000, "uniform", eh, False, False))
-        for eh in RBF_GRID_EH[1:]:
-            cells.append((3, 2_000_000, "uniform", eh, False, False))
+        cells = [(2, 50_000, "uniform", eh, True, True) for eh in RBF_GRID_EH]
+        cells += [(3, 50_000, "uniform", eh, True, True) for eh in RBF_GRID_EH[1:]]
+        cells += [(2, 50_000, "mixture", eh, True, True) for eh in RBF_GRID_EH[2:]]
+        cells += [(3, 50_000, "mixture", RBF_GRID_EH[-1], True, True)]
+        # at N >= 500k the smaller eps*h need more than the mixed operator's
+        # precision gives (the learned and the identity rows stall); the
+        # cells there take eps*h = 1.5 and 2.5
+        for n in (500_000, 2_000_000):
+            for eh in RBF_GRID_EH[2:]:
+                cells.append((2, n, "uniform", eh, n <= 500_000, n <= 500_000))
+                cells.append((3, n, "uniform", eh, False, False))
     out = {"cells": []}
 
     def over_budget():

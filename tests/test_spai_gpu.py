@@ -86,3 +86,33 @@ def test_exact_spai_preconditions_gmres():
     x, it, res = ab.gmres(K, b, M=M, restart=100, max_iters=400, tol=1e-8)
     assert res <= 1e-8
     assert it < it_plain
+
+
+@pytest.mark.parametrize("eh", [2.5, 1.0])
+def test_local_inverse_rows_vs_numpy(eh):
+    """Local mode (one warp per row): the row solves the k x k system of its
+    own k-NN support, A(S, S) w = e_0 -- the exact rows of the learned
+    preconditioner.  Against numpy's least-squares solution of the same
+    system on sampled rows, including rows next to a near-coincident point
+    (eps*h = 1: the local matrices are ill-conditioned, so the check there is
+    the residual of the system rather than the weights)."""
+    n = 3000
+    pos = workloads.uniform(n, 2, seed=89)
+    eps = eh * np.sqrt(n)
+    r = 4.0 / eps
+    p = ab.Particles(2).set(pos)
+    p.init_octree([0, 0], [1, 1], [False, False], 64)
+    K = ab.create_sparse_operator(p, p, r, ab.Kernel.make(ab.K_COMPACT_GAUSSIAN, eps * eps))
+    cols, vals = ab.spai_local_inverse_rows(K, 32)
+    A = dense_kernel(p.positions, r, eps * eps)
+    rng = np.random.default_rng(90)
+    for i in rng.choice(n, 60, replace=False):
+        S = cols[i]
+        assert S[0] == i
+        B = A[np.ix_(S, S)]
+        e = (S == i).astype(float)
+        w = np.linalg.lstsq(B, e, rcond=None)[0]
+        res = np.linalg.norm(B @ vals[i] - e)
+        assert res <= 1e-9 * max(1.0, np.linalg.norm(vals[i])), (i, res)
+        if np.linalg.cond(B) < 1e8:
+            assert np.linalg.norm(vals[i] - w) / np.linalg.norm(w) < 1e-8, i
