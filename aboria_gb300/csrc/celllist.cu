@@ -47,6 +47,8 @@ constexpr int CL_TILE = 16384;                         // keys per sort tile
 constexpr int SW_TPB = 512;                            // sort-pass threads per block
 constexpr int SW_WARPS = SW_TPB / 32;
 constexpr int SW_ROUNDS = CL_TILE / (SW_TPB * CL_ITEMS);  // rounds of 16 keys per thread
+static_assert(CL_TILE % (SW_TPB * CL_ITEMS) == 0 && (1 << 10) % SW_TPB == 0 && CL_TILE <= 65535,
+              "sort tile shape (16-bit counts, whole digits per thread)");
 constexpr int CL_BND_SMEM = 4096;  // boundary entries staged in shared memory (32 KB)
 constexpr int CL_KEYS_TILE = 4096;                     // particles per keys-kernel step
 constexpr int CL_RB = 10;
