@@ -815,6 +815,7 @@ class GMRES {
 
 #ifdef __CUDACC__
 #include "functor_operator.cuh"
+#include "symbolic.cuh"
 #endif
 
 #endif  // ABORIA_GB_ABORIA_H_

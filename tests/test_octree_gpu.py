@@ -37,3 +37,30 @@ def test_octree_sparse_operator_works():
     ref = oracle.sparse_matvec(cl, p.positions, 0.05, ab.K_COMPACT_GAUSSIAN, [400.0], b[cl.perm])
     c = K * b
     assert np.linalg.norm(c - ref) / np.linalg.norm(ref) < 1e-12
+
+
+@pytest.mark.parametrize("dim,periodic,lnorm", [(3, False, 2), (2, True, 2), (3, True, -1),
+                                                (2, False, 1)])
+def test_radius_queries_on_the_octree(dim, periodic, lnorm):
+    """The reference's HyperOctree answers the same radius queries as its cell
+    lists (tree_query_iterator, src/NeighbourSearchBase.h:1438-1718).  On an
+    octree particle set the GPU search gives the oracle's neighbour counts
+    and sets, bit-exact, for stored and foreign query points; columns are
+    storage indices of the octree order."""
+    pos = workloads.uniform(20000, dim, seed=60 + dim)
+    lo, hi, per = [0.0] * dim, [1.0] * dim, [periodic] * dim
+    p = ab.Particles(dim).set(pos)
+    p.init_octree(lo, hi, per, 32)
+    cl = oracle.celllist_build(p.positions, lo, hi, per)
+    q = np.concatenate([p.positions[:2000],
+                        workloads.uniform(500, dim, lo=-0.1, hi=1.1, seed=70 + dim)])
+    r = 0.05 if dim == 3 else 0.02
+    counts = ab.radius_count(p, q, r, lnorm=lnorm)
+    assert np.array_equal(counts, oracle.radius_count(cl, q, r, lnorm))
+    rowptr, cols = ab.radius_query_csr(p, q, r, lnorm=lnorm)
+    orp, ocols, _ = oracle.radius_lists(cl, q, r, lnorm=lnorm)
+    assert np.array_equal(rowptr, orp)
+    for i in range(len(q)):
+        a = np.sort(cols[rowptr[i]:rowptr[i + 1]])
+        b = np.sort(cl.perm[ocols[orp[i]:orp[i + 1]]])
+        assert np.array_equal(a, b), i
