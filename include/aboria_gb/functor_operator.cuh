@@ -195,7 +195,11 @@ struct ConstRadius {
   template <typename R> __host__ __device__ double operator()(const R &) const { return r; }
 };
 
-template <unsigned D, bool REFS, typename RowRef, typename ColRef, typename F, typename RF>
+// NORM: the search norm, 2 euclidean (accumulate dx^2, compare with r^2), 1
+// manhattan (accumulate |dx|), -1 chebyshev (max |dx|), compared with r
+// (src/detail/Distance.h:46-137)
+template <unsigned D, bool REFS, typename RowRef, typename ColRef, typename F, typename RF,
+          int NORM = 2>
 __global__ void functor_sparse_walk(RowRef rbase, ColRef cbase, CellGrid g, F f, RF rf,
                                     const double *__restrict__ b, double *__restrict__ c,
                                     int64_t nrows) {
@@ -209,7 +213,7 @@ __global__ void functor_sparse_walk(RowRef rbase, ColRef cbase, CellGrid g, F f,
   double xi[D];
   for (unsigned d = 0; d < D; ++d) xi[d] = a.pos[d * a.n + i];
   const double r = rf(a);
-  const double r2 = r * r;  // get_value_to_accumulate(r) = pow(r, 2)
+  const double r2 = NORM == 2 ? r * r : r;  // get_value_to_accumulate(r)
   // buckets that may hold a neighbour (one extra bucket each side covers the
   // rounding of the bucket assignment), images -1, 0, +1
   int ulo[3] = {0, 0, 0}, uhi[3] = {0, 0, 0};
@@ -258,7 +262,12 @@ __global__ void functor_sparse_walk(RowRef rbase, ColRef cbase, CellGrid g, F f,
       double acc2 = 0.0;
       for (unsigned d = 0; d < D; ++d) {
         dx[d] = __dsub_rn(cbase.pos[d * cbase.n + j], cur[d]);
-        acc2 = __dadd_rn(acc2, __dmul_rn(dx[d], dx[d]));
+        if (NORM == 2)
+          acc2 = __dadd_rn(acc2, __dmul_rn(dx[d], dx[d]));
+        else if (NORM == 1)
+          acc2 = __dadd_rn(acc2, fabs(dx[d]));
+        else
+          acc2 = fmax(acc2, fabs(dx[d]));
       }
       if (!(acc2 > r2)) {
         ColRef bj = cbase;
@@ -299,7 +308,8 @@ __global__ void functor_dense(RowRef rbase, ColRef cbase, F f, const double *__r
 
 /* The operator of a user closure; K * b like Aboria::Operator.  It refers to
  * its particle sets, which must outlive it (src/Kernels.h:133-135). */
-template <typename RowP, typename ColP, typename F, typename RF, bool DENSE> class FunctorOperator {
+template <typename RowP, typename ColP, typename F, typename RF, bool DENSE, int NORM = 2>
+class FunctorOperator {
   static constexpr unsigned D = RowP::dimension;
   typedef typename RowP::const_reference RowRef;
   typedef typename ColP::const_reference ColRef;
@@ -342,8 +352,9 @@ template <typename RowP, typename ColP, typename F, typename RF, bool DENSE> cla
                                                                                  c, nr, nc);
     } else {
       const detail::CellGrid g = detail::cell_grid(cols_->handle(), nc);
-      detail::functor_sparse_walk<D, REFS><<<(unsigned)((nr * 32 + threads - 1) / threads),
-                                             threads>>>(a, bref, g, f_, rf_, b, c, nr);
+      detail::functor_sparse_walk<D, REFS, RowRef, ColRef, F, RF, NORM>
+          <<<(unsigned)((nr * 32 + threads - 1) / threads), threads>>>(a, bref, g, f_, rf_, b, c,
+                                                                      nr);
     }
     detail::check_cuda(cudaGetLastError(), "user-functor operator launch");
   }
@@ -387,9 +398,9 @@ template <typename RowP, typename ColP, typename F, typename RF, bool DENSE> cla
     const ColRef bref = detail::device_ref(*cols_);
     const detail::CellGrid g = detail::cell_grid(cols_->handle(), nc);
     const int threads = 256;
-    detail::functor_sparse_walk<D, false><<<(unsigned)((nr * 32 + threads - 1) / threads),
-                                            threads>>>(a, bref, g, detail::CountPair{}, rf_,
-                                                       ones.ptr, cnt.ptr, nr);
+    detail::functor_sparse_walk<D, false, RowRef, ColRef, detail::CountPair, RF, NORM>
+        <<<(unsigned)((nr * 32 + threads - 1) / threads), threads>>>(
+            a, bref, g, detail::CountPair{}, rf_, ones.ptr, cnt.ptr, nr);
     detail::check_cuda(cudaGetLastError(), "pair count launch");
     std::vector<double> c(static_cast<size_t>(nr));
     detail::check_cuda(cudaMemcpy(c.data(), cnt.ptr, size_t(nr) * 8, cudaMemcpyDeviceToHost),

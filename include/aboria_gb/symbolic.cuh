@@ -24,9 +24,13 @@
  * the host column of the assigned variable.  A value is a double or a
  * Vector<double, N>; integer accumulations are carried in double.
  *
- * Not covered: nested sums inside an expression, sums over labels other
- * than the assigned row label and the column label, min/max accumulations,
- * the reference's geometry functions beyond norm.
+ * eval(sum(i, x)) sums over the row particles a per-particle value x, itself
+ * a sum over j or an expression of i.  AccumulateWithinDistance<std::plus<T>,
+ * LNorm>(r) sums over the neighbours within r in the 2-, 1- or inf-norm.
+ *
+ * Not covered: a sum inside an arithmetic expression, sums over labels other
+ * than the row label and the column label, min/max accumulations, the
+ * reference's geometry functions beyond norm.
  */
 #ifndef ABORIA_GB_SYMBOLIC_CUH_
 #define ABORIA_GB_SYMBOLIC_CUH_
@@ -275,6 +279,15 @@ template <typename P, typename T, typename C, typename E> struct Sum {
   E e;
   bool within;
   double r;
+  int lnorm;  // within: the search norm (2, 1 or -1)
+};
+
+// sum over the row label i of a per-particle value (a Sum over j or an
+// expression of i), for eval(...)
+template <typename P, typename T, typename C, typename X> struct SumAll {
+  const P *rows;
+  C c;
+  X x;
 };
 
 // A particle reference to the host columns (positions copied to SoA), for
@@ -329,6 +342,47 @@ sym::IfElse<sym::expr_t<C>, sym::expr_t<X>, sym::expr_t<Y>> if_else(const C &c, 
 }
 
 /* Accumulate<std::plus<T>> (src/Symbolic.h): sum(j, cond, expr). */
+namespace sym {
+template <typename T> struct is_sum : std::false_type {};
+template <typename P, typename T, typename C, typename E>
+struct is_sum<Sum<P, T, C, E>> : std::true_type {};
+
+// sum over j for every row particle: n x BR values (BR = 1 for a double)
+template <int NORM, typename P, typename Q, typename F>
+void run_sparse(const P &rows, const Q &cols, double r, const F &f, const double *ones, double *c) {
+  const FunctorOperator<P, Q, F, detail::ConstRadius, false, NORM> op(rows, cols,
+                                                                     detail::ConstRadius{r}, f);
+  op.apply(ones, c);
+}
+template <typename P, typename Q, typename T, typename C, typename E>
+std::vector<double> sum_values(const P &rows, const Sum<Q, T, C, E> &s) {
+  typedef PairTerm<T, C, E> F;
+  typedef radius_of<C> RO;
+  const F f{s.c, s.e};
+  const size_t n = rows.size(), nc = s.cols->size();
+  constexpr unsigned BR = detail::BlockRows<T>::value;
+  std::vector<double> c(n * BR, 0.0);
+  if (n == 0 || nc == 0) return c;
+  std::vector<double> ones(nc, 1.0);
+  if (s.within || RO::sparse) {
+    const double r = s.within ? s.r : RO::get(s.c);
+    if (s.within && s.lnorm == 1)
+      run_sparse<1>(rows, *s.cols, r, f, ones.data(), c.data());
+    else if (s.within && s.lnorm == -1)
+      run_sparse<-1>(rows, *s.cols, r, f, ones.data(), c.data());
+    else
+      run_sparse<2>(rows, *s.cols, r, f, ones.data(), c.data());
+  } else {
+    const auto op = create_dense_operator(rows, *s.cols, f);
+    op.apply(ones.data(), c.data());
+  }
+  return c;
+}
+}  // namespace sym
+
+/* Accumulate<std::plus<T>> (src/Symbolic.h): sum(j, cond, expr) or
+ * sum(j, expr) over the column label; sum(i, expr) / sum(i, cond, expr)
+ * over the row label, evaluated with eval(...). */
 template <typename Functor> struct Accumulate;
 template <typename T> struct Accumulate<std::plus<T>> {
   typedef typename sym::acc_value<T>::type value_type;
@@ -336,23 +390,73 @@ template <typename T> struct Accumulate<std::plus<T>> {
   sym::Sum<Q, value_type, sym::expr_t<C>, sym::expr_t<E>> operator()(const Label<1, Q> &j,
                                                                      const C &cond,
                                                                      const E &e) const {
-    return {j.p, sym::make_expr(cond), sym::make_expr(e), false, 0.0};
+    return {j.p, sym::make_expr(cond), sym::make_expr(e), false, 0.0, 2};
+  }
+  template <typename Q, typename E>
+  sym::Sum<Q, value_type, sym::Lit<bool>, sym::expr_t<E>> operator()(const Label<1, Q> &j,
+                                                                     const E &e) const {
+    return {j.p, sym::Lit<bool>{{}, true}, sym::make_expr(e), false, 0.0, 2};
+  }
+  template <typename P, typename C, typename X>
+  sym::SumAll<P, value_type, sym::expr_t<C>, X> operator()(const Label<0, P> &i, const C &cond,
+                                                            const X &x) const {
+    return {i.p, sym::make_expr(cond), x};
+  }
+  template <typename P, typename X>
+  sym::SumAll<P, value_type, sym::Lit<bool>, X> operator()(const Label<0, P> &i,
+                                                            const X &x) const {
+    return {i.p, sym::Lit<bool>{{}, true}, x};
   }
 };
 
-/* AccumulateWithinDistance<std::plus<T>>(r) (src/Symbolic.h): sum(j, expr)
- * over the neighbours found by a search of radius r (inclusive). */
-template <typename Functor> struct AccumulateWithinDistance;
-template <typename T> struct AccumulateWithinDistance<std::plus<T>> {
+/* AccumulateWithinDistance<std::plus<T>, LNorm>(r) (src/Symbolic.h):
+ * sum(j, expr) over the neighbours found by a search of radius r in the
+ * LNorm norm (2 euclidean, 1 manhattan, -1 chebyshev; inclusive). */
+template <typename Functor, int LNorm = 2> struct AccumulateWithinDistance;
+template <typename T, int LNorm> struct AccumulateWithinDistance<std::plus<T>, LNorm> {
+  static_assert(LNorm == 2 || LNorm == 1 || LNorm == -1, "norm 2, 1 or -1");
   typedef typename sym::acc_value<T>::type value_type;
   double radius;
   explicit AccumulateWithinDistance(double r) : radius(r) {}
   template <typename Q, typename E>
   sym::Sum<Q, value_type, sym::Lit<bool>, sym::expr_t<E>> operator()(const Label<1, Q> &j,
                                                                      const E &e) const {
-    return {j.p, sym::Lit<bool>{{}, true}, sym::make_expr(e), true, radius};
+    return {j.p, sym::Lit<bool>{{}, true}, sym::make_expr(e), true, radius, LNorm};
   }
 };
+
+/* eval(sum(i, [cond,] x)) (src/Symbolic.h): the sum over the row particles,
+ * in storage order, of x -- a sum over j or an expression of i. */
+template <typename P, typename T, typename C, typename X>
+T eval(const sym::SumAll<P, T, C, X> &s) {
+  constexpr unsigned BR = detail::BlockRows<T>::value;
+  const size_t n = s.rows->size();
+  std::vector<double> vals(n * BR, 0.0);
+  const sym::HostRef<P> h(*s.rows);
+  typename P::const_reference a = h.ref;
+  const Vector<double, P::dimension> zero;
+  if constexpr (sym::is_sum<X>::value) {
+    vals = sym::sum_values(*s.rows, s.x);
+  } else {
+    const auto x = sym::make_expr(s.x);
+    for (size_t i = 0; i < n; ++i) {
+      a.index = int64_t(i);
+      const T v = T(x.eval(zero, a, a));
+      for (unsigned k = 0; k < BR; ++k) vals[i * BR + k] = detail::BlockRows<T>::get(v, k);
+    }
+  }
+  T total = T();
+  for (size_t i = 0; i < n; ++i) {
+    a.index = int64_t(i);
+    if (!s.c.eval(zero, a, a)) continue;
+    if constexpr (BR == 1) {
+      total = total + vals[i];
+    } else {
+      for (unsigned k = 0; k < BR; ++k) total[k] = total[k] + vals[i * BR + k];
+    }
+  }
+  return total;
+}
 
 /* s[i] as the target of an assignment, s[i] / s[j] inside an expression */
 template <typename Tag, int L, typename P> struct SymbolAt : sym::VarAt<Tag, L> {
@@ -398,22 +502,9 @@ template <typename Tag, int L, typename P> struct SymbolAt : sym::VarAt<Tag, L> 
   template <typename Q, typename T, typename C, typename E>
   void assign(const sym::Sum<Q, T, C, E> &s, bool add) const {
     static_assert(L == 0, "assign to the row label (label 0)");
-    typedef sym::PairTerm<T, C, E> F;
-    typedef sym::radius_of<C> RO;
-    const F f{s.c, s.e};
-    const size_t n = p->size(), nc = s.cols->size();
-    std::vector<double> ones(nc, 1.0);
+    const size_t n = p->size();
     constexpr unsigned BR = detail::BlockRows<T>::value;
-    std::vector<double> c(n * BR, 0.0);
-    if (n && nc) {
-      if (s.within || RO::sparse) {
-        const auto op = create_sparse_operator(*p, *s.cols, s.within ? s.r : RO::get(s.c), f);
-        op.apply(ones.data(), c.data());
-      } else {
-        const auto op = create_dense_operator(*p, *s.cols, f);
-        op.apply(ones.data(), c.data());
-      }
-    }
+    const std::vector<double> c = sym::sum_values(*p, s);
     auto &col = detail::getter<Tag>::get(const_cast<P &>(*p));
     typedef typename std::decay<decltype(col[0])>::type V;
     for (size_t i = 0; i < n; ++i) {

@@ -8,6 +8,7 @@
 //   symbolic_test run IN OUT      random particles from IN (n, r, then n x 3
 //                                 positions), writes OUT/{ids,count,spring,
 //                                 dense}.bin for the Python test's brute force
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -68,11 +69,41 @@ static int kat() {
   if (get<scalar>(particles)[0] != 2) return fail("s[0] = sum(b, 1) again", get<scalar>(particles)[0], 2);
   if (get<scalar>(particles)[1] != 2) return fail("s[1] = sum(b, 1) again", get<scalar>(particles)[1], 2);
 
+  Accumulate<std::plus<double>> sum_all;
+  const double sum_of_sum = eval(sum_all(a, sum(b, 1.0)));
+  if (sum_of_sum != 4) return fail("eval(sum_all(a, sum(b, 1.0)))", sum_of_sum, 4);
+
   p[a] = if_else(id_[a] == 0, vdouble3(0, 0, 0),
                  vdouble3(diameter / 2.0, diameter / 2.0, diameter / 2.0));
   s[a] = if_else(id_[a] == 0, 0, 1);
   if (get<scalar>(particles)[0] != 0) return fail("s = if_else(...)[0]", get<scalar>(particles)[0], 0);
   if (get<scalar>(particles)[1] != 1) return fail("s = if_else(...)[1]", get<scalar>(particles)[1], 1);
+
+  AccumulateWithinDistance<std::plus<vdouble3>> sumVect(diameter);
+  Accumulate<std::plus<vdouble3>> sum_all_vect;
+  const vdouble3 sum_of_sumv =
+      eval(sum_all_vect(a, sumVect(b, vdouble3(0, 0, 0) + 0.5 * (s[a] / 2.0 + s[b] / 10.0))));
+  for (int d = 0; d < 3; ++d)
+    if (std::fabs(sum_of_sumv[d] - 0.6) > 10 * 2.220446049250313e-16)
+      return fail("eval(sum_all_vect(...))", sum_of_sumv[d], 0.6);
+  p[a] = sumVect(b, vdouble3(0, 0, 0) + 0.5 * (s[a] / 2.0 + s[b] / 10.0));
+  const double want2[2] = {0.05, 0.55};
+  for (int i = 0; i < 2; ++i)
+    for (int d = 0; d < 3; ++d)
+      if (get<position>(particles)[i][d] != want2[i])
+        return fail("p[a] = sumVect(b, ...)", get<position>(particles)[i][d], want2[i]);
+
+  // the inf-norm range sum
+  AccumulateWithinDistance<std::plus<double>, -1> box_sum(diameter);
+  get<position>(particles)[0] = vdouble3(0, 0, 0);
+  get<position>(particles)[1] = vdouble3(0.99 * diameter, 0.99 * diameter, 0.99 * diameter);
+  particles.update_positions();
+  s[a] = sum(b, 1);
+  if (get<scalar>(particles)[0] != 1) return fail("s = sum(b, 1), 2-norm", get<scalar>(particles)[0], 1);
+  if (get<scalar>(particles)[1] != 1) return fail("s = sum(b, 1), 2-norm", get<scalar>(particles)[1], 1);
+  s[a] = box_sum(b, 1);
+  if (get<scalar>(particles)[0] != 2) return fail("s = box_sum(b, 1)", get<scalar>(particles)[0], 2);
+  if (get<scalar>(particles)[1] != 2) return fail("s = box_sum(b, 1)", get<scalar>(particles)[1], 2);
   std::printf("kat ok\n");
   return 0;
 }

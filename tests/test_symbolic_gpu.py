@@ -4,8 +4,10 @@ include/aboria_gb/symbolic.cuh, in a program built by nvcc
 
 * CPU: the program compiles and links against the library.
 * GPU: the known answers of the reference's tests/symbolic.h
-  helper_neighbours (AccumulateWithinDistance sums, univariate if_else and
-  arithmetic assignments to positions and variables, a periodic domain), and
+  helper_neighbours (AccumulateWithinDistance sums in the 2- and inf-norm,
+  univariate if_else and arithmetic assignments to positions and variables,
+  eval of a sum over i of sums over j, scalar and vector, in a periodic
+  domain), and
   on 20,000 random particles the neighbour count sum(j, norm(dx) < r, 1), the
   linear-spring sum of tests/speed_test.h:756-836 (the self pair taken out
   with if_else) and a dense sum(j, true, ...) against an FP64 brute force.
