@@ -29,7 +29,7 @@ __all__ = [
     "K_MULTIQUADRIC", "K_SCALAR_SUM", "default_context", "Preconditioner",
     "schwarz_preconditioner", "spai_preconditioner", "gmres", "knn", "spai_exact_rows", "MLP",
     "spai_features", "learned_preconditioner", "spai_local_inverse_rows", "create_fmm_operator", "fmm_stats", "spai_rows", "gmres_with_fallback",
-    "fp32_peak_tflops", "fmm_set_wait_limit", "create_h2_operator",
+    "fp32_peak_tflops", "fmm_set_wait_limit", "create_h2_operator", "radius_query_csr_transform",
 ]
 
 PREC_FP64, PREC_MIXED = 0, 1
@@ -258,6 +258,27 @@ def radius_query_csr(p: Particles, q, r: float, lnorm: int = 2, with_dx: bool = 
     _check(lib().abx_radius_query_csr_lnorm(p._h, nq, _ptr(q), float(r), int(lnorm), _ptr(rowptr),
                                             _ptr(cols), nnz), "abx_radius_query_csr")
     return rowptr, cols[:nnz]
+
+
+def radius_query_csr_transform(p: Particles, q, r: float, T):
+    """``euclidean_search(query, x, r, transform)`` with a linear transform
+    (``create_linear_transform`` / ``create_scale_transform``) given as its
+    dim x dim matrix T: CSR ``(rowptr, cols, dx)``, dx the transformed
+    separations T (x_j - x - image*L) of the neighbours."""
+    nq = int(q.shape[0])
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    T = np.ascontiguousarray(T, dtype=np.float64).reshape(p.dim, p.dim)
+    rowptr = np.empty(nq + 1, dtype=np.int64)
+    _check(lib().abx_radius_query_csr_transform(p._h, nq, _ptr(q), float(r), _ptr(T),
+                                                _ptr(rowptr), None, None, 0),
+           "abx_radius_query_csr_transform")
+    nnz = int(rowptr[-1])
+    cols = np.empty(max(nnz, 1), dtype=np.int32)
+    dx = np.empty((max(nnz, 1), p.dim), dtype=np.float64)
+    _check(lib().abx_radius_query_csr_transform(p._h, nq, _ptr(q), float(r), _ptr(T),
+                                                _ptr(rowptr), _ptr(cols), _ptr(dx), nnz),
+           "abx_radius_query_csr_transform")
+    return rowptr, cols[:nnz], dx[:nnz]
 
 
 class Kernel(C.Structure):

@@ -1680,6 +1680,161 @@ int abx_radius_query_csr_lnorm(abx_particles *p, int64_t nq, const double *q, do
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
+// Searches in a linearly transformed coordinate system (euclidean_search with
+// a LinearTransform / ScaleTransform, src/Transform.h, src/Search.h:438-445):
+// a particle is a neighbour iff !(|T dx|^2 > r^2), dx = x_j - (x + image*L).
+// The candidates come from the ordinary search at radius r / sigma_min(T)
+// (every point with |T dx| <= r has |dx| <= r / sigma_min), widened by 1e-9
+// relative; the transformed test then runs on the device per candidate.
+namespace abx {
+namespace {
+struct TMat {
+  double m[9];  // row-major D x D
+};
+
+// (T dx)_i = ((T_i0 dx_0 + T_i1 dx_1) + T_i2 dx_2); accum = ((0 + y_0^2) + y_1^2) + y_2^2
+__device__ __forceinline__ bool tf_inside(const double *dx, int D, const TMat &T, double r2,
+                                          double *y) {
+  double acc = 0.0;
+  for (int i = 0; i < D; ++i) {
+    double v = 0.0;
+    for (int k = 0; k < D; ++k) v = __dadd_rn(v, __dmul_rn(T.m[i * D + k], dx[k]));
+    y[i] = v;
+    acc = __dadd_rn(acc, __dmul_rn(v, v));
+  }
+  return !(acc > r2);
+}
+
+__global__ void k_tf_count(const int64_t *__restrict__ rp, const double *__restrict__ dx,
+                           int64_t nq, int D, TMat T, double r2, int64_t *__restrict__ cnt) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  int64_t c = 0;
+  double y[3];
+  for (int64_t e = rp[i]; e < rp[i + 1]; ++e) c += tf_inside(dx + e * D, D, T, r2, y) ? 1 : 0;
+  cnt[i] = c;
+}
+
+__global__ void k_tf_fill(const int64_t *__restrict__ rp, const int32_t *__restrict__ cols,
+                          const double *__restrict__ dx, int64_t nq, int D, TMat T, double r2,
+                          const int64_t *__restrict__ orp, int32_t *__restrict__ ocols,
+                          double *__restrict__ odx) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  int64_t o = orp[i];
+  double y[3];
+  for (int64_t e = rp[i]; e < rp[i + 1]; ++e) {
+    if (!tf_inside(dx + e * D, D, T, r2, y)) continue;
+    ocols[o] = cols[e];
+    if (odx)
+      for (int d = 0; d < D; ++d) odx[o * D + d] = y[d];
+    ++o;
+  }
+}
+
+// smallest singular value of the D x D matrix T: the square root of the
+// smallest eigenvalue of T^T T, by cyclic Jacobi rotations
+double sigma_min(const double *T, int D) {
+  double A[3][3] = {};
+  for (int i = 0; i < D; ++i)
+    for (int j = 0; j < D; ++j)
+      for (int k = 0; k < D; ++k) A[i][j] += T[k * D + i] * T[k * D + j];
+  for (int sweep = 0; sweep < 64; ++sweep) {
+    double off = 0.0;
+    for (int i = 0; i < D; ++i)
+      for (int j = i + 1; j < D; ++j) off += A[i][j] * A[i][j];
+    if (off <= 1e-300) break;
+    for (int p = 0; p < D; ++p)
+      for (int q = p + 1; q < D; ++q) {
+        if (A[p][q] == 0.0) continue;
+        const double th = 0.5 * (A[q][q] - A[p][p]) / A[p][q];
+        const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < D; ++k) {  // A <- A J
+          const double akp = A[k][p], akq = A[k][q];
+          A[k][p] = c * akp - s * akq;
+          A[k][q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < D; ++k) {  // A <- J^T A
+          const double apk = A[p][k], aqk = A[q][k];
+          A[p][k] = c * apk - s * aqk;
+          A[q][k] = s * apk + c * aqk;
+        }
+      }
+  }
+  double lmin = A[0][0];
+  for (int i = 1; i < D; ++i) lmin = std::min(lmin, A[i][i]);
+  return lmin > 0 ? std::sqrt(lmin) : 0.0;
+}
+}  // namespace
+}  // namespace abx
+
+extern "C" int abx_radius_query_csr_transform(abx_particles *p, int64_t nq, const double *q,
+                                              double r, const double *T, int64_t *rowptr,
+                                              int32_t *cols, double *dx, int64_t cap) {
+  ABX_REQUIRE(p && (q || nq == 0) && rowptr && T, ABX_ERR_INVALID, "null argument");
+  ABX_REQUIRE(r >= 0 && std::isfinite(r), ABX_ERR_INVALID, "invalid radius");
+  ABX_TRY(ctx_activate(p->ctx));
+  const int D = p->dim;
+  TMat tm{};
+  for (int k = 0; k < D * D; ++k) {
+    ABX_REQUIRE(std::isfinite(T[k]), ABX_ERR_INVALID, "transform entries must be finite");
+    tm.m[k] = T[k];
+  }
+  const double smin = sigma_min(T, D);
+  ABX_REQUIRE(smin > 0 && std::isfinite(r / smin), ABX_ERR_INVALID,
+              "the transform must be invertible (smallest singular value %g)", smin);
+  const double R = r / smin * (1.0 + 1e-9);
+  abx_context *ctx = p->ctx;
+  cudaStream_t s = ctx->stream;
+  // candidates: CSR with the accepted image's dx, on the device
+  std::vector<int64_t> hc(nq + 1);
+  ABX_TRY(radius_query(p, nq, q, R, nullptr, hc.data(), nullptr, 0, 2));
+  const int64_t nc = hc[nq];
+  DevBuf<int64_t> crp, cnt, orp;
+  DevBuf<int32_t> ccols;
+  DevBuf<double> cdx;
+  ABX_TRY(crp.reserve(nq + 1));
+  ABX_TRY(cnt.reserve(nq + 1));
+  ABX_TRY(ccols.reserve(nc + 1));
+  ABX_TRY(cdx.reserve((size_t)(nc + 1) * D));
+  ABX_TRY(radius_query(p, nq, q, R, nullptr, crp.ptr, ccols.ptr, nc, 2, cdx.ptr));
+  if (nq)
+    k_tf_count<<<ceil_div(nq, TPB), TPB, 0, s>>>(crp.ptr, cdx.ptr, nq, D, tm, r * r, cnt.ptr);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  std::vector<int64_t> h(nq + 1);
+  if (nq) ABX_CHECK_CUDA(cudaMemcpyAsync(h.data(), cnt.ptr, nq * 8, cudaMemcpyDeviceToHost, s));
+  ABX_CHECK_CUDA(cudaStreamSynchronize(s));
+  int64_t run = 0;
+  for (int64_t i = 0; i < nq; ++i) {
+    const int64_t c = h[i];
+    h[i] = run;
+    run += c;
+  }
+  h[nq] = run;
+  ABX_CHECK_CUDA(cudaMemcpy(rowptr, h.data(), (nq + 1) * 8, cudaMemcpyDefault));
+  if (!cols) return ABX_OK;
+  ABX_REQUIRE(cap >= run, ABX_ERR_CAPACITY, "cols capacity %lld < nnz %lld", (long long)cap,
+              (long long)run);
+  DevBuf<int32_t> ocols;
+  DevBuf<double> odx;
+  ABX_TRY(ocols.reserve(run + 1));
+  if (dx) ABX_TRY(odx.reserve((size_t)(run + 1) * D));
+  ABX_TRY(orp.reserve(nq + 1));
+  ABX_CHECK_CUDA(cudaMemcpyAsync(orp.ptr, h.data(), (nq + 1) * 8, cudaMemcpyHostToDevice, s));
+  if (nq)
+    k_tf_fill<<<ceil_div(nq, TPB), TPB, 0, s>>>(crp.ptr, ccols.ptr, cdx.ptr, nq, D, tm, r * r,
+                                                 orp.ptr, ocols.ptr, dx ? odx.ptr : nullptr);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  if (run) {
+    ABX_CHECK_CUDA(cudaMemcpyAsync(cols, ocols.ptr, run * 4, cudaMemcpyDefault, s));
+    if (dx) ABX_CHECK_CUDA(cudaMemcpyAsync(dx, odx.ptr, (size_t)run * D * 8, cudaMemcpyDefault, s));
+  }
+  ABX_CHECK_CUDA(cudaStreamSynchronize(s));
+  return ABX_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Allocation-free sparse matvec (abx_operator_matvec_noalloc).
 //
 // Some callers cannot call cudaMalloc while they apply an operator: code that

@@ -6,7 +6,8 @@
  *     push_back, size, init_neighbour_search, update_positions, get<position>,
  *     get<id>
  *   CellListOrdered / HyperOctree (search-method tags)       src/CellListOrdered.h, src/OctTree.h
- *   euclidean_search(query, x, r)                            src/Search.h:839-845
+ *   euclidean_search(query, x, r[, transform])               src/Search.h:839-845,
+ *     create_linear_transform, create_scale_transform         src/Transform.h
  *   create_sparse_operator / create_dense_operator /
  *   create_fmm_operator<N>                                   src/Operators.h:312-515
  *   K * b on any contiguous double vector (Eigen::VectorXd, std::vector<double>)
@@ -513,6 +514,64 @@ std::vector<SearchResult<P::dimension>> euclidean_search(const P &particles,
   if (nnz)
     detail::check(abx_radius_query_csr_dx(particles.handle(), 1, x.data(), r, rowptr, cols.data(),
                                           dx.data(), rowptr[1]),
+                  "euclidean_search");
+  for (size_t k = 0; k < nnz; ++k) {
+    SearchResult<D> s;
+    s.index = cols[k];
+    for (unsigned d = 0; d < D; ++d) s.dx[d] = dx[k * D + d];
+    out.push_back(s);
+  }
+  return out;
+}
+
+/* Linear coordinate transforms for the searches (src/Transform.h): the
+ * transform's D x D matrix, column k = f(e_k) of the user's linear map f
+ * (exact for the reference's maps whose coefficients multiply single
+ * coordinates: the matrix form adds the other coordinates times zero). */
+template <unsigned int D> struct LinearTransformMatrix {
+  double m[D * D];  // row-major
+};
+template <unsigned int D, typename F> LinearTransformMatrix<D> create_linear_transform(const F &f) {
+  LinearTransformMatrix<D> t;
+  for (unsigned k = 0; k < D; ++k) {
+    Vector<double, D> e;
+    e[k] = 1.0;
+    const Vector<double, D> col = f(e);
+    for (unsigned i = 0; i < D; ++i) t.m[i * D + k] = col[i];
+  }
+  return t;
+}
+/* create_scale_transform(s): x_d -> s_d x_d */
+template <unsigned int D> LinearTransformMatrix<D> create_scale_transform(const Vector<double, D> &s) {
+  LinearTransformMatrix<D> t;
+  for (unsigned i = 0; i < D * D; ++i) t.m[i] = 0.0;
+  for (unsigned i = 0; i < D; ++i) t.m[i * D + i] = s[i];
+  return t;
+}
+
+/* euclidean_search(query, x, r, transform) (src/Search.h:839-845 with a
+ * LinearTransform): the neighbours with |T dx| <= r; dx is returned
+ * transformed, as the reference's dx() is (abx_radius_query_csr_transform). */
+template <typename P>
+std::vector<SearchResult<P::dimension>> euclidean_search(
+    const P &particles, const typename P::double_d &x, double r,
+    const LinearTransformMatrix<P::dimension> &transform) {
+  constexpr unsigned D = P::dimension;
+  std::vector<SearchResult<D>> out;
+  if (!particles.searched()) {
+    detail::check(ABX_ERR_STATE, "euclidean_search before init_neighbour_search");
+    return out;
+  }
+  int64_t rowptr[2] = {0, 0};
+  detail::check(abx_radius_query_csr_transform(particles.handle(), 1, x.data(), r, transform.m,
+                                               rowptr, nullptr, nullptr, 0),
+                "euclidean_search");
+  const size_t nnz = static_cast<size_t>(rowptr[1]);
+  std::vector<int32_t> cols(nnz);
+  std::vector<double> dx(nnz * D);
+  if (nnz)
+    detail::check(abx_radius_query_csr_transform(particles.handle(), 1, x.data(), r, transform.m,
+                                                 rowptr, cols.data(), dx.data(), rowptr[1]),
                   "euclidean_search");
   for (size_t k = 0; k < nnz; ++k) {
     SearchResult<D> s;

@@ -192,6 +192,18 @@ ABX_API int abx_radius_count_lnorm(abx_particles *p, int64_t nq, const double *q
                                    int lnorm, int32_t *counts);
 ABX_API int abx_radius_query_csr_lnorm(abx_particles *p, int64_t nq, const double *q, double r,
                                        int lnorm, int64_t *rowptr, int32_t *cols, int64_t cap);
+/* euclidean_search in a linearly transformed coordinate system
+ * (LinearTransform / ScaleTransform, src/Transform.h; the search iterator's
+ * m_dx = transform(p - x), src/Search.h:438-445): T is the row-major dim x dim
+ * matrix of the transform, y = T dx evaluated as ((T_i0 dx_0 + T_i1 dx_1) +
+ * T_i2 dx_2), and a particle is a neighbour iff !(((0 + y_0^2) + y_1^2) +
+ * y_2^2 > r^2).  rowptr[nq+1] as abx_radius_query_csr; cols (may be NULL:
+ * counts only) and dx[nnz*dim] (may be NULL) receive the neighbours and
+ * their TRANSFORMED separations, as the reference's dx() returns them.  T
+ * must be invertible. */
+ABX_API int abx_radius_query_csr_transform(abx_particles *p, int64_t nq, const double *q,
+                                           double r, const double *T, int64_t *rowptr,
+                                           int32_t *cols, double *dx, int64_t cap);
 
 /* k nearest neighbours of every stored particle among the stored particles
  * (itself included, FP64 distances with periodic images, ties by storage

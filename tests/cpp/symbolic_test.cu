@@ -104,6 +104,32 @@ static int kat() {
   s[a] = box_sum(b, 1);
   if (get<scalar>(particles)[0] != 2) return fail("s = box_sum(b, 1)", get<scalar>(particles)[0], 2);
   if (get<scalar>(particles)[1] != 2) return fail("s = box_sum(b, 1)", get<scalar>(particles)[1], 2);
+
+  // tests/neighbours.h helper_single_particle: searches with a scale transform
+  {
+    typedef Particles<std::tuple<scalar>, 3> T1;
+    T1 test;
+    test.init_neighbour_search(vdouble3(-1, -1, -1), vdouble3(1, 1, 1), vbool3(true, true, true));
+    const double radius = 0.1;
+    test.push_back(vdouble3(0, 0, 0));
+    if (euclidean_search(test, vdouble3(radius / 2, radius / 2, 0), radius).size() != 1)
+      return fail("euclidean_search count", 0, 1);
+    if (euclidean_search(test, vdouble3(2 * radius, 0, 0), radius).size() != 0)
+      return fail("euclidean_search count far", 1, 0);
+    const auto scale = create_scale_transform(vdouble3(1.0 / radius, 1.0 / radius, 1.0 / radius));
+    if (euclidean_search(test, vdouble3(radius / 2, radius / 2, 0), 1.0, scale).size() != 1)
+      return fail("scaled euclidean_search count", 0, 1);
+    if (euclidean_search(test, vdouble3(2 * radius, 0, 0), 1.0, scale).size() != 0)
+      return fail("scaled euclidean_search count far", 1, 0);
+    struct Skew {
+      vdouble3 operator()(const vdouble3 &v) const { return vdouble3(v[0] + 0.3 * v[1], v[1], v[2]); }
+    };
+    const auto skew = create_linear_transform<3>(Skew());
+    // (0.05, 0.2, 0) from the particle: |skew dx| = |(0.11, 0.2, 0)| < 0.25 < |dx| * 1.2
+    const auto hits = euclidean_search(test, vdouble3(-0.05, -0.2, 0), 0.25, skew);
+    if (hits.size() != 1) return fail("skewed euclidean_search count", double(hits.size()), 1);
+    if (hits[0].dx[0] != 0.05 + 0.3 * 0.2) return fail("skewed dx", hits[0].dx[0], 0.05 + 0.3 * 0.2);
+  }
   std::printf("kat ok\n");
   return 0;
 }
