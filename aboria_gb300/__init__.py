@@ -29,7 +29,7 @@ __all__ = [
     "K_MULTIQUADRIC", "K_SCALAR_SUM", "default_context", "Preconditioner",
     "schwarz_preconditioner", "spai_preconditioner", "gmres", "knn", "spai_exact_rows", "MLP",
     "spai_features", "learned_preconditioner", "spai_local_inverse_rows", "create_fmm_operator", "fmm_stats", "spai_rows", "gmres_with_fallback",
-    "fp32_peak_tflops", "fmm_set_wait_limit", "create_h2_operator", "radius_query_csr_transform",
+    "fp32_peak_tflops", "fmm_set_wait_limit", "create_h2_operator", "radius_query_csr_transform", "radius_pairs",
 ]
 
 PREC_FP64, PREC_MIXED = 0, 1
@@ -258,6 +258,21 @@ def radius_query_csr(p: Particles, q, r: float, lnorm: int = 2, with_dx: bool = 
     _check(lib().abx_radius_query_csr_lnorm(p._h, nq, _ptr(q), float(r), int(lnorm), _ptr(rowptr),
                                             _ptr(cols), nnz), "abx_radius_query_csr")
     return rowptr, cols[:nnz]
+
+
+def radius_pairs(p: Particles, r: float):
+    """Every pair within r once (the neighbouring-bucket pair sweep):
+    ``(i, j, dx)`` with i < j storage indices, dx = x_j - (x_i + image*L)."""
+    n = C.c_int64()
+    _check(lib().abx_radius_pairs(p._h, float(r), C.byref(n), None, None, None, 0),
+           "abx_radius_pairs")
+    m = n.value
+    i = np.empty(max(m, 1), dtype=np.int32)
+    j = np.empty(max(m, 1), dtype=np.int32)
+    dx = np.empty((max(m, 1), p.dim), dtype=np.float64)
+    _check(lib().abx_radius_pairs(p._h, float(r), C.byref(n), _ptr(i), _ptr(j), _ptr(dx), m),
+           "abx_radius_pairs")
+    return i[:m], j[:m], dx[:m]
 
 
 def radius_query_csr_transform(p: Particles, q, r: float, T):

@@ -1769,6 +1769,112 @@ double sigma_min(const double *T, int D) {
 }  // namespace
 }  // namespace abx
 
+// Unique pairs within r of one particle set: the pairs a sweep over
+// neighbouring buckets visits (bucket_pair_iterator, src/Search.h:498-764,
+// together with the pairs inside each bucket), each once -- (i, j) with i < j
+// in storage order, dx = x_j - (x_i + image*L) of the accepted image and
+// !(|dx|^2 > r^2) -- from the self search's CSR, filtered on the device.
+namespace abx {
+namespace {
+__global__ void k_soa_to_aos(const double *__restrict__ soa, int64_t n, int dim,
+                             double *__restrict__ aos) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int d = 0; d < dim; ++d) aos[i * dim + d] = soa[(int64_t)d * n + i];
+}
+
+__global__ void k_upper_count(const int64_t *__restrict__ rp, const int32_t *__restrict__ cols,
+                              int64_t n, int64_t *__restrict__ cnt) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int64_t c = 0;
+  for (int64_t e = rp[i]; e < rp[i + 1]; ++e) c += cols[e] > i ? 1 : 0;
+  cnt[i] = c;
+}
+
+__global__ void k_upper_fill(const int64_t *__restrict__ rp, const int32_t *__restrict__ cols,
+                             const double *__restrict__ dx, int64_t n, int D,
+                             const int64_t *__restrict__ orp, int32_t *__restrict__ oi,
+                             int32_t *__restrict__ oj, double *__restrict__ odx) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int64_t o = orp[i];
+  for (int64_t e = rp[i]; e < rp[i + 1]; ++e) {
+    if (cols[e] <= i) continue;
+    oi[o] = (int32_t)i;
+    oj[o] = cols[e];
+    if (odx)
+      for (int d = 0; d < D; ++d) odx[o * D + d] = dx[e * D + d];
+    ++o;
+  }
+}
+}  // namespace
+}  // namespace abx
+
+extern "C" int abx_radius_pairs(abx_particles *p, double r, int64_t *npairs, int32_t *pi,
+                                int32_t *pj, double *dx, int64_t cap) {
+  ABX_REQUIRE(p && npairs, ABX_ERR_INVALID, "null argument");
+  ABX_REQUIRE(r >= 0 && std::isfinite(r), ABX_ERR_INVALID, "invalid radius");
+  ABX_REQUIRE(p->searchable, ABX_ERR_STATE, "init_neighbour_search not called on this particle set");
+  ABX_TRY(ctx_activate(p->ctx));
+  abx_context *ctx = p->ctx;
+  cudaStream_t s = ctx->stream;
+  const int64_t n = p->n;
+  const int D = p->dim;
+  *npairs = 0;
+  if (n == 0) return ABX_OK;
+  DevBuf<double> aos;
+  ABX_TRY(aos.reserve((size_t)n * D));
+  k_soa_to_aos<<<ceil_div(n, TPB), TPB, 0, s>>>(p->pos.ptr, n, D, aos.ptr);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  std::vector<int64_t> hc(n + 1);
+  ABX_TRY(radius_query(p, n, aos.ptr, r, nullptr, hc.data(), nullptr, 0, 2));
+  const int64_t nc = hc[n];
+  DevBuf<int64_t> crp, cnt, orp;
+  DevBuf<int32_t> ccols;
+  DevBuf<double> cdx;
+  ABX_TRY(crp.reserve(n + 1));
+  ABX_TRY(cnt.reserve(n + 1));
+  ABX_TRY(ccols.reserve(nc + 1));
+  if (dx) ABX_TRY(cdx.reserve((size_t)(nc + 1) * D));
+  ABX_TRY(radius_query(p, n, aos.ptr, r, nullptr, crp.ptr, ccols.ptr, nc, 2,
+                       dx ? cdx.ptr : nullptr));
+  k_upper_count<<<ceil_div(n, TPB), TPB, 0, s>>>(crp.ptr, ccols.ptr, n, cnt.ptr);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  std::vector<int64_t> h(n + 1);
+  ABX_CHECK_CUDA(cudaMemcpyAsync(h.data(), cnt.ptr, n * 8, cudaMemcpyDeviceToHost, s));
+  ABX_CHECK_CUDA(cudaStreamSynchronize(s));
+  int64_t run = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t c = h[i];
+    h[i] = run;
+    run += c;
+  }
+  h[n] = run;
+  *npairs = run;
+  if (!pi) return ABX_OK;
+  ABX_REQUIRE(pj, ABX_ERR_INVALID, "pi and pj are both given or both NULL");
+  ABX_REQUIRE(cap >= run, ABX_ERR_CAPACITY, "pair capacity %lld < %lld pairs", (long long)cap,
+              (long long)run);
+  DevBuf<int32_t> oi, oj;
+  DevBuf<double> odx;
+  ABX_TRY(oi.reserve(run + 1));
+  ABX_TRY(oj.reserve(run + 1));
+  if (dx) ABX_TRY(odx.reserve((size_t)(run + 1) * D));
+  ABX_TRY(orp.reserve(n + 1));
+  ABX_CHECK_CUDA(cudaMemcpyAsync(orp.ptr, h.data(), (n + 1) * 8, cudaMemcpyHostToDevice, s));
+  k_upper_fill<<<ceil_div(n, TPB), TPB, 0, s>>>(crp.ptr, ccols.ptr, dx ? cdx.ptr : nullptr, n, D,
+                                                orp.ptr, oi.ptr, oj.ptr, dx ? odx.ptr : nullptr);
+  ABX_CHECK_CUDA(cudaGetLastError());
+  if (run) {
+    ABX_CHECK_CUDA(cudaMemcpyAsync(pi, oi.ptr, run * 4, cudaMemcpyDefault, s));
+    ABX_CHECK_CUDA(cudaMemcpyAsync(pj, oj.ptr, run * 4, cudaMemcpyDefault, s));
+    if (dx) ABX_CHECK_CUDA(cudaMemcpyAsync(dx, odx.ptr, (size_t)run * D * 8, cudaMemcpyDefault, s));
+  }
+  ABX_CHECK_CUDA(cudaStreamSynchronize(s));
+  return ABX_OK;
+}
+
 extern "C" int abx_radius_query_csr_transform(abx_particles *p, int64_t nq, const double *q,
                                               double r, const double *T, int64_t *rowptr,
                                               int32_t *cols, double *dx, int64_t cap) {

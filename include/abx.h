@@ -204,6 +204,15 @@ ABX_API int abx_radius_query_csr_lnorm(abx_particles *p, int64_t nq, const doubl
 ABX_API int abx_radius_query_csr_transform(abx_particles *p, int64_t nq, const double *q,
                                            double r, const double *T, int64_t *rowptr,
                                            int32_t *cols, double *dx, int64_t cap);
+/* Every pair of stored particles within r, once: the pairs a sweep over the
+ * neighbouring buckets of the cell list visits (bucket_pair_iterator /
+ * get_neighbouring_buckets, src/Search.h:498-764, plus the pairs inside each
+ * bucket).  *npairs receives the count; pi, pj (both NULL: count only) and
+ * dx[npairs*dim] (may be NULL) receive the pairs as storage indices with
+ * pi < pj, in increasing pi, with dx = x_pj - (x_pi + image*L) of the image
+ * the search accepted and !(|dx|^2 > r^2).  cap: capacity of pi/pj. */
+ABX_API int abx_radius_pairs(abx_particles *p, double r, int64_t *npairs, int32_t *pi,
+                             int32_t *pj, double *dx, int64_t cap);
 
 /* k nearest neighbours of every stored particle among the stored particles
  * (itself included, FP64 distances with periodic images, ties by storage
