@@ -400,10 +400,12 @@ def rbf_section(ctx, model_path, dim=2, n=None, run_schwarz=True, seed=4040):
                 blocks factorised by FP64 LU, FP64 operator throughout.
     * learned : the trained MLP's sparse approximate inverse (32 k-NN columns
                 per row, BF16 tensor-core inference; rows next to a neighbour
-                with kernel value > 0.5 solved exactly in FP64), FP32 operator
-                with FP64 residual refinement; Schwarz taken as fallback when
-                the learned preconditioner has not converged after 100
-                iterations.
+                with kernel value > 0.5 solved exactly in FP64), FP64
+                operator (these systems hold 8-17 neighbours per row, so the
+                FP64 matvec is cheap, and with the mixed operator the
+                refinement against FP64 stalls at N >= 500k in 2-D);
+                Schwarz taken as fallback when the learned preconditioner
+                has not converged after 100 iterations.
     * without_network : the same, with identity rows where the network answers.
     * local_inverse : the exact FP64 local-inverse rows the network is trained
                 on, as the same sparse approximate inverse (the label method).
@@ -422,7 +424,6 @@ def rbf_section(ctx, model_path, dim=2, n=None, run_schwarz=True, seed=4040):
     f += 1e-3 * np.random.default_rng(seed + 1).standard_normal(n)
     kern = ab.Kernel.make(ab.K_COMPACT_GAUSSIAN, eps * eps)
     K64 = ab.create_sparse_operator(p, p, r, kern, ab.PREC_FP64)
-    K32 = ab.create_sparse_operator(p, p, r, kern, ab.PREC_MIXED)
     out = {"workload": f"{dim}-D N={n} uniform, compact Gaussian eps*h={RBF_EH} (eps={eps:.1f}), "
                        f"cut-off r=4/eps={r:.3g}, f=sin(4 pi x)cos(3 pi y)+1e-3 noise, GMRES(100), "
                        f"tol 1e-8 (FP64 residual)"}
@@ -443,31 +444,31 @@ def rbf_section(ctx, model_path, dim=2, n=None, run_schwarz=True, seed=4040):
         mlp = ab.MLP.load(model_path, ctx=ctx)
 
         def learned(net):
-            M = ab.learned_preconditioner(K32, net, eps, exact_phi=EXACT_PHI)
-            x, it, res, fb = ab.gmres_with_fallback(K32, f, M, K64, restart=100,
+            M = ab.learned_preconditioner(K64, net, eps, exact_phi=EXACT_PHI)
+            x, it, res, fb = ab.gmres_with_fallback(K64, f, M, K64, restart=100,
                                                     learned_max_iters=100, max_iters=2000,
                                                     tol=1e-8, A_check=K64)
             return x, it, fb, M.stats()["domains"]
         (x, it, fb, nex), t = _timed(lambda: learned(mlp), ctx)
-        out["learned_mixed"] = {"seconds": t, "iterations": it, "residual": check(x),
+        out["learned"] = {"seconds": t, "iterations": it, "residual": check(x),
                                 "fallback_taken": bool(fb), "rows_solved_exactly": nex}
         # the same method without the network: identity rows where it answers
         ident = ab.MLP.load(model_path, ctx=ctx)
         ident.params = np.zeros(ident.num_params, np.float32)
         (x, it, fb, nex), t = _timed(lambda: learned(ident), ctx)
-        out["without_network_mixed"] = {"seconds": t, "iterations": it, "residual": check(x),
+        out["without_network"] = {"seconds": t, "iterations": it, "residual": check(x),
                                         "fallback_taken": bool(fb)}
 
     def local_inverse():
         cols, vals = ab.spai_local_inverse_rows(K64, 32)
         M = ab.spai_preconditioner(ctx, cols, vals)
-        x, it, res = ab.gmres(K32, f, M=M, restart=100, max_iters=2000, tol=1e-8, A_check=K64)
+        x, it, res = ab.gmres(K64, f, M=M, restart=100, max_iters=2000, tol=1e-8)
         return x, it
     (x, it), t = _timed(local_inverse, ctx)
-    out["local_inverse_mixed"] = {"seconds": t, "iterations": it, "residual": check(x)}
-    if "learned_mixed" in out and "plain_schwarz_fp64" in out:
+    out["local_inverse"] = {"seconds": t, "iterations": it, "residual": check(x)}
+    if "learned" in out and "plain_schwarz_fp64" in out:
         out["speedup_learned_vs_plain"] = (out["plain_schwarz_fp64"]["seconds"]
-                                           / out["learned_mixed"]["seconds"])
+                                           / out["learned"]["seconds"])
     return out
 
 
@@ -480,7 +481,7 @@ def rbf_case(ctx, models, dim, n, dist, eh, seed, plain=True, fallback=True, max
     or 8 Gaussians of sigma 0.05 clipped into the unit box), compact Gaussian
     exp(-(eps |dx|)^2) cut at eps |dx| = 4, eps = eh * N^(1/dim), GMRES(100).
     Methods as in rbf_section: plain Schwarz/FP64; the learned approximate
-    inverse on the mixed operator (Schwarz fallback after 100 iterations when
+    inverse on the FP64 operator (Schwarz fallback after 100 iterations when
     ``fallback``; else its own result is reported, up to 300 iterations); the
     same without the network (identity rows where it answers).  Seconds
     include every set-up; the learned set-up is split into its phases."""
@@ -497,7 +498,6 @@ def rbf_case(ctx, models, dim, n, dist, eh, seed, plain=True, fallback=True, max
     f += 1e-3 * np.random.default_rng(seed + 1).standard_normal(n)
     kern = ab.Kernel.make(ab.K_COMPACT_GAUSSIAN, eps * eps)
     K64 = ab.create_sparse_operator(p, p, r, kern, ab.PREC_FP64)
-    K32 = ab.create_sparse_operator(p, p, r, kern, ab.PREC_MIXED)
     row = {"dim": dim, "n": n, "dist": dist, "eh": eh, "eps": eps, "seed": seed}
 
     def check(x):
@@ -519,15 +519,14 @@ def rbf_case(ctx, models, dim, n, dist, eh, seed, plain=True, fallback=True, max
         if name not in methods:
             continue
         def run(net=net):
-            M = ab.learned_preconditioner(K32, net, eps, exact_phi=EXACT_PHI)
+            M = ab.learned_preconditioner(K64, net, eps, exact_phi=EXACT_PHI)
             if fallback:
-                x, it, res, fb = ab.gmres_with_fallback(K32, f, M, K64, restart=100,
+                x, it, res, fb = ab.gmres_with_fallback(K64, f, M, K64, restart=100,
                                                         learned_max_iters=100,
                                                         max_iters=max_iters, tol=1e-8,
                                                         A_check=K64)
             else:
-                x, it, res = ab.gmres(K32, f, M=M, restart=100, max_iters=300, tol=1e-8,
-                                      A_check=K64)
+                x, it, res = ab.gmres(K64, f, M=M, restart=100, max_iters=300, tol=1e-8)
                 fb = False
             return x, it, fb, M.stats()
         (x, it, fb, st), t = _timed(run, ctx)
@@ -561,9 +560,8 @@ def rbf_grid_section(ctx, models, quick=False, budget_s=900.0):
         cells += [(3, 50_000, "uniform", eh, True, True) for eh in RBF_GRID_EH[1:]]
         cells += [(2, 50_000, "mixture", eh, True, True) for eh in RBF_GRID_EH[2:]]
         cells += [(3, 50_000, "mixture", RBF_GRID_EH[-1], True, True)]
-        # at N >= 500k the smaller eps*h need more than the mixed operator's
-        # precision gives (the learned and the identity rows stall); the
-        # cells there take eps*h = 1.5 and 2.5
+        # at N >= 500k the cells take eps*h = 1.5 and 2.5 (below, the
+        # approximate inverses stall and fall back to Schwarz)
         for n in (500_000, 2_000_000):
             for eh in RBF_GRID_EH[2:]:
                 cells.append((2, n, "uniform", eh, n <= 500_000, n <= 500_000))
